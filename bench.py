@@ -1,0 +1,355 @@
+"""Benchmark: 30-qubit random U3/CX brick circuit, gates/s and shots/s.
+
+Workload (one step): |0...0> on 30 qubits, 24 brick layers -- U3(theta, phi,
+lambda) on every qubit with angles uniform in [0, 2pi) from the seed, then CX
+on (2i, 2i+1) in even layers and (2i+1, 2i+2) in odd layers (1068 gates) --
+in complex64 with gates fused into blocks of <= 5 qubits, then 1,000,000
+Z-basis shots sampled from the final state.  The same circuit in plain
+complex128 mode (one gate per pass) is timed once beside it, and the fused
+complex64 result is compared with it on the device (1 - fidelity, max |d amp|,
+outcome TV).
+
+`value` = circuit gates / device time of the fused gate passes (state resident
+in HBM, 8 GiB > L2, so no flush is needed); `e2e` = the same metric through
+the public Circuit API with host matrices in and the classical results out.
+
+python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "30q random-circuit gates/s & %HBM peak, FP32-fused vs FP64 plain; shots/s"
+
+
+def brick_gates(n, depth, seed):
+    """(name, params, bits) of the U3/CX brick circuit."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for layer in range(depth):
+        for q in range(n):
+            out.append(("U3", [float(v) for v in rng.uniform(0.0, 2 * math.pi, 3)], [q]))
+        for q in range(0 if layer % 2 == 0 else 1, n - 1, 2):
+            out.append(("CX", [], [q, q + 1]))
+    return out
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(n_sample, depth_sample, seed, n_full):
+    """The oracle (single-threaded complex128 restatement of the reference's
+    algorithm) on the first `depth_sample` brick layers at `n_sample` qubits;
+    gates/s scaled to n_full qubits by 2^(n_sample - n_full), since every
+    gate touches all 2^n amplitudes."""
+    from oracle import oracle as orc
+    from q1tsim_gb300 import gates as G
+    gl = brick_gates(n_sample, depth_sample, seed)
+    mats = [(G.by_name(nm, p).matrix(), b) for nm, p, b in gl]
+    s = orc.OracleState.new(n_sample, 1)
+    t0 = time.perf_counter()
+    for m, b in mats:
+        s.apply_gate(m, b)
+    dt = time.perf_counter() - t0
+    rate = len(mats) / dt
+    return {"value": rate * 2.0 ** (n_sample - n_full), "unit": "gates/s", "cores": 1, "kind": "port",
+            "sample": f"oracle (reference algorithm, 1 thread) on {depth_sample} brick layers = {len(mats)} gates "
+                      f"at {n_sample} qubits in {dt:.2f} s ({rate:.2f} gates/s), scaled by 2^({n_sample}-{n_full})"}
+
+
+def run_reference(args, rank, world):
+    """Reference arm: the reference's CPU algorithm (the oracle port: the Rust
+    reference cannot be built on this image) on the host cores."""
+    if rank != 0:
+        return
+    from oracle import oracle as orc
+    from q1tsim_gb300 import gates as G
+    n_s, depth_s = args.cpu_qubits, 1
+    gl = brick_gates(n_s, depth_s, args.seed)
+    mats = [(G.by_name(nm, p).matrix(), b) for nm, p, b in gl]
+
+    def step():
+        s = orc.OracleState.new(n_s, 1)
+        for m, b in mats:
+            s.apply_gate(m, b)
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = time.perf_counter() - t0
+    rate = args.steps * len(mats) / dt * 2.0 ** (n_s - args.qubits)
+    sample = (f"oracle (reference algorithm, 1 thread; the reference is single-threaded) per step: "
+              f"1 brick layer = {len(mats)} gates at {n_s} qubits; gates/s scaled to {args.qubits} qubits "
+              f"by 2^({n_s}-{args.qubits})")
+    line = {"metric": METRIC, "impl": "reference", "value": rate, "unit": "gates/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": f"random U3/CX brick circuit, {args.qubits} qubits, "
+                                                        f"depth {args.depth}", "qubits": args.qubits},
+            "cpu_baseline": {"value": rate, "unit": "gates/s", "cores": 1, "kind": "port", "sample": sample},
+            "e2e": {"value": rate, "unit": "gates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--qubits", type=int, default=30)
+    ap.add_argument("--depth", type=int, default=24)
+    ap.add_argument("--shots", type=int, default=1_000_000)
+    ap.add_argument("--fusion", type=int, default=5)
+    ap.add_argument("--seed", type=int, default=20240601)
+    ap.add_argument("--no-plain", action="store_true", help="skip the complex128 comparison run")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--cpu-qubits", type=int, default=22)
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+
+    from q1tsim_gb300 import Circuit, Plan, Rng, VectorState
+    from q1tsim_gb300 import gates as G
+
+    n, shots = args.qubits, args.shots
+    gl = brick_gates(n, args.depth, args.seed + rank)
+    gates = [(G.by_name(nm, p), b) for nm, p, b in gl]
+    bits = [b for _, b in gates]
+    mats = np.concatenate([np.ascontiguousarray(g.matrix()).ravel() for g, _ in gates]).view(np.float64)
+    ngates = len(gates)
+
+    stream = torch.cuda.Stream()
+    fused = VectorState(n, shots, "c64")
+    fused.set_stream(stream.cuda_stream)
+    plan = Plan(n, bits, args.fusion)
+    res = np.zeros(shots, dtype=np.uint64)
+    cbits = list(range(n))
+
+    def gate_step():
+        fused.reset_all()
+        fused.apply_plan(plan, mats)
+
+    def shot_step():
+        fused.peek_all_into(cbits, res, rng=Rng(args.seed + 7))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(max(args.warmup, 1)):
+        gate_step()
+        shot_step()
+    barrier()
+
+    # ---- gates: K device-resident circuit runs, CUDA events on the stream
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        with torch.cuda.stream(stream):
+            ev0.record(stream)
+            for _ in range(args.steps):
+                gate_step()
+            ev1.record(stream)
+        barrier()
+    gate_ms = ev0.elapsed_time(ev1)
+    # ---- shots: K samplings of 1e6 shots from the resident state
+    barrier()
+    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s0.record(stream)
+    t_host = time.perf_counter()
+    for _ in range(args.steps):
+        shot_step()
+    s1.record(stream)
+    barrier()
+    shot_wall = time.perf_counter() - t_host
+    shot_ms = s0.elapsed_time(s1)
+
+    t = torch.tensor([gate_ms, shot_wall * 1e3], dtype=torch.float64, device="cuda")
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    gate_ms_max, shot_ms_max = float(t[0]), float(t[1])
+    value = world * args.steps * ngates / (gate_ms_max / 1e3)
+    shots_per_s = world * args.steps * shots / (shot_ms_max / 1e3)
+
+    # ---- per-kernel profile of one step (CUDA events around every launch)
+    fused.profile(True)
+    fused.profile_report(reset=True)
+    gate_step()
+    shot_step()
+    prof = fused.profile_report(reset=True)
+    fused.profile(False)
+    launches_per_step = sum(v["launches"] for v in prof.values())
+    gate_kernels = {k: v for k, v in prof.items() if k.startswith(("dense", "pair", "phase", "fused"))}
+    dom_name = max(gate_kernels, key=lambda k: gate_kernels[k]["ms"])
+    dom = gate_kernels[dom_name]
+    achieved = (dom["bytes"] / dom["launches"]) / (dom["ms"] / dom["launches"] / 1e3) / 1e9
+    peak, peak_kind = peaks()
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            traffic = json.load(f).get(dom_name)
+
+    # ---- plain complex128 run of the same circuit, and the accuracy of c64
+    plain_info, accuracy = None, None
+    if not args.no_plain:
+        plain = VectorState(n, shots, "c128")
+        plain.set_stream(stream.cuda_stream)
+        pplan = Plan(n, bits, 0)
+        plain.apply_plan(pplan, mats)   # warm-up (allocation + first touch)
+        plain.reset_all()
+        barrier()
+        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        p0.record(stream)
+        plain.apply_plan(pplan, mats)
+        p1.record(stream)
+        barrier()
+        plain_ms = p0.elapsed_time(p1)
+        gate_step()
+        accuracy = plain.compare(fused)
+        plain_info = {"gates_per_s": ngates / (plain_ms / 1e3), "ms_per_circuit": plain_ms,
+                      "fused_speedup": (ngates / (gate_ms_max / args.steps / 1e3)) / (ngates / (plain_ms / 1e3))}
+        del plain
+
+    # ---- end to end through the public Circuit API (host in, results out)
+    circ = Circuit(n, n, precision="c64", fusion_width=args.fusion)
+    for g, b in gates:
+        circ.add_gate(g, b)
+    circ.measure_all(cbits)
+    del fused
+    circ.execute(shots, Rng(args.seed))
+    barrier()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        circ.execute(shots, Rng(args.seed + k))
+        _ = circ.cstate()
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    et = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+    if dist is not None:
+        dist.all_reduce(et, op=dist.ReduceOp.MAX)
+    e2e_value = world * args.steps * ngates / float(et[0])
+    h2d = plan.nblocks * 32 * 32 * 8 + n * 8
+    d2h = 2 * 8 * shots
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(args.cpu_qubits, 2, args.seed, n)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "gates/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": gate_ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"random U3/CX brick circuit, {n} qubits, depth {args.depth} "
+                                   f"({ngates} gates), complex64 fused k<={args.fusion}, then {shots} Z shots",
+                       "qubits": n, "depth": args.depth, "gates": ngates, "shots": shots,
+                       "fusion_width": args.fusion, "fused_passes": plan.nblocks,
+                       "parallelism": f"replicas{world}", "l2": "state 8 GiB > L2, no flush needed"},
+            "shots_per_s": shots_per_s, "shot_sampling_ms": shot_ms / args.steps,
+            "plain_c128": plain_info, "accuracy_c64_vs_c128": accuracy,
+            "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak,
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                         "launch_ms": dom["ms"] / dom["launches"],
+                         "bytes_per_launch": dom["bytes"] / dom["launches"]},
+            "kernels_per_step": {k: {"launches": v["launches"], "ms": round(v["ms"], 4)} for k, v in prof.items()},
+            "gpu_launches": launches_per_step * args.steps,
+            "e2e": {"value": e2e_value, "unit": "gates/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "clocks": clk.summary(),
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

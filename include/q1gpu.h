@@ -1,0 +1,175 @@
+/*
+ * q1gpu.h -- C ABI of the GB300 statevector engine for q1tsim.
+ *
+ * The engine replaces q1tsim's coefficient-vector backend, `VectorState`,
+ * behind the `QuState` trait (src/qustate.rs:5-89, src/vectorstate.rs:164-416).
+ * Each entry point below is the call a `QuState` implementation (Rust over
+ * `extern "C"`, or Python over ctypes) makes for one trait method; the
+ * reference item it replaces is cited beside it.
+ *
+ * Conventions
+ *  - Plain pointers and sizes; no library-allocated return values.  The caller
+ *    owns every host buffer and every handle (free with q1g_state_free /
+ *    q1g_plan_free).  Outputs go into caller-provided arrays, as
+ *    `measure_into(res: &mut Array1<u64>)` does (src/vectorstate.rs:237-238).
+ *  - Every function returns a status code (Q1G_OK = 0).  The codes map 1:1 onto
+ *    `crate::error::Error` variants (src/error.rs:135-152) plus device-side
+ *    conditions; q1g_last_error() gives the message of the calling thread's
+ *    last failure.  Nothing panics or aborts across the ABI.
+ *  - Qubit 0 is the most significant bit of the amplitude index
+ *    (src/gates.rs:133-141).  Gate matrices are 2^k x 2^k complex row-major
+ *    arrays of (re, im) doubles whose first bit is bits[0] (src/gates.rs:40-53).
+ *  - Sampling consumes host-supplied uniforms in [0, 1) when `uniforms` is
+ *    non-NULL, else draws from the SplitMix64 stream `rng`, which it advances.
+ *    Identical uniforms give identical shot outcomes.
+ *  - A handle is used from one host thread at a time (a q1tsim Circuit is
+ *    single-threaded, src/gates/parameter.rs:23-31).  Work runs on the
+ *    handle's CUDA stream; results returned to host memory are synchronised.
+ */
+#ifndef Q1GPU_H
+#define Q1GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  1..7 mirror crate::error::Error (src/error.rs:135-152). */
+enum q1g_status {
+    Q1G_OK = 0,
+    Q1G_ERR_INVALID_NR_BITS = 1,             /* Error::InvalidNrBits */
+    Q1G_ERR_INVALID_QBIT = 2,                /* Error::InvalidQBit */
+    Q1G_ERR_INVALID_CBIT = 3,                /* Error::InvalidCBit */
+    Q1G_ERR_INVALID_NR_CONTROL_BITS = 4,     /* Error::InvalidNrControlBits */
+    Q1G_ERR_INVALID_NR_MEASUREMENT_BITS = 5, /* Error::InvalidNrMeasurementBits */
+    Q1G_ERR_NOT_ENOUGH_SPACE = 6,            /* Error::NotEnoughSpace */
+    Q1G_ERR_NOT_EXECUTED = 7,                /* Error::NotExecuted */
+    Q1G_ERR_INVALID_ARGUMENT = 8,            /* NULL pointer, bad size or precision */
+    Q1G_ERR_OUT_OF_MEMORY = 9,               /* device allocation or HBM budget */
+    Q1G_ERR_DEVICE = 10,                     /* CUDA error */
+    Q1G_ERR_TIMEOUT = 11                     /* a bounded device wait expired */
+};
+
+/* Amplitude precision of a state. */
+enum q1g_precision {
+    Q1G_C128 = 0, /* complex128 amplitudes, FP64 arithmetic: the drop-in mode */
+    Q1G_C64 = 1   /* complex64 amplitudes, FP32 arithmetic, fused blocks on tensor cores */
+};
+
+typedef struct q1g_state q1g_state;
+typedef struct q1g_plan q1g_plan;
+
+/* SplitMix64 counter stream: draw k returns mix(seed + (counter+1)*gamma)
+ * as a 53-bit uniform and increments counter.  Stands in for the `rng: &mut R`
+ * argument of the QuState methods (src/qustate.rs:31-80). */
+typedef struct q1g_rng {
+    uint64_t seed;
+    uint64_t counter;
+} q1g_rng;
+
+/* Message of the calling thread's last failed call ("" if none). */
+const char* q1g_last_error(void);
+/* Library version (major*10000 + minor*100 + patch). */
+int q1g_version(void);
+/* Visible device: SM count and memory.  Any pointer may be NULL. */
+int q1g_device_info(int* sm_count, size_t* free_bytes, size_t* total_bytes);
+
+/* ---- construction: VectorState::new / from_qubit_coefs (src/vectorstate.rs:41-83) */
+
+/* |0...0> on nr_bits qubits measured over nr_shots runs (src/vectorstate.rs:41-53). */
+int q1g_state_new(size_t nr_bits, size_t nr_shots, int precision, q1g_state** out);
+/* Product state; coefs = nr_bits pairs (c0, c1) of complex numbers, i.e.
+ * 4*nr_bits doubles, each pair normalised (src/vectorstate.rs:62-83). */
+int q1g_state_from_qubit_coefs(const double* coefs, size_t nr_bits, size_t nr_shots,
+                               int precision, q1g_state** out);
+/* Arbitrary initial state: 2^nr_bits complex (re, im) doubles, used as given.
+ * No reference counterpart: the reference API cannot express it. */
+int q1g_state_from_amplitudes(const double* amps, size_t nr_bits, size_t nr_shots,
+                              int precision, q1g_state** out);
+void q1g_state_free(q1g_state* s);
+
+/* Run the state's work on a caller-owned cudaStream_t (NULL: the state's own). */
+int q1g_state_set_stream(q1g_state* s, void* cuda_stream);
+int q1g_state_synchronize(q1g_state* s);
+/* nr_bits, nr_shots, number of state columns, precision.  Any pointer may be NULL. */
+int q1g_state_info(const q1g_state* s, size_t* nr_bits, size_t* nr_shots, size_t* ncols,
+                   int* precision);
+/* Run count of each column (VectorState::counts, src/vectorstate.rs:31-32). */
+int q1g_state_counts(const q1g_state* s, uint64_t* out, size_t len);
+/* Copy the state to host as complex128, column-major: out[(c*2^n + i)*2 + {0,1}]. */
+int q1g_state_download(q1g_state* s, double* out, size_t len);
+
+/* Accuracy of state b against state a (same qubit and column count), computed
+ * on the device in FP64 over all amplitudes: out[0] = max |a_i - b_i|,
+ * out[1] = 1 - |<a|b>|^2 / (<a|a><b|b>) (infidelity), out[2] = total-variation
+ * distance of the outcome probabilities, out[3] = <a|a>, out[4] = <b|b>.
+ * No reference counterpart: it reports the error of a complex64 run against
+ * the complex128 one. */
+int q1g_state_compare(q1g_state* a, q1g_state* b, double* out5);
+
+/* ---- QuState methods (src/qustate.rs:5-89) */
+
+/* apply_gate (src/vectorstate.rs:166-178 -> src/gates.rs:121-152).
+ * k = nr_affected_bits of the gate; nbits must equal k (else INVALID_NR_BITS). */
+int q1g_apply_gate(q1g_state* s, const double* mat, size_t k, const size_t* bits, size_t nbits);
+/* apply_unary_gate_all (src/vectorstate.rs:180-189); mat is 2x2. */
+int q1g_apply_unary_gate_all(q1g_state* s, const double* mat);
+/* apply_conditional_gate (src/vectorstate.rs:193-227, src/qustate.rs:100-127):
+ * control holds one byte per run (nonzero = apply); ncontrol must equal nr_shots. */
+int q1g_apply_conditional_gate(q1g_state* s, const uint8_t* control, size_t ncontrol,
+                               const double* mat, size_t k, const size_t* bits, size_t nbits);
+/* measure_into (src/vectorstate.rs:237-329): one uniform per state column. */
+int q1g_measure_into(q1g_state* s, size_t qbit, size_t cbit, uint64_t* res, size_t res_len,
+                     const double* uniforms, size_t n_uniforms, q1g_rng* rng);
+/* peek_into (src/vectorstate.rs:346-393): like measure_into, state unchanged. */
+int q1g_peek_into(q1g_state* s, size_t qbit, size_t cbit, uint64_t* res, size_t res_len,
+                  const double* uniforms, size_t n_uniforms, q1g_rng* rng);
+/* measure_all_into (src/vectorstate.rs:106-161, 340-344): one uniform per run.
+ * Within a column, runs receive outcomes in ascending basis-index order; the
+ * state collapses onto one basis column per distinct outcome. */
+int q1g_measure_all_into(q1g_state* s, const size_t* cbits, size_t ncbits, uint64_t* res,
+                         size_t res_len, const double* uniforms, size_t n_uniforms,
+                         q1g_rng* rng);
+/* peek_all_into (src/vectorstate.rs:395-400): like measure_all_into, state unchanged. */
+int q1g_peek_all_into(q1g_state* s, const size_t* cbits, size_t ncbits, uint64_t* res,
+                      size_t res_len, const double* uniforms, size_t n_uniforms, q1g_rng* rng);
+/* reset (src/vectorstate.rs:402-408): measure, then X where the result was 1. */
+int q1g_reset(q1g_state* s, size_t bit, const double* uniforms, size_t n_uniforms, q1g_rng* rng);
+/* reset_all (src/vectorstate.rs:410-415). */
+int q1g_reset_all(q1g_state* s);
+
+/* ---- gate sequences: the lowering point of Circuit::do_execute_with
+ * (src/circuit.rs:643-653).  A plan holds the structure of a run of gates
+ * (qubits per gate) and, for fusion_width > 0, their grouping into fused
+ * blocks of at most fusion_width qubits (<= 5).  q1g_plan_run takes the
+ * gate matrices for this execution, since parameters may change between
+ * executions (src/gates/parameter.rs:23-75). */
+
+/* ks[g] = qubits of gate g; bits_flat = all gates' qubits concatenated. */
+int q1g_plan_create(size_t nr_bits, size_t ngates, const size_t* ks, const size_t* bits_flat,
+                    int fusion_width, q1g_plan** out);
+void q1g_plan_free(q1g_plan* p);
+/* Number of passes (fused blocks or single gates) the plan launches. */
+int q1g_plan_info(const q1g_plan* p, size_t* ngates, size_t* nblocks);
+/* Block i of the plan: its qubits (ascending; *nq in/out) and the indices of
+ * the gates it absorbed, in application order (*ng in/out). */
+int q1g_plan_block(const q1g_plan* p, size_t i, size_t* qubits, size_t* nq, size_t* gates,
+                   size_t* ng);
+/* mats_flat = all gates' matrices concatenated ((re, im) doubles). */
+int q1g_plan_run(q1g_plan* p, q1g_state* s, const double* mats_flat, size_t n_doubles);
+
+/* ---- profiling: per-kernel CUDA-event timing on the state's stream */
+int q1g_profile_enable(q1g_state* s, int enable);
+/* Kernel family names and totals since the last reset.  For entry i < *n:
+ * names[i] (up to 31 chars + NUL in a 32-byte slot), launches, total device ms and
+ * algorithmic bytes moved.  *n is in/out: capacity in, entries out. */
+int q1g_profile_report(q1g_state* s, char* names, uint64_t* launches, double* ms,
+                       double* bytes, size_t* n);
+int q1g_profile_reset(q1g_state* s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* Q1GPU_H */

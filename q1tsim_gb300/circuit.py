@@ -1,0 +1,292 @@
+"""Circuit: q1tsim's circuit API executing on the GPU VectorState.
+
+Mirrors `Circuit` (src/circuit.rs:97-1282) and the Python binding
+(python/q1tsim.py): gates are added by object or by name, then `execute`
+runs the op list (src/circuit.rs:643-762) on a device-resident state and
+`histogram*` count the classical results (src/circuit.rs:773-841).
+
+Runs of consecutive gates are lowered to one `Plan` per run: in the plain
+complex128 mode (fusion_width 0) each gate is its own pass, exactly as
+`apply_gate` would run it; with fusion_width k (complex64 fused mode) the
+plan groups gates into blocks of at most k qubits.  Matrices are evaluated
+again on every execute, since gate parameters may change between runs
+(src/gates/parameter.rs:23-75).
+"""
+import numpy as np
+
+from . import gates as G
+from ._lib import InvalidCBit, InvalidQBit, NotExecuted
+from .vectorstate import Plan, Rng, VectorState
+
+BASES = ("x", "y", "z")
+
+
+class Circuit:
+    def __init__(self, nr_qbits, nr_cbits=0, precision="c128", fusion_width=0):
+        self.nr_qbits = int(nr_qbits)
+        self.nr_cbits = int(nr_cbits)
+        self.precision = precision
+        self.fusion_width = int(fusion_width)
+        self.ops = []
+        self.q_state = None
+        self.c_state = None
+        self.rng = None
+        self._plans = {}
+
+    # ------------------------------------------------------------ building
+    def _check_qbits(self, qbits):
+        for b in qbits:
+            if b >= self.nr_qbits or b < 0:
+                raise InvalidQBit(f"Invalid index {b} for a quantum bit")
+
+    def _check_cbits(self, cbits):
+        for b in cbits:
+            if b >= self.nr_cbits or b < 0:
+                raise InvalidCBit(f"Invalid index {b} for a classical bit")
+
+    def _push(self, op):
+        self.ops.append(op)
+        self._plans.clear()
+
+    @staticmethod
+    def _gate(gate, params):
+        if isinstance(gate, str):
+            return G.by_name(gate, params)
+        return gate
+
+    def add_gate(self, gate, qbits, params=None):
+        """src/circuit.rs:161-175 (object) / python/q1tsim.py add_gate (name)."""
+        g = self._gate(gate, params)
+        qbits = list(qbits)
+        self._check_qbits(qbits)
+        self._push(("gate", g, qbits))
+
+    def add_conditional_gate(self, control, target, gate, qbits, params=None):
+        """src/circuit.rs:182-204: apply when the classical bits `control`
+        (first = least significant) form the word `target`."""
+        g = self._gate(gate, params)
+        control, qbits = list(control), list(qbits)
+        self._check_cbits(control)
+        self._check_qbits(qbits)
+        self._push(("cgate", control, int(target), g, qbits))
+
+    def measure_basis(self, qbit, cbit, basis):
+        self._check_qbits([qbit])
+        self._check_cbits([cbit])
+        self._push(("measure", qbit, cbit, basis.lower()))
+
+    def measure(self, qbit, cbit, basis="z"):
+        self.measure_basis(qbit, cbit, basis)
+
+    def measure_x(self, qbit, cbit):
+        self.measure_basis(qbit, cbit, "x")
+
+    def measure_y(self, qbit, cbit):
+        self.measure_basis(qbit, cbit, "y")
+
+    def measure_z(self, qbit, cbit):
+        self.measure_basis(qbit, cbit, "z")
+
+    def measure_all_basis(self, cbits, basis):
+        cbits = list(cbits)
+        self._check_cbits(cbits)
+        self._push(("measure_all", cbits, basis.lower()))
+
+    def measure_all(self, cbits=None, basis="z"):
+        if cbits is None:
+            cbits = list(range(self.nr_qbits))
+        self.measure_all_basis(cbits, basis)
+
+    def peek_basis(self, qbit, cbit, basis):
+        self._check_qbits([qbit])
+        self._check_cbits([cbit])
+        self._push(("peek", qbit, cbit, basis.lower()))
+
+    def peek(self, qbit, cbit, basis="z"):
+        self.peek_basis(qbit, cbit, basis)
+
+    def peek_all_basis(self, cbits, basis):
+        cbits = list(cbits)
+        self._check_cbits(cbits)
+        self._push(("peek_all", cbits, basis.lower()))
+
+    def peek_all(self, cbits=None, basis="z"):
+        if cbits is None:
+            cbits = list(range(self.nr_qbits))
+        self.peek_all_basis(cbits, basis)
+
+    def reset(self, qbit):
+        self._check_qbits([qbit])
+        self._push(("reset", qbit))
+
+    def reset_all(self):
+        self._push(("reset_all",))
+
+    def barrier(self, qbits):
+        self._check_qbits(list(qbits))
+        self._push(("barrier", list(qbits)))
+
+    # gate shortcuts of src/circuit.rs:430-541 and python/q1tsim.py
+    def h(self, q): self.add_gate(G.H(), [q])
+    def x(self, q): self.add_gate(G.X(), [q])
+    def y(self, q): self.add_gate(G.Y(), [q])
+    def z(self, q): self.add_gate(G.Z(), [q])
+    def s(self, q): self.add_gate(G.S(), [q])
+    def sdg(self, q): self.add_gate(G.Sdg(), [q])
+    def t(self, q): self.add_gate(G.T(), [q])
+    def tdg(self, q): self.add_gate(G.Tdg(), [q])
+    def v(self, q): self.add_gate(G.V(), [q])
+    def vdg(self, q): self.add_gate(G.Vdg(), [q])
+    def i(self, q): self.add_gate(G.I(), [q])
+    def rx(self, theta, q): self.add_gate(G.RX(theta), [q])
+    def ry(self, theta, q): self.add_gate(G.RY(theta), [q])
+    def rz(self, lmb, q): self.add_gate(G.RZ(lmb), [q])
+    def u1(self, lmb, q): self.add_gate(G.U1(lmb), [q])
+    def u2(self, phi, lmb, q): self.add_gate(G.U2(phi, lmb), [q])
+    def u3(self, theta, phi, lmb, q): self.add_gate(G.U3(theta, phi, lmb), [q])
+    def cx(self, c, t): self.add_gate(G.CX(), [c, t])
+    def cy(self, c, t): self.add_gate(G.CY(), [c, t])
+    def cz(self, c, t): self.add_gate(G.CZ(), [c, t])
+    def ch(self, c, t): self.add_gate(G.CH(), [c, t])
+    def crx(self, theta, c, t): self.add_gate(G.CRX(theta), [c, t])
+    def cry(self, theta, c, t): self.add_gate(G.CRY(theta), [c, t])
+    def crz(self, lmb, c, t): self.add_gate(G.CRZ(lmb), [c, t])
+    def swap(self, a, b): self.add_gate(G.Swap(), [a, b])
+
+    def is_stabilizer_circuit(self):
+        return all(op[0] != "gate" or op[1].is_stabilizer() for op in self.ops) and \
+            all(op[0] != "cgate" or op[3].is_stabilizer() for op in self.ops)
+
+    # ----------------------------------------------------------- execution
+    def new_state(self, nr_shots):
+        return VectorState(self.nr_qbits, nr_shots, self.precision)
+
+    def execute(self, nr_shots, rng=None):
+        """Run the circuit from |0...0> over nr_shots runs on the GPU vector
+        backend (src/circuit.rs:562-585; the stabilizer choice of the
+        reference is not made here: every circuit runs on the vector state,
+        as execute_with(QuStateRepr::vector(..)) does)."""
+        if isinstance(self.q_state, VectorState) and self.q_state.nr_shots == nr_shots \
+                and self.q_state.precision == self.precision:
+            self.q_state.reset_all()
+            q_state = self.q_state
+        else:
+            q_state = self.new_state(nr_shots)
+        self.execute_with(nr_shots, rng if rng is not None else Rng(), q_state)
+
+    def execute_with(self, nr_shots, rng, q_state):
+        """src/circuit.rs:594-600"""
+        self.q_state = q_state
+        self.c_state = np.zeros(nr_shots, dtype=np.uint64)
+        self.rng = rng
+        self.reexecute_with_rng(rng)
+
+    def reexecute(self, rng=None):
+        """src/circuit.rs:608-611: run again from the previous state."""
+        self.reexecute_with_rng(rng if rng is not None else (self.rng or Rng()))
+
+    def reexecute_with_rng(self, rng):
+        if self.c_state is None or self.q_state is None:
+            raise NotExecuted("Circuit has not been run yet")
+        self.rng = rng
+        self._do_execute(self.q_state, self.c_state, rng)
+
+    def _segments(self):
+        """Op list with runs of consecutive gates grouped: ("seq", [ops])."""
+        out = []
+        for op in self.ops:
+            if op[0] == "gate":
+                if out and out[-1][0] == "seq":
+                    out[-1][1].append(op)
+                else:
+                    out.append(("seq", [op]))
+            else:
+                out.append(op)
+        return out
+
+    def _run_seq(self, q_state, idx, seq):
+        if hasattr(q_state, "apply_plan"):
+            width = self.fusion_width
+            key = (idx, width)
+            plan = self._plans.get(key)
+            if plan is None:
+                plan = Plan(self.nr_qbits, [op[2] for op in seq], width)
+                self._plans[key] = plan
+            mats = [np.ascontiguousarray(op[1].matrix(), dtype=np.complex128).ravel() for op in seq]
+            flat = np.concatenate(mats).view(np.float64) if mats else np.zeros(0)
+            q_state.apply_plan(plan, flat)
+        else:
+            for op in seq:
+                q_state.apply_gate(op[1].matrix(), op[2])
+
+    def _do_execute(self, q_state, c_state, rng):
+        """src/circuit.rs:643-762"""
+        H, S, Sdg = G.H().matrix(), G.S().matrix(), G.Sdg().matrix()
+        for idx, op in enumerate(self._segments()):
+            kind = op[0]
+            if kind == "seq":
+                self._run_seq(q_state, idx, op[1])
+            elif kind == "cgate":
+                _, control, target, gate, bits = op
+                word = np.zeros(len(c_state), dtype=np.uint64)
+                for dst, src in enumerate(control):
+                    word |= ((c_state >> np.uint64(src)) & np.uint64(1)) << np.uint64(dst)
+                apply = (word == np.uint64(target)).astype(np.uint8)
+                q_state.apply_conditional_gate(apply, gate.matrix(), bits)
+            elif kind in ("measure", "peek"):
+                _, qbit, cbit, basis = op
+                fn = q_state.measure_into if kind == "measure" else q_state.peek_into
+                if basis == "x":
+                    q_state.apply_gate(H, [qbit])
+                    fn(qbit, cbit, c_state, rng=rng)
+                    q_state.apply_gate(H, [qbit])
+                elif basis == "y":
+                    q_state.apply_gate(Sdg, [qbit])
+                    q_state.apply_gate(H, [qbit])
+                    fn(qbit, cbit, c_state, rng=rng)
+                    q_state.apply_gate(H, [qbit])
+                    q_state.apply_gate(S, [qbit])
+                else:
+                    fn(qbit, cbit, c_state, rng=rng)
+            elif kind in ("measure_all", "peek_all"):
+                _, cbits, basis = op
+                fn = q_state.measure_all_into if kind == "measure_all" else q_state.peek_all_into
+                if basis == "x":
+                    q_state.apply_unary_gate_all(H)
+                    fn(cbits, c_state, rng=rng)
+                    q_state.apply_unary_gate_all(H)
+                elif basis == "y":
+                    q_state.apply_unary_gate_all(Sdg)
+                    q_state.apply_unary_gate_all(H)
+                    fn(cbits, c_state, rng=rng)
+                    q_state.apply_unary_gate_all(H)
+                    q_state.apply_unary_gate_all(S)
+                else:
+                    fn(cbits, c_state, rng=rng)
+            elif kind == "reset":
+                q_state.reset(op[1], rng=rng)
+            elif kind == "reset_all":
+                q_state.reset_all()
+            elif kind == "barrier":
+                pass
+
+    # ----------------------------------------------------------- results
+    def cstate(self):
+        return self.c_state
+
+    def histogram(self):
+        """src/circuit.rs:773-789: {u64 key: count}, cbit 0 = LSB."""
+        if self.c_state is None:
+            raise NotExecuted("Circuit has not been run yet")
+        keys, cnt = np.unique(self.c_state, return_counts=True)
+        return {int(k): int(c) for k, c in zip(keys, cnt)}
+
+    def histogram_vec(self):
+        """src/circuit.rs:800-815"""
+        if self.c_state is None:
+            raise NotExecuted("Circuit has not been run yet")
+        return np.bincount(self.c_state.astype(np.int64), minlength=1 << self.nr_cbits).tolist()
+
+    def histogram_string(self):
+        """src/circuit.rs:823-841: keys are binary strings, cbit 0 last."""
+        return {format(k, f"0{self.nr_cbits}b"): c for k, c in self.histogram().items()}

@@ -1,0 +1,667 @@
+// Device-resident VectorState: the host runtime behind the C ABI.
+//
+// Semantics follow q1tsim's VectorState (src/vectorstate.rs:24-416) column by
+// column; only the representation changes: columns are contiguous in HBM,
+// collapsed basis columns are kept as indices, and every amplitude pass is
+// one of the kernels in gate_kernels.cu / state_kernels.cu / measure_kernels.cu.
+#include "engine.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+namespace q1g {
+
+void check_cuda(cudaError_t e, const char* what)
+{
+    if (e == cudaSuccess) return;
+    const int code = (e == cudaErrorMemoryAllocation) ? Q1G_ERR_OUT_OF_MEMORY : Q1G_ERR_DEVICE;
+    throw Error(code, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+void DevBuf::ensure(size_t b)
+{
+    if (b <= bytes) return;
+    release();
+    if (b == 0) return;
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, b);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        throw Error(Q1G_ERR_OUT_OF_MEMORY,
+                    "device allocation of " + std::to_string(b) + " bytes failed: " + cudaGetErrorString(e));
+    }
+    p = q;
+    bytes = b;
+}
+
+void DevBuf::release()
+{
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+}
+
+void HostBuf::ensure(size_t b)
+{
+    if (b <= bytes) return;
+    release();
+    if (b == 0) return;
+    void* q = nullptr;
+    cudaError_t e = cudaMallocHost(&q, b);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        throw Error(Q1G_ERR_OUT_OF_MEMORY, "pinned host allocation failed");
+    }
+    p = q;
+    bytes = b;
+}
+
+void HostBuf::release()
+{
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    bytes = 0;
+}
+
+namespace {
+
+uint64_t splitmix_mix(uint64_t z)
+{
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+}  // namespace
+
+double stream_uniform_host(uint64_t seed, uint64_t counter)
+{
+    const uint64_t z = seed + (counter + 1) * 0x9E3779B97F4A7C15ULL;
+    return (double)(splitmix_mix(z) >> 11) * (1.0 / 9007199254740992.0);
+}
+
+// Smallest k with CDF(k) > u, pmf in log space from 40 sigma below the mean.
+// Stands in for rand_distr::Binomial (src/vectorstate.rs:271, 379).
+uint64_t binomial_inv(uint64_t n, double p, double u)
+{
+    if (n == 0 || p <= 0.0) return 0;
+    if (p >= 1.0) return n;
+    const double nn = (double)n;
+    const double mean = nn * p;
+    const double sd = std::sqrt(nn * p * (1.0 - p));
+    const double lo_d = std::floor(mean - 40.0 * sd - 40.0);
+    const double hi_d = std::ceil(mean + 40.0 * sd + 40.0);
+    const uint64_t lo = lo_d < 0.0 ? 0 : (uint64_t)lo_d;
+    const uint64_t hi = hi_d > nn ? n : (uint64_t)hi_d;
+    const double lp = std::log(p), lq = std::log1p(-p);
+    const double lnf = std::lgamma(nn + 1.0);
+    double cdf = 0.0;
+    for (uint64_t k = lo; k <= hi; ++k) {
+        const double kk = (double)k;
+        const double lpmf = lnf - std::lgamma(kk + 1.0) - std::lgamma(nn - kk + 1.0) + kk * lp + (nn - kk) * lq;
+        cdf += std::exp(lpmf);
+        if (u < cdf) return k;
+    }
+    return hi;
+}
+
+}  // namespace q1g
+
+using namespace q1g;
+
+q1g_state::q1g_state(int nbits_, uint64_t nshots_, int prec_)
+    : nbits(nbits_), nshots(nshots_), prec(prec_), N(uint64_t(1) << nbits_), ncols(1),
+      counts{nshots_}
+{
+    check_cuda(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    own_stream = true;
+}
+
+q1g_state::~q1g_state()
+{
+    if (stream) cudaStreamSynchronize(stream);
+    for (auto& p : pending) {
+        cudaEventDestroy(p.a);
+        cudaEventDestroy(p.b);
+    }
+    if (own_stream && stream) cudaStreamDestroy(stream);
+}
+
+void q1g_state::sync()
+{
+    check_cuda(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+}
+
+void q1g_state::collect_profile()
+{
+    if (pending.empty()) return;
+    sync();
+    for (auto& p : pending) {
+        float ms = 0.f;
+        check_cuda(cudaEventElapsedTime(&ms, p.a, p.b), "cudaEventElapsedTime");
+        auto& t = totals[p.name];
+        t.launches += 1;
+        t.ms += ms;
+        t.bytes += p.bytes;
+        cudaEventDestroy(p.a);
+        cudaEventDestroy(p.b);
+    }
+    pending.clear();
+}
+
+void q1g_state::ensure_dense()
+{
+    if (!sparse) return;
+    amps.ensure(ncols * N * bsz());
+    uscratch.ensure(ncols * sizeof(uint64_t));
+    check_cuda(cudaMemcpyAsync(uscratch.p, basis.data(), ncols * sizeof(uint64_t),
+                               cudaMemcpyHostToDevice, stream), "upload basis");
+    launch("fill_basis", double(ncols * N * bsz()), [&] {
+        return launch_fill_basis(amps.p, prec, ncols * N, uscratch.as<uint64_t>(), ncols, N, stream);
+    });
+    // The basis list must stay alive until the copy ran: wait here.
+    sync();
+    sparse = false;
+    basis.clear();
+}
+
+void q1g_state::apply_op(const GateOp& op, char* base, uint64_t total_amps)
+{
+    const double b2 = 2.0 * bsz();
+    switch (op.kind) {
+        case GateOp::Noop:
+            return;
+        case GateOp::Pair:
+            launch(prec == kC128 ? "pair_c128" : "pair_c64", b2 * op.touched(total_amps), [&] {
+                return launch_pair(base, prec, total_amps, op.map, op.o0, op.o1, op.m2, stream);
+            });
+            return;
+        case GateOp::Phase:
+            launch(prec == kC128 ? "phase_c128" : "phase_c64", b2 * op.touched(total_amps), [&] {
+                return launch_phase(base, prec, total_amps, op.map, op.ph[0], op.ph[1], stream);
+            });
+            return;
+        case GateOp::Dense: {
+            const size_t d = size_t(1) << op.t;
+            std::vector<double> hm(2 * d * d);
+            for (size_t e = 0; e < d * d; ++e) {
+                hm[2 * e] = op.dense[e].real();
+                hm[2 * e + 1] = op.dense[e].imag();
+            }
+            if (prec == kC64) {
+                std::vector<float> hf(hm.begin(), hm.end());
+                matbuf.ensure(hf.size() * sizeof(float));
+                check_cuda(cudaMemcpyAsync(matbuf.p, hf.data(), hf.size() * sizeof(float),
+                                           cudaMemcpyHostToDevice, stream), "upload matrix");
+                sync();
+            } else {
+                matbuf.ensure(hm.size() * sizeof(double));
+                check_cuda(cudaMemcpyAsync(matbuf.p, hm.data(), hm.size() * sizeof(double),
+                                           cudaMemcpyHostToDevice, stream), "upload matrix");
+                sync();
+            }
+            launch(prec == kC128 ? "dense_c128" : "dense_c64", b2 * op.touched(total_amps), [&] {
+                return launch_dense(base, prec, total_amps, op.map, op.offs, op.t, matbuf.p, stream);
+            });
+            return;
+        }
+    }
+}
+
+static void check_gate_bits(int nbits, size_t k, const size_t* bits, size_t nbits_given)
+{
+    if (nbits_given != k)
+        throw Error(Q1G_ERR_INVALID_NR_BITS, "Expected " + std::to_string(k) + " bits for the gate, got " +
+                                                 std::to_string(nbits_given));
+    for (size_t m = 0; m < nbits_given; ++m)
+        if (bits[m] >= (size_t)nbits) throw Error(Q1G_ERR_INVALID_QBIT, "Invalid qubit index " + std::to_string(bits[m]));
+    for (size_t m = 0; m < nbits_given; ++m)
+        for (size_t j = m + 1; j < nbits_given; ++j)
+            if (bits[m] == bits[j])
+                throw Error(Q1G_ERR_INVALID_ARGUMENT, "qubit " + std::to_string(bits[m]) + " given twice");
+}
+
+static GateOp classify_host(const double* mat, size_t k, const size_t* bits, int nbits)
+{
+    const size_t dim = size_t(1) << k;
+    std::vector<cd> m(dim * dim);
+    for (size_t e = 0; e < dim * dim; ++e) m[e] = cd(mat[2 * e], mat[2 * e + 1]);
+    std::vector<int> b(k);
+    for (size_t j = 0; j < k; ++j) b[j] = (int)bits[j];
+    return classify(m.data(), (int)k, b.data(), nbits);
+}
+
+void q1g_state::apply_gate(const double* mat, size_t k, const size_t* bits, size_t nbits_given)
+{
+    check_gate_bits(nbits, k, bits, nbits_given);
+    const GateOp op = classify_host(mat, k, bits, nbits);
+    if (op.kind == GateOp::Noop) return;
+    ensure_dense();
+    apply_op(op, amps.as<char>(), total());
+}
+
+// src/qustate.rs:100-127: (column, length, apply) runs of equal control bits.
+struct CondRange {
+    uint64_t col, len;
+    bool apply;
+};
+
+static std::vector<CondRange> conditional_ranges(const std::vector<uint64_t>& counts,
+                                                 const uint8_t* control)
+{
+    std::vector<CondRange> r;
+    uint64_t off = 0;
+    for (uint64_t c = 0; c < counts.size(); ++c) {
+        const uint64_t count = counts[c];
+        if (count == 0) continue;
+        uint64_t begin = off;
+        bool prev = control[off] != 0;
+        for (uint64_t ib = off + 1; ib < off + count; ++ib) {
+            const bool cur = control[ib] != 0;
+            if (cur != prev) {
+                r.push_back({c, ib - begin, prev});
+                begin = ib;
+                prev = cur;
+            }
+        }
+        if (begin < off + count) r.push_back({c, off + count - begin, prev});
+        off += count;
+    }
+    return r;
+}
+
+void q1g_state::apply_conditional(const uint8_t* control, size_t ncontrol, const double* mat,
+                                  size_t k, const size_t* bits, size_t nbits_given)
+{
+    if (ncontrol != nshots)
+        throw Error(Q1G_ERR_INVALID_NR_CONTROL_BITS, "Expected " + std::to_string(nshots) +
+                                                         " control bits, got " + std::to_string(ncontrol));
+    check_gate_bits(nbits, k, bits, nbits_given);
+    const GateOp op = classify_host(mat, k, bits, nbits);
+    const auto ranges = conditional_ranges(counts, control);
+    bool same_layout = ranges.size() == ncols;
+    for (size_t j = 0; same_layout && j < ranges.size(); ++j) same_layout = ranges[j].col == j;
+    if (same_layout && op.kind == GateOp::Noop) return;
+    ensure_dense();
+    if (!same_layout) {
+        const uint64_t nr = ranges.size();
+        std::vector<CollapseCol> cols(nr);
+        for (uint64_t j = 0; j < nr; ++j) cols[j] = {ranges[j].col, -1, 1.0};
+        spare.ensure(nr * N * bsz());
+        colbuf.ensure(nr * sizeof(CollapseCol));
+        check_cuda(cudaMemcpyAsync(colbuf.p, cols.data(), nr * sizeof(CollapseCol),
+                                   cudaMemcpyHostToDevice, stream), "upload columns");
+        launch("column_copy", 2.0 * nr * N * bsz(), [&] {
+            return launch_collapse_copy(spare.p, amps.p, prec, N, 0, colbuf.as<CollapseCol>(), nr, stream);
+        });
+        sync();
+        amps.swap(spare);
+        if (spare.bytes > (size_t(1) << 30)) spare.release();
+        ncols = nr;
+    }
+    counts.resize(ranges.size());
+    for (size_t j = 0; j < ranges.size(); ++j) counts[j] = ranges[j].len;
+    for (size_t j = 0; j < ranges.size(); ++j)
+        if (ranges[j].apply) apply_op(op, col_ptr(j), N);
+}
+
+std::vector<double> q1g_state::zero_weights(size_t qbit)
+{
+    const int pos = nbits - 1 - (int)qbit;
+    std::vector<double> w0(ncols, 0.0);
+    if (sparse) {
+        for (uint64_t c = 0; c < ncols; ++c) w0[c] = ((basis[c] >> pos) & 1) ? 0.0 : 1.0;
+        return w0;
+    }
+    IndexMap m{};
+    m.nz = 1;
+    m.zpos[0] = pos;
+    m.setmask = 0;
+    const uint64_t half = N / 2;
+    const uint64_t chunk = std::min<uint64_t>(half, 4096);
+    const uint64_t nchunks = ncols * (half / chunk);
+    dscratch.ensure((nchunks + ncols) * sizeof(double));
+    double* d = dscratch.as<double>();
+    launch("qubit_weights", double(ncols * half * bsz()), [&] {
+        return launch_chunk_sums(amps.p, prec, ncols * half, chunk, m, d, stream);
+    });
+    check_cuda(launch_segment_sums(d, ncols, half / chunk, d + nchunks, stream), "segment_sums");
+    hstage.ensure(ncols * sizeof(double));
+    check_cuda(cudaMemcpyAsync(hstage.p, d + nchunks, ncols * sizeof(double), cudaMemcpyDeviceToHost, stream),
+               "download weights");
+    sync();
+    std::memcpy(w0.data(), hstage.p, ncols * sizeof(double));
+    return w0;
+}
+
+void q1g_state::measure(size_t qbit, size_t cbit, uint64_t* res, size_t res_len,
+                        const double* uniforms, size_t nu, q1g_rng* rng, bool collapse)
+{
+    if (qbit >= (size_t)nbits) throw Error(Q1G_ERR_INVALID_QBIT, "Invalid qubit index " + std::to_string(qbit));
+    if (res_len < nshots)
+        throw Error(Q1G_ERR_NOT_ENOUGH_SPACE, "Unable to store " + std::to_string(nshots) +
+                                                  " measurements in array of size " + std::to_string(res_len));
+    if (cbit >= 64) throw Error(Q1G_ERR_INVALID_CBIT, "Invalid classical bit index " + std::to_string(cbit));
+    if (uniforms ? nu < ncols : rng == nullptr)
+        throw Error(Q1G_ERR_INVALID_ARGUMENT, "need one uniform per state column or an rng");
+    std::vector<double> us(ncols);
+    for (uint64_t c = 0; c < ncols; ++c)
+        us[c] = uniforms ? uniforms[c] : stream_uniform_host(rng->seed, rng->counter++);
+    const std::vector<double> w0 = zero_weights(qbit);
+    std::vector<uint64_t> n0(ncols);
+    uint64_t new_nr = 0;
+    for (uint64_t c = 0; c < ncols; ++c) {
+        n0[c] = binomial_inv(counts[c], std::min(w0[c], 1.0), us[c]);
+        new_nr += (n0[c] == 0 || n0[c] == counts[c]) ? 1 : 2;
+    }
+    // results: first n0 runs of a column read 0, the rest 1 (src/vectorstate.rs:290-297)
+    const uint64_t one = uint64_t(1) << cbit;
+    uint64_t rs = 0;
+    for (uint64_t c = 0; c < ncols; ++c) {
+        for (uint64_t r = rs; r < rs + n0[c]; ++r) res[r] &= ~one;
+        for (uint64_t r = rs + n0[c]; r < rs + counts[c]; ++r) res[r] |= one;
+        rs += counts[c];
+    }
+    if (!collapse) return;
+    // collapse (src/vectorstate.rs:299-322, 91-104)
+    std::vector<CollapseCol> cols;
+    std::vector<uint64_t> nc;
+    std::vector<uint64_t> nbasis;
+    cols.reserve(new_nr);
+    for (uint64_t c = 0; c < ncols; ++c) {
+        const double w = w0[c];
+        if (n0[c] == counts[c]) {
+            cols.push_back({c, 0, 1.0 / std::sqrt(w)});
+            nc.push_back(counts[c]);
+        } else if (n0[c] == 0) {
+            cols.push_back({c, 1, 1.0 / std::sqrt(1.0 - w)});
+            nc.push_back(counts[c]);
+        } else {
+            cols.push_back({c, 0, 1.0 / std::sqrt(w)});
+            nc.push_back(n0[c]);
+            cols.push_back({c, 1, 1.0 / std::sqrt(1.0 - w)});
+            nc.push_back(counts[c] - n0[c]);
+        }
+    }
+    if (sparse) {
+        // basis columns are unchanged by their own (certain) outcome
+        counts = nc;
+        return;
+    }
+    const int pos = nbits - 1 - (int)qbit;
+    const bool split = new_nr != ncols;
+    colbuf.ensure(new_nr * sizeof(CollapseCol));
+    check_cuda(cudaMemcpyAsync(colbuf.p, cols.data(), new_nr * sizeof(CollapseCol), cudaMemcpyHostToDevice,
+                               stream), "upload columns");
+    if (!split) {
+        launch("collapse", 2.0 * ncols * N * bsz(), [&] {
+            return launch_collapse_copy(amps.p, amps.p, prec, N, pos, colbuf.as<CollapseCol>(), new_nr, stream);
+        });
+    } else {
+        spare.ensure(new_nr * N * bsz());
+        launch("collapse", double(new_nr + ncols) * N * bsz(), [&] {
+            return launch_collapse_copy(spare.p, amps.p, prec, N, pos, colbuf.as<CollapseCol>(), new_nr, stream);
+        });
+    }
+    sync();
+    if (split) {
+        amps.swap(spare);
+        if (spare.bytes > (size_t(1) << 30)) spare.release();
+    }
+    ncols = new_nr;
+    counts = nc;
+}
+
+void q1g_state::measure_all(const size_t* cbits, size_t ncbits, uint64_t* res, size_t res_len,
+                            const double* uniforms, size_t nu, q1g_rng* rng, bool collapse)
+{
+    if (res_len < nshots)
+        throw Error(Q1G_ERR_NOT_ENOUGH_SPACE, "Unable to store " + std::to_string(nshots) +
+                                                  " measurements in array of size " + std::to_string(res_len));
+    if (ncbits != (size_t)nbits)
+        throw Error(Q1G_ERR_INVALID_NR_MEASUREMENT_BITS, "Expected " + std::to_string(nbits) +
+                                                             " measurement bits, got " + std::to_string(ncbits));
+    for (size_t q = 0; q < ncbits; ++q)
+        if (cbits[q] >= 64) throw Error(Q1G_ERR_INVALID_CBIT, "Invalid classical bit index " + std::to_string(cbits[q]));
+    if (uniforms ? nu < nshots : rng == nullptr)
+        throw Error(Q1G_ERR_INVALID_ARGUMENT, "need one uniform per run or an rng");
+    uint64_t mask = 0;
+    std::vector<uint64_t> cbit_of_pos(64, 0);
+    for (size_t q = 0; q < ncbits; ++q) {
+        mask |= uint64_t(1) << cbits[q];
+        cbit_of_pos[nbits - 1 - q] = uint64_t(1) << cbits[q];
+    }
+    mask = ~mask;
+    auto word_of = [&](uint64_t idx) {
+        uint64_t w = 0;
+        for (int p = 0; p < nbits; ++p)
+            if ((idx >> p) & 1) w |= cbit_of_pos[p];
+        return w;
+    };
+
+    std::vector<uint64_t> outc(nshots);
+    if (sparse) {
+        uint64_t off = 0;
+        for (uint64_t c = 0; c < ncols; ++c) {
+            for (uint64_t r = 0; r < counts[c]; ++r) outc[off + r] = basis[c];
+            if (!uniforms) rng->counter += counts[c] + 1;
+            off += counts[c];
+        }
+        for (uint64_t r = 0; r < nshots; ++r) res[r] = (res[r] & mask) | word_of(outc[r]);
+    } else if (nshots > 0) {
+        const uint64_t chunk = std::min<uint64_t>(N, 1024);
+        const uint64_t ncc = N / chunk;  // chunks per column
+        uint64_t mmax = 0;
+        for (auto c : counts) mmax = std::max(mmax, c);
+        const uint64_t scan_tmp = scan_tmp_doubles(ncc) + 1;
+        const uint64_t spc_tmp = 2 * (mmax + 1) + scan_tmp_doubles(mmax + 1) + 1;
+        const uint64_t nd = ncols * ncc + ncols + scan_tmp + nshots + spc_tmp;
+        dscratch.ensure(nd * sizeof(double));
+        double* d_sums = dscratch.as<double>();
+        double* d_tot = d_sums + ncols * ncc;
+        double* d_stmp = d_tot + ncols;
+        double* d_u = d_stmp + scan_tmp;
+        double* d_spc = d_u + nshots;
+        uscratch.ensure((2 * nshots + 64) * sizeof(uint64_t));
+        uint64_t* d_out = uscratch.as<uint64_t>();
+        uint64_t* d_word = d_out + nshots;
+        uint64_t* d_cpos = d_word + nshots;
+        check_cuda(cudaMemcpyAsync(d_cpos, cbit_of_pos.data(), 64 * sizeof(uint64_t), cudaMemcpyHostToDevice,
+                                   stream), "upload cbits");
+        IndexMap none{};
+        launch("chunk_sums", double(ncols * N * bsz()), [&] {
+            return launch_chunk_sums(amps.p, prec, ncols * N, chunk, none, d_sums, stream);
+        });
+        for (uint64_t c = 0; c < ncols; ++c)
+            launch("prefix_scan", 2.0 * ncc * sizeof(double), [&] {
+                return launch_exclusive_scan(d_sums + c * ncc, ncc, d_stmp, d_tot + c, stream);
+            });
+        std::vector<double> hu;
+        if (uniforms) {
+            hu.assign(uniforms, uniforms + nshots);
+            uint64_t off = 0;
+            for (uint64_t c = 0; c < ncols; ++c) {
+                std::sort(hu.begin() + off, hu.begin() + off + counts[c]);
+                off += counts[c];
+            }
+            check_cuda(cudaMemcpyAsync(d_u, hu.data(), nshots * sizeof(double), cudaMemcpyHostToDevice, stream),
+                       "upload uniforms");
+        } else {
+            uint64_t off = 0;
+            for (uint64_t c = 0; c < ncols; ++c) {
+                const uint64_t m = counts[c];
+                launch("sorted_uniforms", 0.0, [&] {
+                    return launch_sorted_uniforms(rng->seed, rng->counter, m, d_u + off, d_spc, stream);
+                });
+                rng->counter += m + 1;
+                off += m;
+            }
+        }
+        uint64_t off = 0;
+        for (uint64_t c = 0; c < ncols; ++c) {
+            SampleArgs a{};
+            a.amps = col_ptr(c);
+            a.prec = prec;
+            a.col_len = N;
+            a.chunk = chunk;
+            a.excl = d_sums + c * ncc;
+            a.nchunks = ncc;
+            a.total = d_tot + c;
+            a.u = d_u + off;
+            a.nruns = counts[c];
+            a.outcome = d_out + off;
+            a.word = d_word + off;
+            a.nbits = nbits;
+            a.d_cbit_of_pos = d_cpos;
+            launch("sample", double(counts[c] * chunk * bsz()), [&] { return launch_sample(a, stream); });
+            off += counts[c];
+        }
+        hstage.ensure(2 * nshots * sizeof(uint64_t));
+        check_cuda(cudaMemcpyAsync(hstage.p, d_out, 2 * nshots * sizeof(uint64_t), cudaMemcpyDeviceToHost, stream),
+                   "download outcomes");
+        sync();
+        const uint64_t* h_out = hstage.as<uint64_t>();
+        const uint64_t* h_word = h_out + nshots;
+        std::memcpy(outc.data(), h_out, nshots * sizeof(uint64_t));
+        for (uint64_t r = 0; r < nshots; ++r) res[r] = (res[r] & mask) | h_word[r];
+    }
+    if (!collapse) return;
+    // one basis column per distinct (column, outcome), in order
+    std::vector<uint64_t> nb, nc;
+    uint64_t off = 0;
+    for (uint64_t c = 0; c < ncols; ++c) {
+        for (uint64_t r = 0; r < counts[c]; ++r) {
+            if (r == 0 || outc[off + r] != outc[off + r - 1]) {
+                nb.push_back(outc[off + r]);
+                nc.push_back(0);
+            }
+            nc.back() += 1;
+        }
+        off += counts[c];
+    }
+    sparse = true;
+    basis = nb;
+    counts = nc;
+    ncols = nb.size();
+}
+
+void q1g_state::reset_all()
+{
+    sparse = true;
+    basis.assign(1, 0);
+    counts.assign(1, nshots);
+    ncols = 1;
+}
+
+void q1g_state::download(double* out, size_t len)
+{
+    if (len < 2 * ncols * N)
+        throw Error(Q1G_ERR_NOT_ENOUGH_SPACE, "download buffer too small");
+    if (sparse) {
+        std::memset(out, 0, 2 * ncols * N * sizeof(double));
+        for (uint64_t c = 0; c < ncols; ++c) out[2 * (c * N + basis[c])] = 1.0;
+        return;
+    }
+    const uint64_t n = ncols * N;
+    if (prec == kC128) {
+        check_cuda(cudaMemcpyAsync(out, amps.p, n * 16, cudaMemcpyDeviceToHost, stream), "download");
+        sync();
+    } else {
+        std::vector<float> tmp(2 * n);
+        check_cuda(cudaMemcpyAsync(tmp.data(), amps.p, n * 8, cudaMemcpyDeviceToHost, stream), "download");
+        sync();
+        for (uint64_t e = 0; e < 2 * n; ++e) out[e] = tmp[e];
+    }
+}
+
+// ---------------------------------------------------------------- plans
+
+q1g_plan::~q1g_plan()
+{
+    if (staged) {
+        cudaEventSynchronize(staged);
+        cudaEventDestroy(staged);
+    }
+}
+
+namespace q1g {
+
+void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n)
+{
+    if (n != p->mat_doubles)
+        throw Error(Q1G_ERR_INVALID_ARGUMENT, "expected " + std::to_string(p->mat_doubles) + " matrix doubles");
+    if (s->nbits != p->nbits)
+        throw Error(Q1G_ERR_INVALID_ARGUMENT, "plan and state differ in qubit count");
+    const size_t ng = p->gate_bits.size();
+    std::vector<SeqGate> gates(ng);
+    for (size_t g = 0; g < ng; ++g) {
+        const size_t k = p->gate_bits[g].size();
+        const size_t dim = size_t(1) << k;
+        gates[g].bits = p->gate_bits[g];
+        gates[g].mat.resize(dim * dim);
+        const double* m = mats + p->mat_off[g];
+        for (size_t e = 0; e < dim * dim; ++e) gates[g].mat[e] = cd(m[2 * e], m[2 * e + 1]);
+    }
+    std::vector<GateOp> ops;
+    ops.reserve(p->blocks.size());
+    for (const auto& b : p->blocks) {
+        if (b.gates.size() == 1) {
+            const auto& g = gates[b.gates[0]];
+            ops.push_back(classify(g.mat.data(), (int)g.bits.size(), g.bits.data(), s->nbits));
+        } else {
+            const auto m = block_matrix(b, gates);
+            ops.push_back(classify(m.data(), (int)b.qubits.size(), b.qubits.data(), s->nbits));
+        }
+    }
+    // Stage every dense matrix in one pinned upload.
+    size_t dense_bytes = 0;
+    std::vector<size_t> dense_off(ops.size(), 0);
+    const size_t esz = s->prec == kC128 ? 16 : 8;
+    for (size_t i = 0; i < ops.size(); ++i)
+        if (ops[i].kind == GateOp::Dense) {
+            dense_off[i] = dense_bytes;
+            dense_bytes += ops[i].dense.size() * esz;
+        }
+    if (dense_bytes) {
+        if (p->staged) check_cuda(cudaEventSynchronize(p->staged), "plan staging wait");
+        else check_cuda(cudaEventCreateWithFlags(&p->staged, cudaEventDisableTiming), "cudaEventCreate");
+        p->hmats.ensure(dense_bytes);
+        p->dmats.ensure(dense_bytes);
+        for (size_t i = 0; i < ops.size(); ++i) {
+            if (ops[i].kind != GateOp::Dense) continue;
+            char* dst = p->hmats.as<char>() + dense_off[i];
+            for (size_t e = 0; e < ops[i].dense.size(); ++e) {
+                if (s->prec == kC128) {
+                    double v[2] = {ops[i].dense[e].real(), ops[i].dense[e].imag()};
+                    std::memcpy(dst + e * 16, v, 16);
+                } else {
+                    float v[2] = {(float)ops[i].dense[e].real(), (float)ops[i].dense[e].imag()};
+                    std::memcpy(dst + e * 8, v, 8);
+                }
+            }
+        }
+        check_cuda(cudaMemcpyAsync(p->dmats.p, p->hmats.p, dense_bytes, cudaMemcpyHostToDevice, s->stream),
+                   "upload plan matrices");
+        check_cuda(cudaEventRecord(p->staged, s->stream), "cudaEventRecord");
+    }
+    bool any = false;
+    for (const auto& op : ops) any |= op.kind != GateOp::Noop;
+    if (!any) return;
+    s->ensure_dense();
+    const uint64_t total = s->total();
+    const double b2 = 2.0 * s->bsz();
+    for (size_t i = 0; i < ops.size(); ++i) {
+        const GateOp& op = ops[i];
+        if (op.kind == GateOp::Dense) {
+            const void* dm = p->dmats.as<char>() + dense_off[i];
+            s->launch(s->prec == kC128 ? "dense_c128" : "dense_c64", b2 * op.touched(total), [&] {
+                return launch_dense(s->amps.p, s->prec, total, op.map, op.offs, op.t, dm, s->stream);
+            });
+        } else {
+            s->apply_op(op, s->amps.as<char>(), total);
+        }
+    }
+}
+
+}  // namespace q1g

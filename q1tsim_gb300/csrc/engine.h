@@ -1,0 +1,156 @@
+// Host runtime of the engine: the device-resident VectorState and plans.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <exception>
+#include <utility>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/q1gpu.h"
+#include "gate_plan.h"
+#include "kernels.h"
+
+namespace q1g {
+
+struct Error : std::exception {
+    int code;
+    std::string msg;
+    Error(int c, std::string m) : code(c), msg(std::move(m)) {}
+    const char* what() const noexcept override { return msg.c_str(); }
+};
+
+void check_cuda(cudaError_t e, const char* what);
+
+// Grow-only device allocation.
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    void ensure(size_t b);
+    void release();
+    void swap(DevBuf& o)
+    {
+        std::swap(p, o.p);
+        std::swap(bytes, o.bytes);
+    }
+    ~DevBuf() { release(); }
+    template <typename T> T* as() const { return static_cast<T*>(p); }
+};
+
+// Grow-only pinned host allocation.
+struct HostBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    HostBuf() = default;
+    HostBuf(const HostBuf&) = delete;
+    HostBuf& operator=(const HostBuf&) = delete;
+    void ensure(size_t b);
+    void release();
+    ~HostBuf() { release(); }
+    template <typename T> T* as() const { return static_cast<T*>(p); }
+};
+
+struct ProfTotals {
+    uint64_t launches = 0;
+    double ms = 0.0;
+    double bytes = 0.0;
+};
+
+// Inverse CDF of Binomial(n, p) at u (the n0 draw of measure_into).
+uint64_t binomial_inv(uint64_t n, double p, double u);
+double stream_uniform_host(uint64_t seed, uint64_t counter);
+
+}  // namespace q1g
+
+struct q1g_state {
+    int nbits = 0;
+    uint64_t nshots = 0;
+    int prec = q1g::kC128;
+    uint64_t N = 1;
+    uint64_t ncols = 1;
+    std::vector<uint64_t> counts;
+    // Columns collapsed onto basis states are kept as indices only
+    // (the reference materialises them densely, src/vectorstate.rs:150-158).
+    bool sparse = true;
+    std::vector<uint64_t> basis{0};
+
+    q1g::DevBuf amps, spare;
+    q1g::DevBuf dscratch;   // doubles
+    q1g::DevBuf uscratch;   // uint64
+    q1g::DevBuf matbuf;     // one dense matrix
+    q1g::DevBuf colbuf;     // CollapseCol table
+    q1g::HostBuf hstage;    // pinned staging for results
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+
+    bool prof = false;
+    struct Pending {
+        std::string name;
+        double bytes;
+        cudaEvent_t a, b;
+    };
+    std::vector<Pending> pending;
+    std::map<std::string, q1g::ProfTotals> totals;
+
+    q1g_state(int nbits_, uint64_t nshots_, int prec_);
+    ~q1g_state();
+
+    size_t bsz() const { return q1g::amp_bytes(prec); }
+    uint64_t total() const { return ncols * N; }
+    char* col_ptr(uint64_t c) const { return amps.as<char>() + c * N * bsz(); }
+
+    // Launch through `f` (returning cudaError_t), timed when profiling.
+    template <class F>
+    void launch(const char* name, double bytes, F f)
+    {
+        cudaEvent_t a = nullptr, b = nullptr;
+        if (prof) {
+            q1g::check_cuda(cudaEventCreate(&a), "cudaEventCreate");
+            q1g::check_cuda(cudaEventRecord(a, stream), "cudaEventRecord");
+        }
+        q1g::check_cuda(f(), name);
+        if (prof) {
+            q1g::check_cuda(cudaEventCreate(&b), "cudaEventCreate");
+            q1g::check_cuda(cudaEventRecord(b, stream), "cudaEventRecord");
+            pending.push_back({name, bytes, a, b});
+        }
+    }
+    void collect_profile();
+
+    void ensure_dense();
+    void apply_op(const q1g::GateOp& op, char* base, uint64_t total_amps);
+    void apply_gate(const double* mat, size_t k, const size_t* bits, size_t nbits_given);
+    void apply_conditional(const uint8_t* control, size_t ncontrol, const double* mat, size_t k,
+                           const size_t* bits, size_t nbits_given);
+    std::vector<double> zero_weights(size_t qbit);
+    void measure(size_t qbit, size_t cbit, uint64_t* res, size_t res_len, const double* uniforms,
+                 size_t nu, q1g_rng* rng, bool collapse);
+    void measure_all(const size_t* cbits, size_t ncbits, uint64_t* res, size_t res_len,
+                     const double* uniforms, size_t nu, q1g_rng* rng, bool collapse);
+    void reset_all();
+    void download(double* out, size_t len);
+    void sync();
+};
+
+struct q1g_plan {
+    int nbits = 0;
+    int width = 0;
+    std::vector<std::vector<int>> gate_bits;
+    std::vector<size_t> mat_off;   // offset (doubles) of each gate's matrix
+    size_t mat_doubles = 0;
+    std::vector<q1g::FusedBlock> blocks;
+    q1g::HostBuf hmats;            // pinned staging of dense matrices
+    q1g::DevBuf dmats;
+    cudaEvent_t staged = nullptr;  // last upload of hmats finished
+    ~q1g_plan();
+};
+
+namespace q1g {
+void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n);
+}

@@ -1,0 +1,253 @@
+// Gate classification and fusion (host side).
+#include "gate_plan.h"
+
+#include <algorithm>
+#include <stdexcept>
+
+#include "engine.h"
+
+namespace q1g {
+
+uint64_t GateOp::touched(uint64_t total) const
+{
+    const uint64_t units = total >> map.nz;
+    switch (kind) {
+        case Pair: return 2 * units;
+        case Phase: return units;
+        case Dense: return (uint64_t(1) << t) * units;
+        default: return 0;
+    }
+}
+
+GateOp classify(const cd* mat, int k, const int* bits, int nbits)
+{
+    if (k < 0 || k > kMaxMapBits)
+        throw Error(Q1G_ERR_INVALID_ARGUMENT, "gates on more than 12 qubits are not supported");
+    const int dim = 1 << k;
+    auto M = [&](int r, int c) { return mat[(size_t)r * dim + c]; };
+    auto gbit = [&](int x, int m) { return (x >> (k - 1 - m)) & 1; };
+
+    std::vector<int> ctrl, tgt;
+    for (int m = 0; m < k; ++m) {
+        bool is_ctrl = true;
+        for (int r = 0; r < dim && is_ctrl; ++r)
+            for (int c = 0; c < dim; ++c)
+                if (gbit(r, m) == 0 || gbit(c, m) == 0) {
+                    const cd expect = r == c ? cd(1.0, 0.0) : cd(0.0, 0.0);
+                    if (M(r, c) != expect) {
+                        is_ctrl = false;
+                        break;
+                    }
+                }
+        (is_ctrl ? ctrl : tgt).push_back(m);
+    }
+    const int t = (int)tgt.size();
+    int cpat = 0;
+    for (int m : ctrl) cpat |= 1 << (k - 1 - m);
+    auto full_index = [&](int s) {
+        int x = cpat;
+        for (int j = 0; j < t; ++j)
+            if ((s >> (t - 1 - j)) & 1) x |= 1 << (k - 1 - tgt[j]);
+        return x;
+    };
+    auto pos = [&](int m) { return nbits - 1 - bits[m]; };
+    auto offset = [&](int s) {
+        uint64_t o = 0;
+        for (int j = 0; j < t; ++j)
+            if ((s >> (t - 1 - j)) & 1) o |= uint64_t(1) << pos(tgt[j]);
+        return o;
+    };
+
+    GateOp op;
+    op.k = k;
+    op.map.nz = k;
+    for (int m = 0; m < k; ++m) op.map.zpos[m] = pos(m);
+    std::sort(op.map.zpos, op.map.zpos + k);
+    op.map.setmask = 0;
+    for (int m : ctrl) op.map.setmask |= uint64_t(1) << pos(m);
+
+    const int tdim = 1 << t;
+    std::vector<cd> G((size_t)tdim * tdim);
+    for (int r = 0; r < tdim; ++r)
+        for (int c = 0; c < tdim; ++c) G[(size_t)r * tdim + c] = M(full_index(r), full_index(c));
+
+    std::vector<int> nonfixed;
+    for (int s = 0; s < tdim; ++s) {
+        bool fixed = G[(size_t)s * tdim + s] == cd(1.0, 0.0);
+        for (int o = 0; o < tdim && fixed; ++o)
+            if (o != s && (G[(size_t)s * tdim + o] != cd(0.0, 0.0) || G[(size_t)o * tdim + s] != cd(0.0, 0.0)))
+                fixed = false;
+        if (!fixed) nonfixed.push_back(s);
+    }
+    if (nonfixed.empty()) {
+        op.kind = GateOp::Noop;
+    } else if (nonfixed.size() == 1) {
+        const int s = nonfixed[0];
+        op.kind = GateOp::Phase;
+        op.map.setmask |= offset(s);
+        const cd g = G[(size_t)s * tdim + s];
+        op.ph[0] = g.real();
+        op.ph[1] = g.imag();
+    } else if (nonfixed.size() == 2) {
+        const int s0 = nonfixed[0], s1 = nonfixed[1];
+        op.kind = GateOp::Pair;
+        op.o0 = offset(s0);
+        op.o1 = offset(s1);
+        const cd e[4] = {G[(size_t)s0 * tdim + s0], G[(size_t)s0 * tdim + s1],
+                         G[(size_t)s1 * tdim + s0], G[(size_t)s1 * tdim + s1]};
+        for (int q = 0; q < 4; ++q) {
+            op.m2[2 * q] = e[q].real();
+            op.m2[2 * q + 1] = e[q].imag();
+        }
+    } else {
+        if (t > 5)
+            throw Error(Q1G_ERR_INVALID_ARGUMENT,
+                        "a gate acting densely on more than 5 non-control qubits is not supported");
+        op.kind = GateOp::Dense;
+        op.t = t;
+        for (int s = 0; s < tdim; ++s) op.offs.off[s] = offset(s);
+        op.dense = G;
+    }
+    return op;
+}
+
+std::vector<cd> embed_matrix(const std::vector<cd>& mat, const std::vector<int>& bits,
+                             const std::vector<int>& qubits)
+{
+    const int k = (int)bits.size();
+    const int m = (int)qubits.size();
+    const int dim = 1 << m;
+    std::vector<int> bpos(k);  // position (within the block index) of gate bit j
+    for (int j = 0; j < k; ++j) {
+        auto it = std::find(qubits.begin(), qubits.end(), bits[j]);
+        bpos[j] = m - 1 - (int)(it - qubits.begin());
+    }
+    int gmask = 0;
+    for (int j = 0; j < k; ++j) gmask |= 1 << bpos[j];
+    const int gdim = 1 << k;
+    std::vector<cd> full((size_t)dim * dim, cd(0.0, 0.0));
+    for (int col = 0; col < dim; ++col) {
+        int gin = 0;
+        for (int j = 0; j < k; ++j) gin |= ((col >> bpos[j]) & 1) << (k - 1 - j);
+        const int base = col & ~gmask;
+        for (int gout = 0; gout < gdim; ++gout) {
+            int row = base;
+            for (int j = 0; j < k; ++j) row |= ((gout >> (k - 1 - j)) & 1) << bpos[j];
+            full[(size_t)row * dim + col] += mat[(size_t)gout * gdim + gin];
+        }
+    }
+    return full;
+}
+
+std::vector<cd> block_matrix(const FusedBlock& b, const std::vector<SeqGate>& gates)
+{
+    const int dim = 1 << b.qubits.size();
+    std::vector<cd> acc((size_t)dim * dim, cd(0.0, 0.0));
+    for (int i = 0; i < dim; ++i) acc[(size_t)i * dim + i] = 1.0;
+    std::vector<cd> tmp((size_t)dim * dim);
+    for (int gi : b.gates) {
+        const auto e = embed_matrix(gates[gi].mat, gates[gi].bits, b.qubits);
+        for (int r = 0; r < dim; ++r)
+            for (int c = 0; c < dim; ++c) {
+                cd s(0.0, 0.0);
+                for (int q = 0; q < dim; ++q) s += e[(size_t)r * dim + q] * acc[(size_t)q * dim + c];
+                tmp[(size_t)r * dim + c] = s;
+            }
+        acc.swap(tmp);
+    }
+    return acc;
+}
+
+namespace {
+
+std::vector<int> set_union(const std::vector<int>& a, const std::vector<int>& b)
+{
+    std::vector<int> u;
+    std::set_union(a.begin(), a.end(), b.begin(), b.end(), std::back_inserter(u));
+    return u;
+}
+
+bool intersects(const std::vector<int>& a, const std::vector<int>& b)
+{
+    size_t i = 0, j = 0;
+    while (i < a.size() && j < b.size()) {
+        if (a[i] == b[j]) return true;
+        if (a[i] < b[j]) ++i; else ++j;
+    }
+    return false;
+}
+
+}  // namespace
+
+std::vector<FusedBlock> fuse(const std::vector<std::vector<int>>& gate_bits, int nbits, int width)
+{
+    std::vector<FusedBlock> out;
+    std::vector<FusedBlock> open;  // pairwise disjoint
+    for (int gi = 0; gi < (int)gate_bits.size(); ++gi) {
+        std::vector<int> q = gate_bits[gi];
+        std::sort(q.begin(), q.end());
+        std::vector<int> touched;
+        for (int b = 0; b < (int)open.size(); ++b)
+            if (intersects(open[b].qubits, q)) touched.push_back(b);
+        if (width <= 0 || (int)q.size() > width) {
+            for (int b : touched) out.push_back(open[b]);
+            for (int j = (int)touched.size() - 1; j >= 0; --j) open.erase(open.begin() + touched[j]);
+            out.push_back(FusedBlock{q, {gi}});
+            continue;
+        }
+        // keep the largest touched blocks that still fit with the gate
+        std::vector<int> order = touched;
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+            return open[a].qubits.size() > open[b].qubits.size();
+        });
+        std::vector<int> u = q;
+        std::vector<char> chosen(open.size(), 0);
+        for (int b : order) {
+            auto cand = set_union(u, open[b].qubits);
+            if ((int)cand.size() <= width) {
+                u = cand;
+                chosen[b] = 1;
+            }
+        }
+        FusedBlock merged;
+        merged.qubits = u;
+        std::vector<FusedBlock> keep;
+        for (int b = 0; b < (int)open.size(); ++b) {
+            const bool is_touched = std::find(touched.begin(), touched.end(), b) != touched.end();
+            if (!is_touched) {
+                keep.push_back(open[b]);
+            } else if (chosen[b]) {
+                merged.gates.insert(merged.gates.end(), open[b].gates.begin(), open[b].gates.end());
+            } else {
+                out.push_back(open[b]);  // must precede the gate
+            }
+        }
+        merged.gates.push_back(gi);
+        keep.push_back(merged);
+        open.swap(keep);
+    }
+    for (auto& b : open) out.push_back(b);
+
+    if (width <= 0) return out;
+    // Move each block back past disjoint blocks and merge it into the first
+    // earlier block whose union with it fits.
+    std::vector<FusedBlock> res;
+    for (auto& b : out) {
+        bool merged = false;
+        for (int e = (int)res.size() - 1; e >= 0; --e) {
+            auto u = set_union(res[e].qubits, b.qubits);
+            if ((int)u.size() <= width) {
+                res[e].qubits = u;
+                res[e].gates.insert(res[e].gates.end(), b.gates.begin(), b.gates.end());
+                merged = true;
+                break;
+            }
+            if (intersects(res[e].qubits, b.qubits)) break;
+        }
+        if (!merged) res.push_back(b);
+    }
+    (void)nbits;
+    return res;
+}
+
+}  // namespace q1g

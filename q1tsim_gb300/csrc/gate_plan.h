@@ -1,0 +1,66 @@
+// Host-side gate lowering: matrix classification and the gate-fusion pass.
+#pragma once
+
+#include <stdint.h>
+
+#include <complex>
+#include <vector>
+
+#include "kernels.h"
+
+namespace q1g {
+
+using cd = std::complex<double>;
+
+// A gate (or fused block) lowered onto kernel arguments.
+struct GateOp {
+    enum Kind { Noop, Pair, Phase, Dense } kind = Noop;
+    IndexMap map{};          // all gate positions zeroed, controls in setmask
+    uint64_t o0 = 0, o1 = 0; // Pair: offsets of the two touched basis states
+    double m2[8] = {0};      // Pair: 2x2 (re, im) row-major
+    double ph[2] = {1, 0};   // Phase
+    int t = 0;               // Dense: number of target qubits
+    DenseOffsets offs{};     // Dense: offsets of the 2^t target states
+    std::vector<cd> dense;   // Dense: 2^t x 2^t row-major
+    int k = 0;               // gate qubits including controls
+    // Amplitudes read and written per launch over `total` amplitudes.
+    uint64_t touched(uint64_t total) const;
+};
+
+// Classify the 2^k x 2^k matrix `mat` acting on qubits `bits` (bits[0] is the
+// most significant bit of the matrix index, src/gates.rs:40-53) of an
+// nbits-qubit state: control qubits (identity whenever the bit is 0) move
+// into the index map, basis states the gate leaves fixed are dropped, and
+// what remains is a Phase (one state), a Pair (two) or a Dense update.
+GateOp classify(const cd* mat, int k, const int* bits, int nbits);
+
+// A gate of a sequence: qubits and matrix.
+struct SeqGate {
+    std::vector<int> bits;
+    std::vector<cd> mat;   // 2^k x 2^k row-major
+};
+
+// Fusion: the gate list grouped into blocks of at most `width` qubits.  A
+// block's qubits are ascending (first = most significant matrix bit) and its
+// gates are the sequence indices it absorbed, in order.
+struct FusedBlock {
+    std::vector<int> qubits;
+    std::vector<int> gates;
+};
+
+// Greedy fusion over open blocks on disjoint qubit sets: a gate joins the
+// open blocks it touches when their union fits in `width` qubits; otherwise
+// the largest subset that fits is kept and the other touched blocks are
+// emitted first.  A final pass merges an emitted block into an earlier one
+// when every block in between is disjoint from it.  Only the qubit lists are
+// used, so the grouping can be computed once per circuit structure.
+std::vector<FusedBlock> fuse(const std::vector<std::vector<int>>& gate_bits, int nbits, int width);
+
+// Matrix of a block: product of its gates' matrices embedded on its qubits.
+std::vector<cd> block_matrix(const FusedBlock& b, const std::vector<SeqGate>& gates);
+
+// Embed `mat` on `bits` into the 2^|qubits| space of `qubits`.
+std::vector<cd> embed_matrix(const std::vector<cd>& mat, const std::vector<int>& bits,
+                             const std::vector<int>& qubits);
+
+}  // namespace q1g

@@ -1,0 +1,92 @@
+// Host-side launch interface of the engine's CUDA kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace q1g {
+
+constexpr int kC128 = 0;   // complex128 amplitudes, FP64 arithmetic
+constexpr int kC64 = 1;    // complex64 amplitudes, FP32 arithmetic
+
+inline size_t amp_bytes(int prec) { return prec == kC128 ? 16 : 8; }
+
+// Offsets of the 2^t target basis states of a DENSE update (t <= 5).
+struct DenseOffsets {
+    uint64_t off[32];
+};
+
+// ---- gate_kernels.cu: one gate per pass over `total` amplitudes
+cudaError_t launch_pair(void* amps, int prec, uint64_t total, const IndexMap& map,
+                        uint64_t o0, uint64_t o1, const double* m /*2x2 (re,im)*/,
+                        cudaStream_t st);
+cudaError_t launch_phase(void* amps, int prec, uint64_t total, const IndexMap& map,
+                         double ph_re, double ph_im, cudaStream_t st);
+// dmat: device matrix 2^tb x 2^tb, complex in the state's precision.
+cudaError_t launch_dense(void* amps, int prec, uint64_t total, const IndexMap& map,
+                         const DenseOffsets& offs, int tb, const void* dmat, cudaStream_t st);
+
+// ---- state_kernels.cu: construction, conversion, collapse
+cudaError_t launch_fill_basis(void* amps, int prec, uint64_t n_amps, const uint64_t* d_col_index,
+                              uint64_t ncols, uint64_t col_len, cudaStream_t st);
+cudaError_t launch_product_state(void* amps, int prec, int nbits, const double* d_coefs,
+                                 cudaStream_t st);
+cudaError_t launch_convert_c128_to_c64(float2* dst, const double2* src, uint64_t n, cudaStream_t st);
+cudaError_t launch_convert_c64_to_c128(double2* dst, const float2* src, uint64_t n, cudaStream_t st);
+// New column j = old column src_col[j] with amplitudes whose bit `pos` differs
+// from keep[j] zeroed and the rest scaled by scale[j] (src/vectorstate.rs:91-104).
+struct CollapseCol {
+    uint64_t src_col;
+    int keep;       // 0 or 1: the measured value this column keeps; -1: plain copy
+    double scale;
+};
+cudaError_t launch_collapse_copy(void* dst, const void* src, int prec, uint64_t col_len, int pos,
+                                 const CollapseCol* d_cols, uint64_t ncols, cudaStream_t st);
+
+// ---- measure_kernels.cu
+// Per-chunk FP64 sums of |a|^2.  The kernel walks `units` virtual indices j,
+// reads amplitude expand_index(j, map) (so a map with zeroed positions reads
+// only that sub-lattice, e.g. the qubit=0 half), and sums chunks of `chunk`
+// consecutive j; chunk must divide the virtual column length.
+cudaError_t launch_chunk_sums(const void* amps, int prec, uint64_t units, uint64_t chunk,
+                              const IndexMap& map, double* out, cudaStream_t st);
+// Deterministic per-segment reduction: out[s] = sum of in[s*len .. (s+1)*len).
+cudaError_t launch_segment_sums(const double* in, uint64_t nseg, uint64_t len, double* out,
+                                cudaStream_t st);
+// In-place exclusive prefix sum of n doubles; *total_out (device) = the sum.
+// `tmp` must hold scan_tmp_doubles(n) doubles.
+uint64_t scan_tmp_doubles(uint64_t n);
+cudaError_t launch_exclusive_scan(double* data, uint64_t n, double* tmp, double* total_out,
+                                  cudaStream_t st);
+// Ascending uniforms by normalised exponential spacings from the SplitMix64
+// stream (seed, counter0): out[j] = S_j / S_m, S_j = sum_{k<=j} -log1p(-u_k),
+// for j < m, drawing m+1 uniforms.
+// tmp: 2*(m+1) + scan_tmp_doubles(m+1) + 1 doubles.
+cudaError_t launch_sorted_uniforms(uint64_t seed, uint64_t counter0, uint64_t m, double* out,
+                                   double* tmp, cudaStream_t st);
+// One warp per run: outcome[r] = first index i of the column with inclusive
+// prefix > u[r] * total, found through the chunk prefix (excl) and a warp
+// scan of the chunk; word[r] = classical word of the outcome.
+struct SampleArgs {
+    const void* amps;       // the column
+    int prec;
+    uint64_t col_len;       // 2^n
+    uint64_t chunk;
+    const double* excl;     // exclusive chunk prefix, nchunks entries
+    uint64_t nchunks;
+    const double* total;    // device scalar
+    const double* u;        // sorted uniforms of the column's runs
+    uint64_t nruns;
+    uint64_t* outcome;      // per run
+    uint64_t* word;         // per run
+    int nbits;
+    const uint64_t* d_cbit_of_pos;  // classical bit mask for each bit position
+};
+cudaError_t launch_sample(const SampleArgs& a, cudaStream_t st);
+// Per-block partials (6 doubles per block) comparing two states.
+cudaError_t launch_compare(const void* a, int prec_a, const void* b, int prec_b, uint64_t n,
+                           double* part, unsigned blocks, cudaStream_t st);
+
+}  // namespace q1g

@@ -1,0 +1,146 @@
+// State construction, precision conversion and measurement collapse kernels.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace q1g {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+inline unsigned blocks_for(uint64_t n, int per_block)
+{
+    uint64_t g = (n + per_block - 1) / per_block;
+    if (g > 0x7fffffffULL) g = 0x7fffffffULL;
+    return (unsigned)(g ? g : 1);
+}
+
+template <typename T>
+__global__ void k_set_basis(T* a, const uint64_t* col_index, uint64_t ncols, uint64_t col_len)
+{
+    uint64_t c = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (c < ncols) a[c * col_len + col_index[c]] = cmake<T>(1.0, 0.0);
+}
+
+// amp(i) = c_0[b_0] * c_1[b_1] * ... multiplied left to right, b_q the bit of
+// qubit q (position n-1-q) -- the kron chain of src/vectorstate.rs:68-74.
+template <typename T>
+__global__ void k_product_state(T* a, int nbits, const double* coefs)
+{
+    const uint64_t n = uint64_t(1) << nbits;
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
+        double re = 1.0, im = 0.0;
+        for (int q = 0; q < nbits; ++q) {
+            const int b = (i >> (nbits - 1 - q)) & 1;
+            const double cr = coefs[4 * q + 2 * b], ci = coefs[4 * q + 2 * b + 1];
+            const double nr = cr * re - ci * im;
+            const double ni = cr * im + ci * re;
+            re = nr;
+            im = ni;
+        }
+        a[i] = cmake<T>(re, im);
+    }
+}
+
+__global__ void k_c128_to_c64(float2* dst, const double2* src, uint64_t n)
+{
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
+        double2 v = src[i];
+        dst[i] = make_float2((float)v.x, (float)v.y);
+    }
+}
+
+__global__ void k_c64_to_c128(double2* dst, const float2* src, uint64_t n)
+{
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
+        float2 v = src[i];
+        dst[i] = make_double2(v.x, v.y);
+    }
+}
+
+template <typename T, typename R>
+__global__ void k_collapse_copy(T* dst, const T* src, uint64_t col_len,
+                                int pos, const CollapseCol* __restrict__ cols, uint64_t ncols)
+{
+    const uint64_t total = col_len * ncols;
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    for (uint64_t g = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; g < total; g += stride) {
+        const uint64_t j = g / col_len;
+        const uint64_t i = g - j * col_len;
+        const CollapseCol c = cols[j];
+        T v = src[c.src_col * col_len + i];
+        if (c.keep >= 0) {
+            if ((int)((i >> pos) & 1) != c.keep) {
+                v.x = R(0);
+                v.y = R(0);
+            } else {
+                v.x = v.x * R(c.scale);
+                v.y = v.y * R(c.scale);
+            }
+        }
+        dst[g] = v;
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_fill_basis(void* amps, int prec, uint64_t n_amps, const uint64_t* d_col_index,
+                              uint64_t ncols, uint64_t col_len, cudaStream_t st)
+{
+    cudaError_t e = cudaMemsetAsync(amps, 0, n_amps * amp_bytes(prec), st);
+    if (e != cudaSuccess) return e;
+    if (ncols == 0) return cudaSuccess;
+    if (prec == kC128)
+        k_set_basis<double2><<<blocks_for(ncols, kThreads), kThreads, 0, st>>>(
+            (double2*)amps, d_col_index, ncols, col_len);
+    else
+        k_set_basis<float2><<<blocks_for(ncols, kThreads), kThreads, 0, st>>>(
+            (float2*)amps, d_col_index, ncols, col_len);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_product_state(void* amps, int prec, int nbits, const double* d_coefs,
+                                 cudaStream_t st)
+{
+    const uint64_t n = uint64_t(1) << nbits;
+    const unsigned grid = blocks_for(n, kThreads) > 152 * 64 ? 152 * 64 : blocks_for(n, kThreads);
+    if (prec == kC128)
+        k_product_state<double2><<<grid, kThreads, 0, st>>>((double2*)amps, nbits, d_coefs);
+    else
+        k_product_state<float2><<<grid, kThreads, 0, st>>>((float2*)amps, nbits, d_coefs);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_convert_c128_to_c64(float2* dst, const double2* src, uint64_t n, cudaStream_t st)
+{
+    const unsigned grid = blocks_for(n, kThreads) > 152 * 64 ? 152 * 64 : blocks_for(n, kThreads);
+    k_c128_to_c64<<<grid, kThreads, 0, st>>>(dst, src, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_convert_c64_to_c128(double2* dst, const float2* src, uint64_t n, cudaStream_t st)
+{
+    const unsigned grid = blocks_for(n, kThreads) > 152 * 64 ? 152 * 64 : blocks_for(n, kThreads);
+    k_c64_to_c128<<<grid, kThreads, 0, st>>>(dst, src, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_collapse_copy(void* dst, const void* src, int prec, uint64_t col_len, int pos,
+                                 const CollapseCol* d_cols, uint64_t ncols, cudaStream_t st)
+{
+    const uint64_t total = col_len * ncols;
+    if (total == 0) return cudaSuccess;
+    const unsigned grid = blocks_for(total, kThreads) > 152 * 64 ? 152 * 64 : blocks_for(total, kThreads);
+    if (prec == kC128)
+        k_collapse_copy<double2, double><<<grid, kThreads, 0, st>>>(
+            (double2*)dst, (const double2*)src, col_len, pos, d_cols, ncols);
+    else
+        k_collapse_copy<float2, float><<<grid, kThreads, 0, st>>>(
+            (float2*)dst, (const float2*)src, col_len, pos, d_cols, ncols);
+    return cudaGetLastError();
+}
+
+}  // namespace q1g

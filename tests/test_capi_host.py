@@ -1,0 +1,116 @@
+"""The C-ABI library: builds, loads and exports every declared symbol; the
+host-only parts of the ABI (plans and the fusion pass) work without a GPU.
+No kernel is launched here."""
+import ctypes
+import itertools
+
+import numpy as np
+import pytest
+
+from q1tsim_gb300 import _lib, build
+from q1tsim_gb300 import gates as G
+from q1tsim_gb300.vectorstate import Plan
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return _lib.load()
+
+
+def test_exports_every_declared_symbol(lib):
+    declared = _lib.declared_symbols()
+    assert len(declared) >= 29
+    for name in declared:
+        assert hasattr(lib, name), name
+
+
+def test_version_and_last_error(lib):
+    assert lib.q1g_version() >= 100
+    assert lib.q1g_last_error() is not None
+
+
+def test_null_arguments_are_errors_not_crashes(lib):
+    assert lib.q1g_state_new(3, 1, 0, None) == _lib.InvalidArgument.code
+    assert b"NULL" in lib.q1g_last_error()
+    h = ctypes.c_void_p()
+    assert lib.q1g_state_new(3, 1, 7, ctypes.byref(h)) == _lib.InvalidArgument.code
+    assert lib.q1g_plan_create(4, 1, None, None, 0, ctypes.byref(h)) == _lib.InvalidArgument.code
+    with pytest.raises(_lib.InvalidQBit):
+        Plan(3, [[0, 5]])
+    with pytest.raises(_lib.InvalidArgument):
+        Plan(3, [[0]], fusion_width=7)
+
+
+def _commutes_ok(gate_bits, blocks):
+    """Every gate appears once, and two gates sharing a qubit keep their
+    relative order in the flattened block sequence."""
+    flat = [g for _, gs in blocks for g in gs]
+    assert sorted(flat) == list(range(len(gate_bits)))
+    pos = {g: i for i, g in enumerate(flat)}
+    for a, b in itertools.combinations(range(len(gate_bits)), 2):
+        if set(gate_bits[a]) & set(gate_bits[b]):
+            assert pos[a] < pos[b], (a, b)
+    for qb, gs in blocks:
+        assert set(q for g in gs for q in gate_bits[g]) <= set(qb)
+
+
+def brick(n, depth):
+    bits = []
+    for layer in range(depth):
+        bits += [[q] for q in range(n)]
+        start = 0 if layer % 2 == 0 else 1
+        bits += [[q, q + 1] for q in range(start, n - 1, 2)]
+    return bits
+
+
+@pytest.mark.parametrize("width", [1, 2, 3, 4, 5])
+def test_fusion_respects_order_and_width(lib, width):
+    rng = np.random.default_rng(width)
+    for n in (4, 9, 16):
+        gb = brick(n, 6)
+        for _ in range(40):
+            k = int(rng.integers(1, 4))
+            gb.append([int(q) for q in rng.choice(n, size=k, replace=False)])
+        p = Plan(n, gb, fusion_width=width)
+        blocks = p.blocks()
+        _commutes_ok(gb, blocks)
+        for qb, gs in blocks:
+            assert len(qb) <= max(width, max(len(gb[g]) for g in gs))
+        assert p.nblocks < len(gb)
+
+
+def test_fusion_product_equals_sequence(lib):
+    """The fused blocks, multiplied out on the host, give the same unitary as
+    the gate sequence (numpy, 6 qubits)."""
+    n = 6
+    rng = np.random.default_rng(3)
+    gates = []
+    for _ in range(60):
+        if rng.random() < 0.6:
+            q = int(rng.integers(n))
+            gates.append((G.U3(*rng.uniform(0, 6.28, 3)), [q]))
+        else:
+            a, b = (int(v) for v in rng.choice(n, 2, replace=False))
+            gates.append((G.CX(), [a, b]))
+    seq = np.eye(1 << n, dtype=complex)
+    for g, b in gates:
+        seq = G.embed(g.matrix(), b, n) @ seq
+    p = Plan(n, [b for _, b in gates], fusion_width=4)
+    fused = np.eye(1 << n, dtype=complex)
+    for qb, gs in p.blocks():
+        blk = np.eye(1 << len(qb), dtype=complex)
+        for gi in gs:
+            g, b = gates[gi]
+            local = [qb.index(q) for q in b]
+            blk = G.embed(g.matrix(), local, len(qb)) @ blk
+        fused = G.embed(blk, qb, n) @ fused
+    np.testing.assert_allclose(fused, seq, atol=1e-12)
+    assert p.nblocks < len(gates) // 2
+
+
+def test_plain_plan_is_one_pass_per_gate(lib):
+    gb = brick(8, 3)
+    p = Plan(8, gb, fusion_width=0)
+    assert p.nblocks == len(gb)
+    assert [gs for _, gs in p.blocks()] == [[i] for i in range(len(gb))]

@@ -1,0 +1,456 @@
+"""Parity of the CUDA engine with the CPU oracle, through the C ABI.
+
+complex128 mode: max |d amp| <= 1e-12 against the oracle and identical shot
+outcomes for identical uniforms.  complex64 mode (plain and fused):
+max |d amp| <= 2e-6 on normalised states and 1 - fidelity <= 1e-6.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+from q1tsim_gb300 import Circuit, Plan, Rng, VectorState
+from q1tsim_gb300 import _lib
+from q1tsim_gb300 import gates as G
+from refcheck import dec, kats, measurement_ok
+
+pytestmark = pytest.mark.gpu
+
+TOL128 = 1e-12
+TOL64 = 2e-6
+K = kats()
+
+
+def rand_state(n, rng):
+    a = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    return a / np.linalg.norm(a)
+
+
+def pair(n, shots, amps=None, prec="c128"):
+    if amps is None:
+        return orc.OracleState.new(n, shots), VectorState(n, shots, prec)
+    return orc.OracleState.from_amplitudes(amps, shots), VectorState.from_amplitudes(amps, shots, prec)
+
+
+def same(o, g, tol=TOL128):
+    assert g.counts == o.counts
+    so, sg = o.states(), g.states()
+    assert so.shape == sg.shape
+    np.testing.assert_allclose(sg, so, rtol=0, atol=tol)
+
+
+def random_gate(n, rng):
+    kinds = ["u3", "h", "x", "y", "z", "s", "t", "rz", "rx", "v", "cx", "cz", "cy", "ch", "cu1",
+             "crz", "swap", "ccx", "ccz", "kron", "u3u3", "dense3", "cu3"]
+    if n < 3:
+        kinds = [k for k in kinds if k not in ("ccx", "ccz", "dense3")]
+    if n < 2:
+        kinds = [k for k in kinds if k in ("u3", "h", "x", "y", "z", "s", "t", "rz", "rx", "v")]
+    k = kinds[rng.integers(len(kinds))]
+    ang = rng.uniform(0, 2 * np.pi, 3)
+    one = {"u3": G.U3(*ang), "h": G.H(), "x": G.X(), "y": G.Y(), "z": G.Z(), "s": G.S(), "t": G.T(),
+           "rz": G.RZ(ang[0]), "rx": G.RX(ang[0]), "v": G.V()}
+    if k in one:
+        return one[k], [int(rng.integers(n))]
+    if k in ("cx", "cz", "cy", "ch", "cu1", "crz", "swap", "kron", "u3u3", "cu3"):
+        b = [int(v) for v in rng.choice(n, 2, replace=False)]
+        g = {"cx": G.CX(), "cz": G.CZ(), "cy": G.CY(), "ch": G.CH(), "cu1": G.CU1(ang[0]),
+             "crz": G.CRZ(ang[1]), "swap": G.Swap(), "kron": G.Kron(G.H(), G.H()),
+             "u3u3": G.Kron(G.U3(*ang), G.RY(ang[1])), "cu3": G.CU3(*ang)}[k]
+        return g, b
+    b = [int(v) for v in rng.choice(n, 3, replace=False)]
+    if k == "ccx":
+        return G.CCX(), b
+    if k == "ccz":
+        return G.CCZ(), b
+    c = G.Composite("d3", 3, [(G.U3(*ang), [0]), (G.CX(), [0, 1]), (G.U3(*ang[::-1]), [2]),
+                              (G.CZ(), [1, 2]), (G.H(), [1])])
+    return c, b
+
+
+# ------------------------------------------------------------------ KATs
+
+@pytest.mark.parametrize("prec,tol", [("c128", 1e-14), ("c64", TOL64)])
+@pytest.mark.parametrize("case", K["vectorstate"], ids=lambda c: c["name"])
+def test_vectorstate_kats_on_gpu(case, prec, tol):
+    init = case["init"]
+    if init["kind"] == "new":
+        s = VectorState(init["nr_bits"], init["nr_shots"], prec)
+    else:
+        s = VectorState.from_qubit_coefs(dec(init["coefs"]), init["nr_shots"], prec)
+    for op in case["ops"]:
+        if op["op"] == "gate":
+            s.apply_gate(dec(op["mat"]), op["bits"])
+        elif op["op"] == "cond":
+            s.apply_conditional_gate(op["control"], dec(op["mat"]), op["bits"])
+        else:
+            s.reset_all()
+    assert s.counts == case["expect"]["counts"]
+    np.testing.assert_allclose(s.states(), dec(case["expect"]["states"]), rtol=0, atol=tol)
+
+
+@pytest.mark.parametrize("case", K["apply"], ids=lambda c: c["gate"] + "@" + c["source"])
+def test_gate_apply_kats_on_gpu(case):
+    state, expect, mat = dec(case["state"]), dec(case["expect"]), dec(case["mat"])
+    for c in range(state.shape[1]):
+        s = VectorState.from_amplitudes(state[:, c], 1)
+        s.apply_gate(mat, case["bits"])
+        np.testing.assert_allclose(s.states()[:, 0], expect[:, c], rtol=0, atol=1e-14)
+
+
+# ------------------------------------------------------ random circuits
+
+@pytest.mark.parametrize("n", [1, 2, 3, 5, 8, 11, 13])
+def test_random_gates_c128_match_oracle(n):
+    rng = np.random.default_rng(100 + n)
+    amps = rand_state(n, rng)
+    o, g = pair(n, 64, amps)
+    for _ in range(60):
+        gate, bits = random_gate(n, rng)
+        o.apply_gate(gate.matrix(), bits)
+        g.apply_gate(gate, bits)
+    same(o, g)
+
+
+@pytest.mark.parametrize("n", [2, 6, 12])
+def test_random_gates_c64_match_oracle(n):
+    rng = np.random.default_rng(200 + n)
+    amps = rand_state(n, rng)
+    o, g = pair(n, 64, amps, "c64")
+    for _ in range(40):
+        gate, bits = random_gate(n, rng)
+        o.apply_gate(gate.matrix(), bits)
+        g.apply_gate(gate, bits)
+    so, sg = o.states()[:, 0], g.states()[:, 0]
+    assert np.max(np.abs(so - sg)) <= TOL64
+    assert 1 - abs(np.vdot(so, sg)) ** 2 <= 1e-6
+
+
+def test_multi_column_gates_and_conditionals():
+    """Gates act on every column; conditional gates split columns by run
+    (src/vectorstate.rs:193-227)."""
+    rng = np.random.default_rng(5)
+    n, shots = 7, 40
+    o, g = pair(n, shots, rand_state(n, rng))
+    for step in range(6):
+        control = rng.integers(0, 2, shots).astype(np.uint8)
+        gate, bits = random_gate(n, rng)
+        o.apply_conditional_gate(control, gate.matrix(), bits)
+        g.apply_conditional_gate(control, gate, bits)
+        same(o, g)
+        gate, bits = random_gate(n, rng)
+        o.apply_gate(gate.matrix(), bits)
+        g.apply_gate(gate, bits)
+        same(o, g)
+    assert len(g.counts) > 1
+
+
+# ---------------------------------------------------------- measurement
+
+@pytest.mark.parametrize("prec", ["c128", "c64"])
+def test_measure_into_identical_outcomes(prec):
+    rng = np.random.default_rng(9)
+    n, shots = 9, 500
+    o, g = pair(n, shots, rand_state(n, rng), prec)
+    ro = np.zeros(shots, dtype=np.uint64)
+    rg = np.zeros(shots, dtype=np.uint64)
+    for step in range(8):
+        q = int(rng.integers(n))
+        cb = int(rng.integers(8))
+        u = rng.random(len(o.counts))
+        if step % 3 == 2:
+            o.peek_into(q, cb, ro, uniforms=u)
+            g.peek_into(q, cb, rg, uniforms=u)
+        else:
+            o.measure_into(q, cb, ro, uniforms=u)
+            g.measure_into(q, cb, rg, uniforms=u)
+        assert np.array_equal(ro, rg)
+        assert g.counts == o.counts
+        gate, bits = random_gate(n, rng)
+        o.apply_gate(gate.matrix(), bits)
+        g.apply_gate(gate, bits)
+        if prec == "c128":
+            same(o, g)
+        else:
+            np.testing.assert_allclose(g.states(), o.states(), atol=1e-5)
+
+
+@pytest.mark.parametrize("prec", ["c128", "c64"])
+@pytest.mark.parametrize("n", [1, 4, 10, 14])
+def test_measure_all_identical_outcomes(prec, n):
+    rng = np.random.default_rng(30 + n)
+    shots = 3000
+    o, g = pair(n, shots, rand_state(n, rng), prec)
+    # split into a few columns first
+    u0 = rng.random(1)
+    ro = np.zeros(shots, dtype=np.uint64)
+    rg = np.zeros(shots, dtype=np.uint64)
+    o.measure_into(0, 40, ro, uniforms=u0)
+    g.measure_into(0, 40, rg, uniforms=u0)
+    cbits = [int(c) for c in rng.permutation(n)]
+    u = rng.random(shots)
+    o.peek_all_into(cbits, ro, uniforms=u)
+    g.peek_all_into(cbits, rg, uniforms=u)
+    assert np.array_equal(ro, rg)
+    o.measure_all_into(cbits, ro, uniforms=u)
+    g.measure_all_into(cbits, rg, uniforms=u)
+    assert np.array_equal(ro, rg)
+    assert g.counts == o.counts
+    if (1 << n) * len(o.counts) <= (1 << 22):
+        np.testing.assert_allclose(g.states(), o.states(), atol=0)
+    # a gate after the collapse densifies the basis columns again
+    gate, bits = random_gate(n, rng)
+    o.apply_gate(gate.matrix(), bits)
+    g.apply_gate(gate, bits)
+    if (1 << n) * len(o.counts) <= (1 << 22):
+        np.testing.assert_allclose(g.states(), o.states(), atol=1e-12 if prec == "c128" else 1e-6)
+
+
+def test_rng_stream_matches_oracle():
+    """The device-generated sorted uniforms agree with the oracle's host
+    generation (same SplitMix64 stream); outcomes then agree except, with
+    vanishing probability, at FP rounding boundaries."""
+    rng = np.random.default_rng(77)
+    n, shots = 12, 20000
+    amps = rand_state(n, rng)
+    o, g = pair(n, shots, amps)
+    ro = np.zeros(shots, dtype=np.uint64)
+    rg = np.zeros(shots, dtype=np.uint64)
+    r1, r2 = orc.Rng(1234), Rng(1234)
+    o.peek_all_into(list(range(n)), ro, rng=r1)
+    g.peek_all_into(list(range(n)), rg, rng=r2)
+    assert r1.state[1] == r2.counter == shots + 1
+    assert np.mean(ro == rg) >= 0.999
+    # single-qubit measurement draws one uniform per column on the host
+    o.measure_into(3, 50, ro, rng=r1)
+    g.measure_into(3, 50, rg, rng=r2)
+    assert np.array_equal(ro >> np.uint64(50), rg >> np.uint64(50))
+
+
+def test_reset_and_reset_all_parity():
+    rng = np.random.default_rng(4)
+    n, shots = 6, 200
+    o, g = pair(n, shots, rand_state(n, rng))
+    for q in (0, 3, 5):
+        u = rng.random(len(o.counts))
+        o.reset(q, uniforms=u)
+        g.reset(q, uniforms=u)
+        same(o, g)
+    g.reset_all()
+    o.reset_all()
+    same(o, g)
+
+
+def test_measurement_statistics_large_shot_count():
+    """1e6 shots of a 20-qubit state: every qubit's marginal within the
+    reference's binomial bounds (src/stats.rs)."""
+    rng = np.random.default_rng(8)
+    n, shots = 20, 1_000_000
+    amps = rand_state(n, rng)
+    g = VectorState.from_amplitudes(amps, shots, "c64")
+    res = np.zeros(shots, dtype=np.uint64)
+    g.peek_all_into(list(range(n)), res, rng=Rng(5))
+    p = np.abs(amps) ** 2
+    idx = np.arange(1 << n)
+    for q in range(n):
+        p1 = p[((idx >> (n - 1 - q)) & 1) == 1].sum()
+        c1 = int(((res >> np.uint64(q)) & np.uint64(1)).sum())
+        assert measurement_ok(c1, shots, p1, 1e-6)
+
+
+# ------------------------------------------------------------- fusion
+
+@pytest.mark.parametrize("width", [2, 3, 4, 5])
+def test_fused_plans_match_plain(width):
+    rng = np.random.default_rng(width)
+    n = 13
+    amps = rand_state(n, rng)
+    gl = [random_gate(n, rng) for _ in range(80)]
+    mats = np.concatenate([np.ascontiguousarray(gt.matrix()).ravel() for gt, _ in gl]).view(np.float64)
+    o = orc.OracleState.from_amplitudes(amps, 1)
+    for gt, b in gl:
+        o.apply_gate(gt.matrix(), b)
+    ref = o.states()[:, 0]
+    for prec, tol in (("c128", TOL128), ("c64", TOL64)):
+        g = VectorState.from_amplitudes(amps, 1, prec)
+        p = Plan(n, [b for _, b in gl], width)
+        g.apply_plan(p, mats)
+        out = g.states()[:, 0]
+        assert np.max(np.abs(out - ref)) <= tol, (prec, np.max(np.abs(out - ref)))
+        assert 1 - abs(np.vdot(ref, out)) ** 2 <= 1e-6
+
+
+def test_plan_rerun_with_new_parameters():
+    """Matrices are re-read on every run (src/gates/parameter.rs:23-75)."""
+    n = 5
+    th = G.Parameter(0.3)
+    c = Circuit(n, n)
+    for q in range(n):
+        c.add_gate(G.RX(th), [q])
+    c.measure_all(list(range(n)))
+    c.execute(1000, Rng(1))
+    h0 = c.histogram()
+    th.assign(0.0)
+    c.execute(1000, Rng(1))
+    assert c.histogram() == {0: 1000}
+    assert h0 != {0: 1000}
+
+
+# ------------------------------------------------------------- circuits
+
+def test_circuit_execute_kat():
+    """src/circuit.rs:1455-1468"""
+    c = Circuit(2, 2)
+    c.add_gate(G.X(), [0])
+    c.add_gate(G.X(), [1])
+    c.add_gate(G.CX(), [0, 1])
+    c.measure(0, 0)
+    c.measure(1, 1)
+    c.execute(5, Rng(0))
+    assert list(c.cstate()) == [0b01] * 5
+
+
+def test_circuit_conditional_kat():
+    """src/circuit.rs:1619-1652 (c_state injected before reexecute)."""
+    c = Circuit(2, 2)
+    c.add_conditional_gate([0, 1], 1, G.X(), [1])
+    c.measure_all([0, 1])
+    c.execute(5, Rng(0))
+    assert list(c.cstate()) == [0] * 5
+    for control, target, qb, want in [([0, 1], 1, [1], [0b10, 0, 0, 0, 0]),
+                                      ([0, 1], 2, [1], [0, 0b10, 0b10, 0, 0]),
+                                      ([1], 1, [0], [0, 0b01, 0b01, 0b01, 0])]:
+        c = Circuit(2, 2)
+        c.q_state = VectorState(2, 5)
+        c.c_state = np.array([0b01, 0b10, 0b10, 0b11, 0b00], dtype=np.uint64)
+        c.add_conditional_gate(control, target, G.X(), qb)
+        c.measure_all([0, 1])
+        c.reexecute(Rng(1))
+        assert list(c.cstate()) == want
+
+
+def test_circuit_measure_all_and_basis_kats():
+    """src/circuit.rs:1654-1733"""
+    n = 1024
+    c = Circuit(2, 2)
+    c.x(0)
+    c.measure_all([0, 1])
+    c.execute(n, Rng(2))
+    assert c.histogram_vec() == [0, n, 0, 0]
+    c = Circuit(2, 2)
+    c.x(0)
+    c.measure_all([1, 0])
+    c.execute(n, Rng(2))
+    assert c.histogram_vec() == [0, 0, n, 0]
+    c = Circuit(2, 2)
+    c.h(0)
+    c.h(1)
+    c.measure_all([0, 1])
+    c.execute(n, Rng(3))
+    assert all(measurement_ok(v, n, 0.25) for v in c.histogram_vec())
+    c = Circuit(2, 2)
+    c.h(0)
+    c.h(1)
+    c.measure_all_basis([0, 1], "x")
+    c.execute(n, Rng(3))
+    assert c.histogram_vec() == [n, 0, 0, 0]
+    c = Circuit(2, 2)
+    c.x(0)
+    c.h(0)
+    c.h(1)
+    c.s(0)
+    c.s(1)
+    c.measure_all_basis([0, 1], "y")
+    c.execute(n, Rng(3))
+    assert c.histogram_vec() == [0, n, 0, 0]
+
+
+def test_circuit_peek_all_kat():
+    """src/circuit.rs:1736-1760"""
+    n = 1024
+    c = Circuit(1, 3)
+    c.h(0)
+    c.peek_all([0])
+    c.h(0)
+    c.peek_all([1])
+    c.h(0)
+    c.peek_all([2])
+    c.execute(n, Rng(4))
+    h = c.histogram_vec()
+    assert measurement_ok(h[0] + h[2] + h[4] + h[6], n, 0.5)
+    assert h[0] + h[1] + h[4] + h[5] == n
+    assert measurement_ok(h[0] + h[1] + h[2] + h[3], n, 0.5)
+
+
+def test_circuit_reset_and_histograms():
+    """src/circuit.rs:1851-1986"""
+    n = 1024
+    c = Circuit(2, 2)
+    c.h(0)
+    c.z(0)
+    c.x(1)
+    c.reset(0)
+    c.measure(0, 0)
+    c.measure(1, 1)
+    c.execute(n, Rng(6))
+    assert c.histogram_vec() == [0, 0, n, 0]
+    c = Circuit(5, 5)
+    c.h(0)
+    c.z(0)
+    c.x(4)
+    c.h(3)
+    c.reset_all()
+    c.measure_all([0, 1, 2, 3, 4])
+    c.execute(n, Rng(6))
+    h = c.histogram_vec()
+    assert h[0] == n and sum(h[1:]) == 0
+    c = Circuit(2, 2)
+    c.add_gate("H", [0])
+    c.add_gate("h", [1])
+    c.measure(0, 0)
+    c.measure(1, 1)
+    c.execute(4096, Rng(7))
+    hs = c.histogram_string()
+    assert sorted(hs) == ["00", "01", "10", "11"]
+    assert sum(hs.values()) == 4096
+    assert all(measurement_ok(v, 4096, 0.25) for v in hs.values())
+
+
+def test_circuit_gpu_equals_oracle_backend():
+    """The same Circuit op list executed by the oracle and by the GPU state
+    gives identical classical results for the same uniform stream."""
+    rng = np.random.default_rng(12)
+    n = 8
+    c = Circuit(n, n + 2)
+    for layer in range(6):
+        for q in range(n):
+            c.add_gate(G.U3(*rng.uniform(0, 6.28, 3)), [q])
+        for q in range(layer % 2, n - 1, 2):
+            c.cx(q, q + 1)
+        if layer == 2:
+            c.measure(3, n)
+            c.add_conditional_gate([n], 1, G.X(), [3])
+        if layer == 4:
+            c.measure(5, n + 1, "x")
+    c.measure_all(list(range(n)))
+    c.execute_with(2000, Rng(99), VectorState(n, 2000))
+    gpu = c.cstate().copy()
+    c.execute_with(2000, Rng(99), orc.OracleState.new(n, 2000))
+    assert np.array_equal(c.cstate(), gpu)
+
+
+# --------------------------------------------------------------- errors
+
+def test_error_codes_on_gpu():
+    s = VectorState(3, 4)
+    with pytest.raises(_lib.InvalidNrBits):
+        s.apply_gate(G.CX(), [0])
+    with pytest.raises(_lib.InvalidQBit):
+        s.apply_gate(G.H(), [3])
+    with pytest.raises(_lib.NotEnoughSpace):
+        s.measure_into(0, 0, np.zeros(2, dtype=np.uint64), Rng(0))
+    with pytest.raises(_lib.InvalidNrMeasurementBits):
+        s.measure_all_into([0, 1], np.zeros(4, dtype=np.uint64), Rng(0))
+    with pytest.raises(_lib.InvalidNrControlBits):
+        s.apply_conditional_gate([1, 0, 1], G.X(), [0])
+    with pytest.raises(_lib.InvalidQBit):
+        s.measure_into(5, 0, np.zeros(4, dtype=np.uint64), Rng(0))
