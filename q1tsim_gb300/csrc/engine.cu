@@ -8,6 +8,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 
 namespace q1g {
@@ -587,6 +588,58 @@ q1g_plan::~q1g_plan()
 
 namespace q1g {
 
+// Tensor-core lowering of one fused block: the block matrix on its qubits,
+// padded with untouched qubits to five, the tile geometry and the 32 KB
+// operand image.
+struct TcBlock {
+    IndexMap tilemap{};
+    TcOffsets offs{};
+    std::vector<float> image;
+};
+
+static TcBlock lower_tc(const std::vector<cd>& mat, const std::vector<int>& bits, int nbits)
+{
+    // pad with the lowest-numbered (highest-position) qubits the block leaves alone
+    std::vector<int> q = bits;
+    for (int cand = 0; (int)q.size() < 5 && cand < nbits; ++cand)
+        if (std::find(q.begin(), q.end(), cand) == q.end()) q.push_back(cand);
+    std::sort(q.begin(), q.end());
+    const auto m32 = embed_matrix(mat, bits, q);
+    std::vector<double> md(2 * 32 * 32);
+    for (size_t e = 0; e < m32.size(); ++e) {
+        md[2 * e] = m32[e].real();
+        md[2 * e + 1] = m32[e].imag();
+    }
+    TcBlock t;
+    t.image.assign(16384 / 4 * 2, 0.0f);
+    build_tc_image(md.data(), t.image.data());
+    std::vector<int> gpos(5);
+    for (int j = 0; j < 5; ++j) gpos[j] = nbits - 1 - q[j];
+    for (int g = 0; g < 32; ++g) {
+        uint64_t o = 0;
+        for (int j = 0; j < 5; ++j)
+            if ((g >> (4 - j)) & 1) o |= uint64_t(1) << gpos[j];
+        t.offs.goff[g] = o;
+    }
+    std::vector<int> rows;
+    for (int p = 0; (int)rows.size() < 7; ++p)
+        if (std::find(gpos.begin(), gpos.end(), p) == gpos.end()) rows.push_back(p);
+    for (int r = 0; r < 7; ++r) t.offs.rpos[r] = rows[r];
+    std::vector<int> z = gpos;
+    z.insert(z.end(), rows.begin(), rows.end());
+    std::sort(z.begin(), z.end());
+    t.tilemap.nz = 12;
+    for (int j = 0; j < 12; ++j) t.tilemap.zpos[j] = z[j];
+    t.tilemap.setmask = 0;
+    return t;
+}
+
+static bool tc_enabled()
+{
+    const char* e = std::getenv("Q1G_FUSED_KERNEL");
+    return !(e && std::string(e) == "simt");
+}
+
 void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n)
 {
     if (n != p->mat_doubles)
@@ -603,34 +656,53 @@ void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n)
         const double* m = mats + p->mat_off[g];
         for (size_t e = 0; e < dim * dim; ++e) gates[g].mat[e] = cd(m[2 * e], m[2 * e + 1]);
     }
+    const bool use_tc = s->prec == kC64 && s->nbits >= 12 && tc_enabled();
     std::vector<GateOp> ops;
+    std::vector<TcBlock> tcs;
+    std::vector<int> tc_of(p->blocks.size(), -1);
     ops.reserve(p->blocks.size());
-    for (const auto& b : p->blocks) {
+    for (size_t bi = 0; bi < p->blocks.size(); ++bi) {
+        const auto& b = p->blocks[bi];
+        std::vector<cd> m;
+        std::vector<int> bits;
         if (b.gates.size() == 1) {
-            const auto& g = gates[b.gates[0]];
-            ops.push_back(classify(g.mat.data(), (int)g.bits.size(), g.bits.data(), s->nbits));
+            m = gates[b.gates[0]].mat;
+            bits = gates[b.gates[0]].bits;
         } else {
-            const auto m = block_matrix(b, gates);
-            ops.push_back(classify(m.data(), (int)b.qubits.size(), b.qubits.data(), s->nbits));
+            m = block_matrix(b, gates);
+            bits = b.qubits;
+        }
+        ops.push_back(classify(m.data(), (int)bits.size(), bits.data(), s->nbits));
+        if (use_tc && ops.back().kind == GateOp::Dense && ops.back().t >= 3 && bits.size() <= 5) {
+            tc_of[bi] = (int)tcs.size();
+            tcs.push_back(lower_tc(m, bits, s->nbits));
         }
     }
-    // Stage every dense matrix in one pinned upload.
-    size_t dense_bytes = 0;
-    std::vector<size_t> dense_off(ops.size(), 0);
+    // Stage every dense matrix and tensor-core image in one pinned upload.
+    size_t bytes = 0;
+    std::vector<size_t> off(ops.size(), 0);
     const size_t esz = s->prec == kC128 ? 16 : 8;
-    for (size_t i = 0; i < ops.size(); ++i)
-        if (ops[i].kind == GateOp::Dense) {
-            dense_off[i] = dense_bytes;
-            dense_bytes += ops[i].dense.size() * esz;
-        }
-    if (dense_bytes) {
+    for (size_t i = 0; i < ops.size(); ++i) {
+        size_t sz = 0;
+        if (tc_of[i] >= 0) sz = tcs[tc_of[i]].image.size() * sizeof(float);
+        else if (ops[i].kind == GateOp::Dense) sz = ops[i].dense.size() * esz;
+        if (!sz) continue;
+        off[i] = bytes;
+        bytes += (sz + 255) & ~size_t(255);
+    }
+    if (bytes) {
         if (p->staged) check_cuda(cudaEventSynchronize(p->staged), "plan staging wait");
         else check_cuda(cudaEventCreateWithFlags(&p->staged, cudaEventDisableTiming), "cudaEventCreate");
-        p->hmats.ensure(dense_bytes);
-        p->dmats.ensure(dense_bytes);
+        p->hmats.ensure(bytes);
+        p->dmats.ensure(bytes);
         for (size_t i = 0; i < ops.size(); ++i) {
+            char* dst = p->hmats.as<char>() + off[i];
+            if (tc_of[i] >= 0) {
+                const auto& img = tcs[tc_of[i]].image;
+                std::memcpy(dst, img.data(), img.size() * sizeof(float));
+                continue;
+            }
             if (ops[i].kind != GateOp::Dense) continue;
-            char* dst = p->hmats.as<char>() + dense_off[i];
             for (size_t e = 0; e < ops[i].dense.size(); ++e) {
                 if (s->prec == kC128) {
                     double v[2] = {ops[i].dense[e].real(), ops[i].dense[e].imag()};
@@ -641,26 +713,46 @@ void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n)
                 }
             }
         }
-        check_cuda(cudaMemcpyAsync(p->dmats.p, p->hmats.p, dense_bytes, cudaMemcpyHostToDevice, s->stream),
+        check_cuda(cudaMemcpyAsync(p->dmats.p, p->hmats.p, bytes, cudaMemcpyHostToDevice, s->stream),
                    "upload plan matrices");
         check_cuda(cudaEventRecord(p->staged, s->stream), "cudaEventRecord");
     }
+    p->last_h2d_bytes = bytes;
     bool any = false;
     for (const auto& op : ops) any |= op.kind != GateOp::Noop;
     if (!any) return;
     s->ensure_dense();
     const uint64_t total = s->total();
     const double b2 = 2.0 * s->bsz();
+    if (!tcs.empty()) {
+        s->errbuf.ensure(sizeof(int));
+        check_cuda(cudaMemsetAsync(s->errbuf.p, 0, sizeof(int), s->stream), "clear error flag");
+    }
     for (size_t i = 0; i < ops.size(); ++i) {
         const GateOp& op = ops[i];
-        if (op.kind == GateOp::Dense) {
-            const void* dm = p->dmats.as<char>() + dense_off[i];
+        if (tc_of[i] >= 0) {
+            const TcBlock& t = tcs[tc_of[i]];
+            const void* img = p->dmats.as<char>() + off[i];
+            const uint64_t ntiles = total >> 12;
+            s->launch("fused_tc_c64", 2.0 * total * s->bsz(), [&] {
+                return launch_fused_tc(s->amps.as<float2>(), ntiles, t.tilemap, t.offs, img,
+                                       s->errbuf.as<int>(), s->sm_count(), s->stream);
+            });
+        } else if (op.kind == GateOp::Dense) {
+            const void* dm = p->dmats.as<char>() + off[i];
             s->launch(s->prec == kC128 ? "dense_c128" : "dense_c64", b2 * op.touched(total), [&] {
                 return launch_dense(s->amps.p, s->prec, total, op.map, op.offs, op.t, dm, s->stream);
             });
         } else {
             s->apply_op(op, s->amps.as<char>(), total);
         }
+    }
+    if (!tcs.empty()) {
+        int flag = 0;
+        check_cuda(cudaMemcpyAsync(&flag, s->errbuf.p, sizeof(int), cudaMemcpyDeviceToHost, s->stream),
+                   "read error flag");
+        s->sync();
+        if (flag) throw Error(Q1G_ERR_TIMEOUT, "a tensor-core block kernel gave up waiting on its MMAs");
     }
 }
 

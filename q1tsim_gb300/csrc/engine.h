@@ -85,6 +85,7 @@ struct q1g_state {
     q1g::DevBuf uscratch;   // uint64
     q1g::DevBuf matbuf;     // one dense matrix
     q1g::DevBuf colbuf;     // CollapseCol table
+    q1g::DevBuf errbuf;     // error flag of bounded device waits
     q1g::HostBuf hstage;    // pinned staging for results
     cudaStream_t stream = nullptr;
     bool own_stream = false;
@@ -102,6 +103,16 @@ struct q1g_state {
     ~q1g_state();
 
     size_t bsz() const { return q1g::amp_bytes(prec); }
+    int sms = 0;
+    int sm_count()
+    {
+        if (!sms) {
+            int dev = 0;
+            q1g::check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+            q1g::check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "sm count");
+        }
+        return sms;
+    }
     uint64_t total() const { return ncols * N; }
     char* col_ptr(uint64_t c) const { return amps.as<char>() + c * N * bsz(); }
 
@@ -148,6 +159,7 @@ struct q1g_plan {
     q1g::HostBuf hmats;            // pinned staging of dense matrices
     q1g::DevBuf dmats;
     cudaEvent_t staged = nullptr;  // last upload of hmats finished
+    size_t last_h2d_bytes = 0;     // matrices uploaded by the last run
     ~q1g_plan();
 };
 

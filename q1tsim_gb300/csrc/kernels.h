@@ -28,6 +28,21 @@ cudaError_t launch_phase(void* amps, int prec, uint64_t total, const IndexMap& m
 cudaError_t launch_dense(void* amps, int prec, uint64_t total, const IndexMap& map,
                          const DenseOffsets& offs, int tb, const void* dmat, cudaStream_t st);
 
+// ---- fused_tc.cu: 5-qubit fused blocks on the tensor cores (complex64)
+// rpos: the 7 row positions (ascending); goff[g]: offset of gate state g.
+struct TcOffsets {
+    int rpos[7];
+    int pad_;
+    uint64_t goff[32];
+};
+uint32_t fused_tc_smem_bytes();
+// d_bimage: the block's 32 KB hi/lo image of the real 64x64 embedding in the
+// kernel's swizzled layout; d_err: set to 1 if a bounded wait expired.
+cudaError_t launch_fused_tc(float2* amps, uint64_t ntiles, const IndexMap& tilemap, const TcOffsets& offs,
+                            const void* d_bimage, int* d_err, int sm_count, cudaStream_t st);
+// Host: the 32 KB image for the 32x32 complex matrix m (row-major (re, im)).
+void build_tc_image(const double* m, float* image);
+
 // ---- state_kernels.cu: construction, conversion, collapse
 cudaError_t launch_fill_basis(void* amps, int prec, uint64_t n_amps, const uint64_t* d_col_index,
                               uint64_t ncols, uint64_t col_len, cudaStream_t st);
