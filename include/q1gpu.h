@@ -160,6 +160,40 @@ int q1g_plan_block(const q1g_plan* p, size_t i, size_t* qubits, size_t* nq, size
 /* mats_flat = all gates' matrices concatenated ((re, im) doubles). */
 int q1g_plan_run(q1g_plan* p, q1g_state* s, const double* mats_flat, size_t n_doubles);
 
+/* ---- batches of independent circuits: one persistent launch, replayed from a
+ * CUDA graph.  Each circuit runs on its own complex64 state of at most two run
+ * columns.  A circuit is a program of gates, at most one mid-circuit Z
+ * measurement (measure_into, src/vectorstate.rs:237-329), gates conditioned on
+ * that measured bit (apply_conditional_gate, src/vectorstate.rs:193-227), and a
+ * final measure_all (src/vectorstate.rs:106-161).  This is what
+ * Circuit::execute (src/circuit.rs:562-762) does for each circuit, for many
+ * circuits at once.  Uniforms come from the SplitMix64 stream `seed` of each
+ * circuit, drawn in the order the single-state entry points draw them. */
+typedef struct q1g_batch q1g_batch;
+
+enum q1g_batch_op {
+    Q1G_OP_GATE = 0,        /* bits: k qubits; matrix 2^k x 2^k (k <= 4) */
+    Q1G_OP_MEASURE = 1,     /* args: (qubit, cbit) */
+    Q1G_OP_CONDITIONAL = 2, /* bits + matrix as a gate; args: (cbit, value 0/1) */
+    Q1G_OP_MEASURE_ALL = 3  /* bits: the nr_bits classical bits (cbits[q] for qubit q); must be last */
+};
+
+/* fusion_width: 1..4 qubits per fused block. */
+int q1g_batch_create(int fusion_width, q1g_batch** out);
+void q1g_batch_free(q1g_batch* b);
+/* Add one circuit.  kinds/nbits/args have nops entries (args: 2 per op);
+ * bits_flat and mats_flat concatenate the ops' bits and matrices. */
+int q1g_batch_add_circuit(q1g_batch* b, size_t nr_bits, size_t nr_shots, uint64_t seed, size_t nops,
+                          const int* kinds, const size_t* nbits, const size_t* bits_flat,
+                          const double* mats_flat, const size_t* args);
+/* Run every circuit; results = each circuit's classical words, circuits in
+ * the order added, runs in column order (the c_state of src/circuit.rs). */
+int q1g_batch_run(q1g_batch* b, uint64_t* results, size_t len);
+/* Circuits, total runs, device arena bytes, lowered ops, device time of the
+ * last run in ms.  Any pointer may be NULL. */
+int q1g_batch_info(const q1g_batch* b, size_t* ncircuits, size_t* total_runs, size_t* arena_bytes,
+                   size_t* nops, double* last_ms);
+
 /* ---- profiling: per-kernel CUDA-event timing on the state's stream */
 int q1g_profile_enable(q1g_state* s, int enable);
 /* Kernel family names and totals since the last reset.  For entry i < *n:

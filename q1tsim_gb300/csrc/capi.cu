@@ -7,6 +7,7 @@
 #include <new>
 #include <string>
 
+#include "batch.h"
 #include "engine.h"
 
 namespace q1g {
@@ -413,6 +414,62 @@ int q1g_plan_run(q1g_plan* p, q1g_state* s, const double* mats_flat, size_t n_do
         need(s, "state");
         if (n_doubles) need(mats_flat, "mats_flat");
         plan_run(p, s, mats_flat, n_doubles);
+    });
+}
+
+int q1g_batch_create(int fusion_width, q1g_batch** out)
+{
+    return guarded([&] {
+        need(out, "out");
+        if (fusion_width < 1 || fusion_width > 4)
+            throw Error(Q1G_ERR_INVALID_ARGUMENT, "batch fusion_width must be in 1..4");
+        auto* b = new q1g_batch();
+        b->width = fusion_width;
+        *out = b;
+    });
+}
+
+void q1g_batch_free(q1g_batch* b) { delete b; }
+
+int q1g_batch_add_circuit(q1g_batch* b, size_t nr_bits, size_t nr_shots, uint64_t seed, size_t nops,
+                          const int* kinds, const size_t* nbits, const size_t* bits_flat, const double* mats_flat,
+                          const size_t* args)
+{
+    return guarded([&] {
+        need(b, "batch");
+        if (nops) {
+            need(kinds, "kinds");
+            need(nbits, "nbits");
+            need(args, "args");
+        }
+        batch_add_circuit(b, nr_bits, nr_shots, seed, nops, kinds, nbits, bits_flat, mats_flat, args);
+    });
+}
+
+int q1g_batch_run(q1g_batch* b, uint64_t* results, size_t len)
+{
+    return guarded([&] {
+        need(b, "batch");
+        batch_run(b, results, len);
+    });
+}
+
+int q1g_batch_info(const q1g_batch* b, size_t* ncircuits, size_t* total_runs, size_t* arena_bytes, size_t* nops,
+                   double* last_ms)
+{
+    return guarded([&] {
+        need(b, "batch");
+        uint64_t runs = 0;
+        for (const auto& c : b->circuits) runs += c.nshots;
+        if (ncircuits) *ncircuits = b->circuits.size();
+        if (total_runs) *total_runs = runs;
+        if (arena_bytes) {
+            uint64_t amps = 0;
+            for (const auto& c : b->circuits) amps += 2 * (uint64_t(1) << c.nbits);
+            *arena_bytes = amps * sizeof(float2);
+        }
+        if (nops) *nops = b->ops.size();
+        if (last_ms) *last_ms = b->last_ms;
     });
 }
 

@@ -451,7 +451,7 @@ void q1g_state::measure_all(const size_t* cbits, size_t ncbits, uint64_t* res, s
         }
         for (uint64_t r = 0; r < nshots; ++r) res[r] = (res[r] & mask) | word_of(outc[r]);
     } else if (nshots > 0) {
-        const uint64_t chunk = std::min<uint64_t>(N, 1024);
+        const uint64_t chunk = std::min<uint64_t>(N, 256);
         const uint64_t ncc = N / chunk;  // chunks per column
         uint64_t mmax = 0;
         for (auto c : counts) mmax = std::max(mmax, c);
@@ -470,9 +470,8 @@ void q1g_state::measure_all(const size_t* cbits, size_t ncbits, uint64_t* res, s
         uint64_t* d_cpos = d_word + nshots;
         check_cuda(cudaMemcpyAsync(d_cpos, cbit_of_pos.data(), 64 * sizeof(uint64_t), cudaMemcpyHostToDevice,
                                    stream), "upload cbits");
-        IndexMap none{};
         launch("chunk_sums", double(ncols * N * bsz()), [&] {
-            return launch_chunk_sums(amps.p, prec, ncols * N, chunk, none, d_sums, stream);
+            return launch_chunk_sums_dense(amps.p, prec, ncols * N, chunk, d_sums, stream);
         });
         for (uint64_t c = 0; c < ncols; ++c)
             launch("prefix_scan", 2.0 * ncc * sizeof(double), [&] {

@@ -11,7 +11,10 @@
 // R[2g'+1][2g] = Im M, R[2g'+1][2g+1] = Re M).  It runs on tcgen05.mma
 // kind::tf32 (M=128, N=64, K=8) with the accumulator in TMEM.  FP32 accuracy
 // comes from the 3xTF32 split (Ootomo & Yokota 2022): x = hi + lo with
-// hi = tf32(x), lo = tf32(x - hi), and D = A_lo*B_hi + A_hi*B_lo + A_hi*B_hi.
+// hi = tf32(x), lo = tf32(x - hi), and D = A_hi*B_hi + (A_lo*B_hi + A_hi*B_lo).
+// The correction products go to a second TMEM accumulator with the lo halves
+// pre-scaled by 2^11 (exact), and the epilogue adds D_corr * 2^-11: summed in
+// one accumulator with the main products, the correction terms were lost.
 //
 // One CTA = 4 warps; thread t owns row t: it loads its 32 amplitudes (for a
 // fixed g the warp reads 32 consecutive row positions, so loads and stores
@@ -34,7 +37,9 @@ namespace q1g {
 namespace {
 
 constexpr int kTcThreads = 128;
-constexpr uint32_t kTmemCols = 64;
+constexpr uint32_t kTmemCols = 128;   // D_main in columns 0-63, D_corr in 64-127
+constexpr float kLoScale = 2048.0f;     // 2^11: lo halves are stored scaled up
+constexpr float kLoUnscale = 1.0f / 2048.0f;
 constexpr uint32_t kAtomA = 16384;   // 128 rows x 128 B
 constexpr uint32_t kAtomB = 8192;    // 64 rows x 128 B
 constexpr uint32_t kOffAhi = 0;
@@ -65,11 +70,11 @@ __device__ __forceinline__ uint64_t desc_sw128(uint32_t saddr)
 // Instruction descriptor, kind::tf32: D f32, A/B tf32, both K-major, N=64, M=128.
 constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
 
+// Nearest TF32 value (ties away from zero) as an FP32 with the 13 low
+// mantissa bits cleared, so that x - to_tf32(x) is the exact remainder.
 __device__ __forceinline__ float to_tf32(float x)
 {
-    uint32_t r;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-    return __uint_as_float(r);
+    return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
 }
 
 __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
@@ -176,8 +181,8 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, IndexMap tilemap, TcOffsets 
             const int g0 = 2 * c;
             const float4 v = make_float4(x[g0].x, x[g0].y, x[g0 + 1].x, x[g0 + 1].y);
             const float4 h = make_float4(to_tf32(v.x), to_tf32(v.y), to_tf32(v.z), to_tf32(v.w));
-            const float4 l = make_float4(to_tf32(v.x - h.x), to_tf32(v.y - h.y), to_tf32(v.z - h.z),
-                                         to_tf32(v.w - h.w));
+            const float4 l = make_float4(to_tf32((v.x - h.x) * kLoScale), to_tf32((v.y - h.y) * kLoScale),
+                                         to_tf32((v.z - h.z) * kLoScale), to_tf32((v.w - h.w) * kLoScale));
             const uint32_t atom = (uint32_t)(c >> 3) * kAtomA;
             const uint32_t off = atom + row_byte + ((((uint32_t)c & 7u) ^ swz) << 4);
             *(float4*)(smem + kOffAhi + off) = h;
@@ -187,16 +192,20 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, IndexMap tilemap, TcOffsets 
         __syncthreads();
         if (tid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t apass[3] = {sbase + kOffAlo, sbase + kOffAhi, sbase + kOffAhi};
-            const uint32_t bpass[3] = {sbase + kOffBhi, sbase + kOffBlo, sbase + kOffBhi};
+            // pass 0: D_main = A_hi B_hi; passes 1-2: D_corr = A_lo' B_hi + A_hi B_lo'
+            // (lo' = 2^11 lo), kept apart so the small terms never meet the large
+            // ones inside one accumulation.
+            const uint32_t apass[3] = {sbase + kOffAhi, sbase + kOffAlo, sbase + kOffAhi};
+            const uint32_t bpass[3] = {sbase + kOffBhi, sbase + kOffBhi, sbase + kOffBlo};
+            const uint32_t dcol[3] = {0u, 64u, 64u};
 #pragma unroll
             for (int pss = 0; pss < 3; ++pss)
 #pragma unroll
                 for (int ks = 0; ks < 8; ++ks) {
                     const uint32_t ka = (uint32_t)(ks >> 2) * kAtomA + (uint32_t)(ks & 3) * 32u;
                     const uint32_t kb = (uint32_t)(ks >> 2) * kAtomB + (uint32_t)(ks & 3) * 32u;
-                    mma_tf32(tmem, desc_sw128(apass[pss] + ka), desc_sw128(bpass[pss] + kb),
-                             (pss | ks) != 0 ? 1u : 0u);
+                    const uint32_t acc = (pss == 2 || ks != 0) ? 1u : 0u;
+                    mma_tf32(tmem + dcol[pss], desc_sw128(apass[pss] + ka), desc_sw128(bpass[pss] + kb), acc);
                 }
             mma_commit(bar);
         }
@@ -224,14 +233,22 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, IndexMap tilemap, TcOffsets 
         }
         phase ^= 1u;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        uint32_t d[64];
         const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
-        tmem_ld32(taddr, d);
-        tmem_ld32(taddr + 32, d + 32);
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-        for (int g = 0; g < 32; ++g)
-            a[cur | offs.goff[g]] = make_float2(__uint_as_float(d[2 * g]), __uint_as_float(d[2 * g + 1]));
+        for (int half = 0; half < 2; ++half) {
+            uint32_t dm[32], dc[32];
+            tmem_ld32(taddr + 32u * half, dm);
+            tmem_ld32(taddr + 64u + 32u * half, dc);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const int g = 16 * half + j;
+                const float re = __fmaf_rn(__uint_as_float(dc[2 * j]), kLoUnscale, __uint_as_float(dm[2 * j]));
+                const float im =
+                    __fmaf_rn(__uint_as_float(dc[2 * j + 1]), kLoUnscale, __uint_as_float(dm[2 * j + 1]));
+                a[cur | offs.goff[g]] = make_float2(re, im);
+            }
+        }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     }
     if (failed) {
@@ -276,7 +293,7 @@ void build_tc_image(const double* m, float* image)
                     const int n = 2 * gp + cp, k = 2 * g + c;
                     const float v = (float)rv[cp][c];
                     const float hi = host_tf32(v);
-                    const float lo = host_tf32(v - hi);
+                    const float lo = host_tf32((v - hi) * 2048.0f);
                     const int atom = k >> 5, kc = (k & 31) >> 2, e = k & 3;
                     const size_t off = (size_t)atom * kAtomB + (size_t)(n >> 3) * 1024 + (size_t)(n & 7) * 128 +
                                        (size_t)((kc ^ (n & 7)) << 4) + (size_t)e * 4;

@@ -67,6 +67,10 @@ cudaError_t launch_collapse_copy(void* dst, const void* src, int prec, uint64_t 
 // consecutive j; chunk must divide the virtual column length.
 cudaError_t launch_chunk_sums(const void* amps, int prec, uint64_t units, uint64_t chunk,
                               const IndexMap& map, double* out, cudaStream_t st);
+// Chunk sums for shot sampling: `chunk` = min(2^n, 256) consecutive
+// amplitudes per chunk, reduced as described in measure_kernels.cu.
+cudaError_t launch_chunk_sums_dense(const void* amps, int prec, uint64_t total, uint64_t chunk, double* out,
+                                    cudaStream_t st);
 // Deterministic per-segment reduction: out[s] = sum of in[s*len .. (s+1)*len).
 cudaError_t launch_segment_sums(const double* in, uint64_t nseg, uint64_t len, double* out,
                                 cudaStream_t st);
@@ -82,8 +86,9 @@ cudaError_t launch_exclusive_scan(double* data, uint64_t n, double* tmp, double*
 cudaError_t launch_sorted_uniforms(uint64_t seed, uint64_t counter0, uint64_t m, double* out,
                                    double* tmp, cudaStream_t st);
 // One warp per run: outcome[r] = first index i of the column with inclusive
-// prefix > u[r] * total, found through the chunk prefix (excl) and a warp
-// scan of the chunk; word[r] = classical word of the outcome.
+// prefix > u[r] * total, found through the chunk prefix (excl), a warp scan
+// of the chunk's group sums and a scan of the group; word[r] = classical
+// word of the outcome.  `chunk` must be the one used for the chunk sums.
 struct SampleArgs {
     const void* amps;       // the column
     int prec;
@@ -100,6 +105,44 @@ struct SampleArgs {
     const uint64_t* d_cbit_of_pos;  // classical bit mask for each bit position
 };
 cudaError_t launch_sample(const SampleArgs& a, cudaStream_t st);
+// ---- batch.cu: many circuits in one persistent launch (complex64)
+enum { kBatchDense = 0, kBatchMeasure = 1, kBatchSample = 2 };
+struct BatchOp {
+    int kind;
+    int t;            // dense: target qubits (1..4)
+    int cond;         // dense: -1 all columns, else only columns whose measured bit equals it
+    int pos;          // measure: bit position
+    int cbit;         // measure: classical bit
+    uint32_t mat;     // dense: first float2 of the 2^t x 2^t matrix in the pool
+    uint32_t cpos;    // sample: index of the 64-entry classical-bit table
+    int pad_;
+    uint64_t cmask;   // sample: classical bits the outcome overwrites
+    IndexMap map;     // dense: the gate positions, zeroed
+    uint64_t offs[16];
+};
+struct BatchCircuit {
+    uint64_t state_off;   // amplitude offset of column 0 (column 1 follows)
+    uint64_t res_off;     // first classical word of this circuit's runs
+    uint32_t op_begin, op_end;
+    int nbits;
+    int pad_;
+    uint64_t nshots;
+    uint64_t seed;        // SplitMix64 stream of this circuit's uniforms
+};
+struct BatchArgs {
+    float2* arena;
+    uint64_t* results;
+    const BatchCircuit* circuits;   // in queue order
+    int ncircuits;
+    const BatchOp* ops;
+    const float2* mats;
+    const uint64_t* cbit_tables;
+    double* scratch;
+    uint64_t scratch_per_cta;
+    unsigned* queue;
+};
+cudaError_t launch_batch(const BatchArgs& a, int sm_count, cudaStream_t st);
+
 // Per-block partials (6 doubles per block) comparing two states.
 cudaError_t launch_compare(const void* a, int prec_a, const void* b, int prec_b, uint64_t n,
                            double* part, unsigned blocks, cudaStream_t st);

@@ -8,6 +8,7 @@
 // results.
 #include "common.cuh"
 #include "kernels.h"
+#include "sampling.cuh"
 
 namespace q1g {
 
@@ -18,13 +19,6 @@ __device__ __forceinline__ double norm_sqr(T v)
 {
     const double x = (double)v.x, y = (double)v.y;
     return x * x + y * y;
-}
-
-__device__ __forceinline__ double warp_sum(double v)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
 }
 
 // Sum of v over the block (blockDim.x a multiple of 32, <= 1024); result in
@@ -147,19 +141,6 @@ k_scan_tiles(double* data, uint64_t n, const double* offsets)
 
 // ------------------------------------------------- sorted uniforms
 
-__device__ __forceinline__ uint64_t splitmix_mix(uint64_t z)
-{
-    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
-    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
-    return z ^ (z >> 31);
-}
-
-__device__ __forceinline__ double stream_uniform(uint64_t seed, uint64_t counter)
-{
-    const uint64_t z = seed + (counter + 1) * 0x9E3779B97F4A7C15ULL;
-    return (double)(splitmix_mix(z) >> 11) * (1.0 / 9007199254740992.0);
-}
-
 __global__ void k_exp_spacings(uint64_t seed, uint64_t counter0, uint64_t n, double* e, double* copy)
 {
     const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
@@ -180,58 +161,41 @@ __global__ void k_normalise_spacings(const double* excl, const double* e, const 
 }
 
 // ----------------------------------------------------------- sampling
+//
+// Outcome probabilities are summed hierarchically, with the same arithmetic
+// in the reduction and in the search so the two agree: p_i = |a_i|^2 in the
+// state's precision, groups of 8 consecutive p_i summed sequentially in that
+// precision, chunks of 32 groups (256 amplitudes) summed in FP64, and the
+// FP64 exclusive prefix over chunks.  A shot finds its chunk by binary search
+// on that prefix, its group by an FP64 warp scan of the chunk's 32 group
+// sums, and its amplitude by a sequential scan of the group.
+
+// One warp per chunk of `chunk` (<= 256) amplitudes.
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_chunk_sums_dense(const T* __restrict__ a, uint64_t nchunks, uint64_t chunk, double* out)
+{
+    using R = typename ProbT<T>::R;
+    const int lane = threadIdx.x & 31;
+    const uint64_t warps = (uint64_t(gridDim.x) * blockDim.x) >> 5;
+    for (uint64_t c = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; c < nchunks; c += warps) {
+        R p[8];
+        group_probs(a, c * chunk, chunk, lane, p);
+        const double s = warp_sum((double)group_sum(p));
+        if (lane == 0) out[c] = s;
+    }
+}
 
 template <typename T>
 __global__ void __launch_bounds__(256)
 k_sample(SampleArgs s)
 {
     const uint64_t r = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
     if (r >= s.nruns) return;
-    const T* a = (const T*)s.amps;
-    const double total = *s.total;
-    double target = s.u[r] * total;
-    // u < 1, but keep the target strictly inside the mass if rounding pushed
-    // it onto the total: the sample then lands on the last nonzero amplitude.
-    if (!(target < total)) target = nextafter(total, 0.0);
-    // largest chunk c with excl[c] <= target
-    uint64_t lo = 0, hi = s.nchunks - 1;
-    while (lo < hi) {
-        const uint64_t mid = (lo + hi + 1) >> 1;
-        if (s.excl[mid] <= target) lo = mid; else hi = mid - 1;
-    }
-    const uint64_t c = lo;
-    const double tl = target - s.excl[c];
-    const uint64_t i0 = c * s.chunk;
-    double base = 0.0;
-    int64_t found = -1, last_nz = -1;
-    for (uint64_t st = 0; st < s.chunk; st += 32) {
-        const uint64_t i = st + lane;
-        const double w = i < s.chunk ? norm_sqr(a[i0 + i]) : 0.0;
-        double incl = w;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const double y = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += y;
-        }
-        incl += base;
-        const unsigned hit = __ballot_sync(0xffffffffu, w > 0.0 && incl > tl);
-        const unsigned nz = __ballot_sync(0xffffffffu, w > 0.0);
-        if (nz) last_nz = (int64_t)(st + 31 - __clz(nz));
-        if (hit) {
-            found = (int64_t)(st + __ffs(hit) - 1);
-            break;
-        }
-        base = __shfl_sync(0xffffffffu, incl, 31);
-    }
-    if (found < 0) found = last_nz >= 0 ? last_nz : 0;
-    if (lane == 0) {
-        const uint64_t idx = i0 + (uint64_t)found;
-        uint64_t word = 0;
-        for (int p = 0; p < s.nbits; ++p)
-            if ((idx >> p) & 1) word |= s.d_cbit_of_pos[p];
+    uint64_t idx;
+    if (sample_one((const T*)s.amps, s.chunk, s.excl, s.nchunks, *s.total, s.u[r], threadIdx.x & 31, &idx)) {
         s.outcome[r] = idx;
-        s.word[r] = word;
+        s.word[r] = outcome_word(idx, s.nbits, s.d_cbit_of_pos);
     }
 }
 
@@ -288,6 +252,18 @@ cudaError_t launch_chunk_sums(const void* amps, int prec, uint64_t units, uint64
         k_chunk_sums<double2><<<grid, 256, 0, st>>>((const double2*)amps, units, chunk, map, out);
     else
         k_chunk_sums<float2><<<grid, 256, 0, st>>>((const float2*)amps, units, chunk, map, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_chunk_sums_dense(const void* amps, int prec, uint64_t total, uint64_t chunk, double* out,
+                                    cudaStream_t st)
+{
+    const uint64_t nchunks = total / chunk;
+    const unsigned grid = cap_grid((nchunks * 32 + 255) / 256);
+    if (prec == kC128)
+        k_chunk_sums_dense<double2><<<grid, 256, 0, st>>>((const double2*)amps, nchunks, chunk, out);
+    else
+        k_chunk_sums_dense<float2><<<grid, 256, 0, st>>>((const float2*)amps, nchunks, chunk, out);
     return cudaGetLastError();
 }
 

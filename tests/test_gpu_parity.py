@@ -276,7 +276,30 @@ def test_fused_plans_match_plain(width):
         g.apply_plan(p, mats)
         out = g.states()[:, 0]
         assert np.max(np.abs(out - ref)) <= tol, (prec, np.max(np.abs(out - ref)))
-        assert 1 - abs(np.vdot(ref, out)) ** 2 <= 1e-6
+        # fidelity of the normalised states; the tensor cores' FP32
+        # accumulation rounds toward zero, so the norm itself may drift by a
+        # few 1e-8 per block (sampling divides by the total)
+        nrm = np.linalg.norm(out)
+        assert abs(nrm - 1.0) <= 1e-5, nrm
+        assert 1 - abs(np.vdot(ref, out)) ** 2 / nrm ** 2 <= 1e-9
+
+
+def test_tensor_core_block_is_exact_on_split_values():
+    """A 3-qubit cyclic permutation (entries 0/1) on amplitudes with 20
+    fraction bits goes through the tensor-core block kernel; hi + lo recovers
+    every amplitude, so the result is exact, not TF32-rounded."""
+    n = 12
+    k = np.arange(1 << n) % 4096
+    amps = ((1.0 + k * 2.0 ** -20) / 64.0).astype(np.complex128)
+    P = np.zeros((8, 8), dtype=np.complex128)
+    for s in range(8):
+        P[(s + 1) % 8, s] = 1.0
+    g = VectorState.from_amplitudes(amps, 1, "c64")
+    g.apply_plan(Plan(n, [[0, 1, 2]], 3), P.ravel().view(np.float64))
+    o = orc.OracleState.from_amplitudes(amps, 1)
+    o.apply_gate(P, [0, 1, 2])
+    out, ref = g.states()[:, 0], o.states()[:, 0]
+    assert np.array_equal(out, ref), float(np.max(np.abs(out - ref)))
 
 
 def test_plan_rerun_with_new_parameters():
