@@ -203,6 +203,30 @@ int q1g_profile_report(q1g_state* s, char* names, uint64_t* launches, double* ms
                        double* bytes, size_t* n);
 int q1g_profile_reset(q1g_state* s);
 
+/* ---- shot sampling that allocates nothing.  No counterpart in the
+ * reference: it exists for callers that cannot call cudaMalloc, such as a
+ * framework whose pool allocator owns all device memory, or a
+ * latency-critical loop that must not stall on an allocation.
+ *
+ * Samples nshots outcomes from one column of 2^nr_bits amplitudes (precision
+ * Q1G_C128 or Q1G_C64) in device memory, using the ascending uniforms in
+ * [0, 1) at d_sorted_uniforms (device).  It writes d_outcomes[r] (the basis
+ * index) and d_words[r] (the classical word: qubit q's bit at cbits[q];
+ * cbits NULL means cbits[q] = q, as VectorState::measure_all).  The kernels and
+ * results are those of q1g_peek_all_into for the same column and uniforms.
+ *
+ * Scratch: a fixed device array inside the library, about 0.5 MB, holding up
+ * to nr_bits = 24 (larger states are rejected with Q1G_ERR_INVALID_ARGUMENT).
+ * Every GPU that loads the library keeps it until the process exits.  The
+ * first call on a device looks up the array's address (cudaGetSymbolAddress);
+ * make that first call before any stream capture.  All calls share the one
+ * array, so calls that overlap on the GPU race; serialise them (one stream).
+ * The call is asynchronous on cuda_stream (NULL: the legacy default stream)
+ * and allocates no device or host memory of its own. */
+int q1g_sample_shots_noalloc(const void* d_amps, int precision, size_t nr_bits,
+                             const double* d_sorted_uniforms, size_t nshots, uint64_t* d_outcomes,
+                             uint64_t* d_words, const size_t* cbits, void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

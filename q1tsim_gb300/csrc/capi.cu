@@ -473,6 +473,16 @@ int q1g_batch_info(const q1g_batch* b, size_t* ncircuits, size_t* total_runs, si
     });
 }
 
+int q1g_sample_shots_noalloc(const void* d_amps, int precision, size_t nr_bits, const double* d_sorted_uniforms,
+                             size_t nshots, uint64_t* d_outcomes, uint64_t* d_words, const size_t* cbits,
+                             void* cuda_stream)
+{
+    return guarded([&] {
+        sample_shots_noalloc(d_amps, precision, nr_bits, d_sorted_uniforms, nshots, d_outcomes, d_words, cbits,
+                             (cudaStream_t)cuda_stream);
+    });
+}
+
 int q1g_profile_enable(q1g_state* s, int enable)
 {
     return guarded([&] {

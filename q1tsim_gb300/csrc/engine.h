@@ -165,4 +165,8 @@ struct q1g_plan {
 
 namespace q1g {
 void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n);
+// noalloc.cu: the sampler whose scratch is a fixed device array.
+void sample_shots_noalloc(const void* d_amps, int precision, size_t nr_bits, const double* d_sorted_uniforms,
+                          size_t nshots, uint64_t* d_outcomes, uint64_t* d_words, const size_t* cbits,
+                          cudaStream_t st);
 }
