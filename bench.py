@@ -45,6 +45,18 @@ def brick_gates(n, depth, seed):
     return out
 
 
+def world_aggregate(local_ms, local_units, dist, device):
+    """(max over ranks of the elapsed ms, sum over ranks of the units done).
+    Replicas do not exchange data; only these two numbers are reduced."""
+    import torch
+    ms = torch.tensor([float(local_ms)], dtype=torch.float64, device=device)
+    units = torch.tensor([float(local_units)], dtype=torch.float64, device=device)
+    if dist is not None:
+        dist.all_reduce(ms, op=dist.ReduceOp.MAX)
+        dist.all_reduce(units, op=dist.ReduceOp.SUM)
+    return float(ms[0]), float(units[0])
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -129,6 +141,128 @@ def cpu_baseline(n_sample, depth_sample, seed, n_full):
                       f"at {n_sample} qubits in {dt:.2f} s ({rate:.2f} gates/s), scaled by 2^({n_sample}-{n_full})"}
 
 
+def qft_leg(args):
+    """configs[1]: QFT on a random normalised 28-qubit state (re, im i.i.d.
+    N(0,1) from the seed), complex64 fused against complex128 plain."""
+    import torch
+    from q1tsim_gb300 import Plan, VectorState, workloads
+    n = args.qft_qubits
+    rng = np.random.default_rng(args.seed + 5)
+    amps = rng.standard_normal(1 << n) + 1j * rng.standard_normal(1 << n)
+    amps /= np.linalg.norm(amps)
+    qc = workloads.qft(n, measure=False)
+    bits = [op[2] for op in qc.ops]
+    mats = np.concatenate([np.ascontiguousarray(op[1].matrix()).ravel() for op in qc.ops]).view(np.float64)
+    out = {"workload": f"QFT ({len(bits)} gates: H, CU1(pi/2^k), Swap) on a random N(0,1) {n}-qubit state",
+           "gates": len(bits)}
+    for prec, width in (("c128", 0), ("c64", args.fusion)):
+        st = VectorState.from_amplitudes(amps, 1, prec)
+        plan = Plan(n, bits, width)
+        st.apply_plan(plan, mats)      # warm-up
+        st2 = VectorState.from_amplitudes(amps, 1, prec)
+        st2.synchronize()
+        t0 = time.perf_counter()
+        st2.apply_plan(plan, mats)
+        st2.synchronize()
+        dt = time.perf_counter() - t0
+        out[prec] = {"ms": dt * 1e3, "passes": plan.nblocks, "gates_per_s": len(bits) / dt}
+        out["_" + prec] = st2
+        del st
+    acc = out.pop("_c128").compare(out.pop("_c64"))
+    out["accuracy_c64_vs_c128"] = acc
+    del amps
+    torch.cuda.empty_cache()
+    return out
+
+
+def cfg0_leg(args):
+    """configs[0]: 16-qubit U3/CX brick, 20 layers, measure_all over 8192
+    runs, histogram -- on the GPU (complex128 plain and complex64 fused) and
+    in full on the CPU oracle."""
+    from oracle import oracle as orc
+    from q1tsim_gb300 import Rng, workloads
+    res = {"workload": "16-qubit U3/CX brick, 20 layers (470 gates), measure_all over 8192 runs, histogram"}
+    for prec, width in (("c128", 0), ("c64", args.fusion)):
+        c = workloads.brick(16, 20, args.seed + 3, precision=prec, fusion_width=width)
+        c.execute(8192, Rng(1))
+        t0 = time.perf_counter()
+        for k in range(5):
+            c.execute(8192, Rng(k))
+            h = c.histogram()
+        res[prec] = {"ms": (time.perf_counter() - t0) / 5 * 1e3, "distinct_outcomes": len(h)}
+    c = workloads.brick(16, 20, args.seed + 3, precision="c128", fusion_width=0)
+    t0 = time.perf_counter()
+    c.execute_with(8192, Rng(1), orc.OracleState.new(16, 8192))
+    c.histogram()
+    cpu_ms = (time.perf_counter() - t0) * 1e3
+    res["cpu_baseline"] = {"ms": cpu_ms, "cores": 1, "kind": "port",
+                           "sample": "the full workload on the oracle (reference algorithm, 1 thread)"}
+    res["speedup_c128_vs_cpu"] = cpu_ms / res["c128"]["ms"]
+    return res
+
+
+def batch_leg(args):
+    """configs[3]: independent circuits (8-20 qubits, depth 10-40, U3/CX/CZ,
+    one mid-circuit measurement + conditional X, 1024 runs each) in one
+    persistent launch replayed from a CUDA graph."""
+    from q1tsim_gb300 import workloads
+    from q1tsim_gb300.batch import Batch
+    t0 = time.perf_counter()
+    circuits = workloads.batch_workload(args.batch_circuits, args.seed + 11)
+    b = Batch(4)
+    for i, c in enumerate(circuits):
+        b.add(c, 1024, args.seed + i)
+    setup_s = time.perf_counter() - t0
+    b.run()   # builds the device program and the graph
+    dev_ms, wall_ms = [], []
+    for _ in range(max(args.steps, 3)):
+        w0 = time.perf_counter()
+        b.run()
+        wall_ms.append((time.perf_counter() - w0) * 1e3)
+        dev_ms.append(b.info()["last_ms"])
+    ngates = sum(1 for c in circuits for op in c.ops if op[0] in ("gate", "cgate"))
+    ms = statistics.median(dev_ms)
+    info = b.info()
+    # CPU: the oracle runs the first circuits one by one
+    from oracle import oracle as orc
+    from q1tsim_gb300.vectorstate import Rng
+    sample = circuits[:12]
+    c0 = time.perf_counter()
+    for i, c in enumerate(sample):
+        c.execute_with(1024, Rng(args.seed + i), orc.OracleState.new(c.nr_qbits, 1024))
+    cpu_s = time.perf_counter() - c0
+    work = lambda cs: sum((2 ** c.nr_qbits) * sum(1 for op in c.ops if op[0] in ("gate", "cgate")) for c in cs)
+    cpu_total_s = cpu_s * work(circuits) / work(sample)
+    return {"workload": f"{len(circuits)} circuits, 8-20 qubits, depth 10-40 U3/CX/CZ, mid-circuit measure + "
+                        "conditional X, 1024 runs each, complex64, fusion k<=4",
+            "circuits": len(circuits), "gates": ngates, "device_ms": ms, "e2e_ms": statistics.median(wall_ms),
+            "circuits_per_s": len(circuits) / (ms / 1e3), "gates_per_s": ngates / (ms / 1e3),
+            "e2e_circuits_per_s": len(circuits) / (statistics.median(wall_ms) / 1e3),
+            "arena_gib": info["arena_bytes"] / 2 ** 30, "lowered_ops": info["ops"],
+            "launches_per_run": 1, "setup_s": setup_s,
+            "cpu_baseline": {"value": len(circuits) / cpu_total_s, "unit": "circuits/s", "cores": 1, "kind": "port",
+                             "sample": f"oracle on the first {len(sample)} circuits in {cpu_s:.2f} s, scaled to "
+                                       "the batch by sum(gates x 2^n)"}}
+
+
+def serving_leg(args):
+    """configs[4]: a Poisson stream (mean 2000 circuits/s) of GHZ, QFT and
+    brick circuits, 10-26 qubits, depth 5-50, 4096 shots, complex64 fused,
+    admitted by HBM budget into concurrent slots."""
+    from q1tsim_gb300.serving import latency_stats, mixed_requests, serve
+    reqs = mixed_requests(args.serve_requests, args.seed + 23)
+    done, wall, srv = serve(reqs, rate_hz=2000.0, hbm_budget_bytes=64 << 30, slots=8, seed=args.seed)
+    st = latency_stats(done)
+    first = min(r.arrival for r in done)
+    last = max(r.done for r in done)
+    st.update({"requests": len(reqs), "offered_rate_hz": 2000.0,
+               "circuits_per_s": len(done) / (last - first), "peak_inflight": srv.peak_inflight,
+               "peak_budget_gib": srv.peak_used / 2 ** 30, "slots": 8, "hbm_budget_gib": 64,
+               "workload": "Poisson 2000/s mix of GHZ, QFT (on a random product state) and U3/CX brick "
+                           "circuits, 10-26 qubits, depth 5-50, 4096 shots, complex64 fused"})
+    return st
+
+
 def run_reference(args, rank, world):
     """Reference arm: the reference's CPU algorithm (the oracle port: the Rust
     reference cannot be built on this image) on the host cores."""
@@ -179,6 +313,13 @@ def main():
     ap.add_argument("--no-plain", action="store_true", help="skip the complex128 comparison run")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--cpu-qubits", type=int, default=22)
+    ap.add_argument("--batch-circuits", type=int, default=4096)
+    ap.add_argument("--serve-requests", type=int, default=1000)
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-circuits leg")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving leg")
+    ap.add_argument("--no-qft", action="store_true", help="skip the 28-qubit QFT accuracy leg")
+    ap.add_argument("--no-cfg0", action="store_true", help="skip the 16-qubit CPU-runnable leg")
+    ap.add_argument("--qft-qubits", type=int, default=28)
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -252,12 +393,10 @@ def main():
     shot_wall = time.perf_counter() - t_host
     shot_ms = s0.elapsed_time(s1)
 
-    t = torch.tensor([gate_ms, shot_wall * 1e3], dtype=torch.float64, device="cuda")
-    if dist is not None:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    gate_ms_max, shot_ms_max = float(t[0]), float(t[1])
-    value = world * args.steps * ngates / (gate_ms_max / 1e3)
-    shots_per_s = world * args.steps * shots / (shot_ms_max / 1e3)
+    gate_ms_max, gates_all = world_aggregate(gate_ms, args.steps * ngates, dist, "cuda")
+    shot_ms_max, shots_all = world_aggregate(shot_wall * 1e3, args.steps * shots, dist, "cuda")
+    value = gates_all / (gate_ms_max / 1e3)
+    shots_per_s = shots_all / (shot_ms_max / 1e3)
 
     # ---- per-kernel profile of one step (CUDA events around every launch)
     fused.profile(True)
@@ -313,16 +452,19 @@ def main():
         _ = circ.cstate()
     barrier()
     e2e_s = time.perf_counter() - t0
-    et = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-    if dist is not None:
-        dist.all_reduce(et, op=dist.ReduceOp.MAX)
-    e2e_value = world * args.steps * ngates / float(et[0])
+    e2e_ms_max, e2e_gates = world_aggregate(e2e_s * 1e3, args.steps * ngates, dist, "cuda")
+    e2e_value = e2e_gates / (e2e_ms_max / 1e3)
     h2d = plan.nblocks * 32 * 32 * 8 + n * 8
     d2h = 2 * 8 * shots
 
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(args.cpu_qubits, 2, args.seed, n)
+    del circ
+    batched = None if args.no_batch else batch_leg(args)
+    serving = None if args.no_serve else serving_leg(args)
+    qft = None if args.no_qft else qft_leg(args)
+    cfg0 = None if args.no_cfg0 else cfg0_leg(args)
 
     if rank == 0:
         line = {
@@ -345,6 +487,10 @@ def main():
             "e2e": {"value": e2e_value, "unit": "gates/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "clocks": clk.summary(),
             "cpu_baseline": cpu,
+            "batched": batched,
+            "serving": serving,
+            "qft_random_state": qft,
+            "cpu_runnable_16q": cfg0,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:

@@ -159,6 +159,9 @@ int q1g_plan_block(const q1g_plan* p, size_t i, size_t* qubits, size_t* nq, size
                    size_t* ng);
 /* mats_flat = all gates' matrices concatenated ((re, im) doubles). */
 int q1g_plan_run(q1g_plan* p, q1g_state* s, const double* mats_flat, size_t n_doubles);
+/* Kernel for dense complex64 blocks of >= 3 qubits on states of >= 12 qubits:
+ * 1 (default) = tcgen05 tensor cores (3xTF32), 0 = CUDA cores (FP32). */
+int q1g_plan_set_tensor_cores(q1g_plan* p, int enable);
 
 /* ---- batches of independent circuits: one persistent launch, replayed from a
  * CUDA graph.  Each circuit runs on its own complex64 state of at most two run

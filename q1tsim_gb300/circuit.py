@@ -23,15 +23,20 @@ BASES = ("x", "y", "z")
 
 class Circuit:
     def __init__(self, nr_qbits, nr_cbits=0, precision="c128", fusion_width=0):
+        """fusion_width: qubits per fused block (0 = one pass per gate, the
+        plain drop-in mode) or "auto" to let the autotuner choose the width
+        and the dense-block kernel on the first execution."""
         self.nr_qbits = int(nr_qbits)
         self.nr_cbits = int(nr_cbits)
         self.precision = precision
-        self.fusion_width = int(fusion_width)
+        self.fusion_width = fusion_width if fusion_width == "auto" else int(fusion_width)
         self.ops = []
         self.q_state = None
         self.c_state = None
         self.rng = None
         self._plans = {}
+        self._frozen = None
+        self._segs = None
 
     # ------------------------------------------------------------ building
     def _check_qbits(self, qbits):
@@ -47,6 +52,26 @@ class Circuit:
     def _push(self, op):
         self.ops.append(op)
         self._plans.clear()
+        self._frozen = None
+        self._segs = None
+
+    def freeze(self):
+        """Evaluate every gate matrix now and reuse them on later executions
+        (a request handed to a server arrives with its matrices evaluated).
+        Parameters changed afterwards take effect only after unfreeze()."""
+        self._frozen = {}
+        for idx, op in enumerate(self._segments()):
+            if op[0] == "seq":
+                self._frozen[idx] = self._flat(op[1])
+        return self
+
+    def unfreeze(self):
+        self._frozen = None
+
+    @staticmethod
+    def _flat(seq):
+        mats = [np.ascontiguousarray(op[1].matrix(), dtype=np.complex128).ravel() for op in seq]
+        return np.concatenate(mats).view(np.float64) if mats else np.zeros(0)
 
     @staticmethod
     def _gate(gate, params):
@@ -193,6 +218,8 @@ class Circuit:
 
     def _segments(self):
         """Op list with runs of consecutive gates grouped: ("seq", [ops])."""
+        if self._segs is not None:
+            return self._segs
         out = []
         for op in self.ops:
             if op[0] == "gate":
@@ -202,18 +229,21 @@ class Circuit:
                     out.append(("seq", [op]))
             else:
                 out.append(op)
+        self._segs = out
         return out
 
     def _run_seq(self, q_state, idx, seq):
         if hasattr(q_state, "apply_plan"):
-            width = self.fusion_width
-            key = (idx, width)
-            plan = self._plans.get(key)
+            flat = self._frozen[idx] if self._frozen is not None else self._flat(seq)
+            plan = self._plans.get(idx)
             if plan is None:
-                plan = Plan(self.nr_qbits, [op[2] for op in seq], width)
-                self._plans[key] = plan
-            mats = [np.ascontiguousarray(op[1].matrix(), dtype=np.complex128).ravel() for op in seq]
-            flat = np.concatenate(mats).view(np.float64) if mats else np.zeros(0)
+                bits = [op[2] for op in seq]
+                width, tc = self.fusion_width, True
+                if width == "auto":
+                    from . import autotune
+                    width, tc = autotune.tune(self.nr_qbits, q_state.precision, bits, flat)
+                plan = Plan(self.nr_qbits, bits, width, tensor_cores=tc)
+                self._plans[idx] = plan
             q_state.apply_plan(plan, flat)
         else:
             for op in seq:

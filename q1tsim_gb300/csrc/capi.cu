@@ -143,6 +143,9 @@ int q1g_state_from_amplitudes(const double* amps, size_t nr_bits, size_t nr_shot
             if (s->spare.bytes > (size_t(1) << 30)) s->spare.release();
             s->sparse = false;
             s->basis.clear();
+            double nrm = 0.0;
+            for (uint64_t i = 0; i < 2 * s->N; ++i) nrm += amps[i] * amps[i];
+            s->norms.assign(1, nrm);
         } catch (...) {
             delete s;
             throw;
@@ -223,17 +226,27 @@ int q1g_state_compare(q1g_state* a, q1g_state* b, double* out5)
         const unsigned blocks = (unsigned)std::min<uint64_t>(want ? want : 1, 152 * 16);
         DevBuf part;
         part.ensure(6 * blocks * sizeof(double));
-        check_cuda(launch_compare(a->amps.p, a->prec, b->amps.p, b->prec, n, part.as<double>(), blocks, a->stream),
-                   "compare");
         std::vector<double> h(6 * blocks);
-        check_cuda(cudaMemcpyAsync(h.data(), part.p, h.size() * sizeof(double), cudaMemcpyDeviceToHost, a->stream),
-                   "download compare");
-        a->sync();
-        double s[5] = {0, 0, 0, 0, 0}, mx = 0.0;
-        for (unsigned i = 0; i < blocks; ++i) {
-            for (int k = 0; k < 5; ++k) s[k] += h[6 * i + k];
-            mx = std::max(mx, h[6 * i + 5]);
-        }
+        auto pass = [&](double wa, double wb, double* sums, double* mx) {
+            check_cuda(launch_compare(a->amps.p, a->prec, b->amps.p, b->prec, n, wa, wb, part.as<double>(), blocks,
+                                      a->stream),
+                       "compare");
+            check_cuda(cudaMemcpyAsync(h.data(), part.p, h.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                       a->stream),
+                       "download compare");
+            a->sync();
+            for (int k = 0; k < 5; ++k) sums[k] = 0.0;
+            *mx = 0.0;
+            for (unsigned i = 0; i < blocks; ++i) {
+                for (int k = 0; k < 5; ++k) sums[k] += h[6 * i + k];
+                *mx = std::max(*mx, h[6 * i + 5]);
+            }
+        };
+        double s[5], mx = 0.0, s2[5], mx2 = 0.0;
+        pass(1.0, 1.0, s, &mx);
+        // second pass: total variation between the normalised distributions
+        pass(1.0 / s[0], 1.0 / s[1], s2, &mx2);
+        s[4] = s2[4];
         out5[0] = mx;
         out5[1] = 1.0 - (s[2] * s[2] + s[3] * s[3]) / (s[0] * s[1]);
         out5[2] = 0.5 * s[4];
@@ -404,6 +417,14 @@ int q1g_plan_block(const q1g_plan* p, size_t i, size_t* qubits, size_t* nq, size
         for (size_t j = 0; j < b.gates.size(); ++j) gates[j] = (size_t)b.gates[j];
         *nq = b.qubits.size();
         *ng = b.gates.size();
+    });
+}
+
+int q1g_plan_set_tensor_cores(q1g_plan* p, int enable)
+{
+    return guarded([&] {
+        need(p, "plan");
+        p->tensor_cores = enable != 0;
     });
 }
 

@@ -301,6 +301,11 @@ void q1g_state::apply_conditional(const uint8_t* control, size_t ncontrol, const
         if (spare.bytes > (size_t(1) << 30)) spare.release();
         ncols = nr;
     }
+    if (!same_layout) {
+        std::vector<double> nn(ranges.size());
+        for (size_t j = 0; j < ranges.size(); ++j) nn[j] = norms[ranges[j].col];
+        norms.swap(nn);
+    }
     counts.resize(ranges.size());
     for (size_t j = 0; j < ranges.size(); ++j) counts[j] = ranges[j].len;
     for (size_t j = 0; j < ranges.size(); ++j)
@@ -390,6 +395,7 @@ void q1g_state::measure(size_t qbit, size_t cbit, uint64_t* res, size_t res_len,
         counts = nc;
         return;
     }
+    norms.assign(new_nr, 1.0);
     const int pos = nbits - 1 - (int)qbit;
     const bool split = new_nr != ncols;
     colbuf.ensure(new_nr * sizeof(CollapseCol));
@@ -544,6 +550,7 @@ void q1g_state::measure_all(const size_t* cbits, size_t ncbits, uint64_t* res, s
     basis = nb;
     counts = nc;
     ncols = nb.size();
+    norms.assign(ncols, 1.0);
 }
 
 void q1g_state::reset_all()
@@ -552,6 +559,7 @@ void q1g_state::reset_all()
     basis.assign(1, 0);
     counts.assign(1, nshots);
     ncols = 1;
+    norms.assign(1, 1.0);
 }
 
 void q1g_state::download(double* out, size_t len)
@@ -614,29 +622,48 @@ static TcBlock lower_tc(const std::vector<cd>& mat, const std::vector<int>& bits
     build_tc_image(md.data(), t.image.data());
     std::vector<int> gpos(5);
     for (int j = 0; j < 5; ++j) gpos[j] = nbits - 1 - q[j];
-    for (int g = 0; g < 32; ++g) {
-        uint64_t o = 0;
-        for (int j = 0; j < 5; ++j)
-            if ((g >> (4 - j)) & 1) o |= uint64_t(1) << gpos[j];
-        t.offs.goff[g] = o;
-    }
     std::vector<int> rows;
     for (int p = 0; (int)rows.size() < 7; ++p)
         if (std::find(gpos.begin(), gpos.end(), p) == gpos.end()) rows.push_back(p);
-    for (int r = 0; r < 7; ++r) t.offs.rpos[r] = rows[r];
     std::vector<int> z = gpos;
     z.insert(z.end(), rows.begin(), rows.end());
     std::sort(z.begin(), z.end());
     t.tilemap.nz = 12;
     for (int j = 0; j < 12; ++j) t.tilemap.zpos[j] = z[j];
     t.tilemap.setmask = 0;
+    // tile coordinate bit b <-> position z[b]
+    for (int b = 0; b < 12; ++b) {
+        t.offs.tpos[b] = (uint8_t)z[b];
+        t.offs.rowmask[b] = 0;
+        t.offs.gatemask[b] = 0;
+        for (int r = 0; r < 7; ++r)
+            if (rows[r] == z[b]) {
+                t.offs.rowmask[b] = 1u << r;
+                t.offs.row_tbit[r] = 1u << b;
+            }
+        for (int j = 0; j < 5; ++j)
+            if (gpos[j] == z[b]) t.offs.gatemask[b] = 1u << (4 - j);
+    }
+    for (int g = 0; g < 32; ++g) {
+        uint32_t jc = 0;
+        for (int b = 0; b < 12; ++b)
+            if (t.offs.gatemask[b] && (g & t.offs.gatemask[b])) jc |= 1u << b;
+        t.offs.jgate[g] = jc;
+    }
+    for (int k = 0; k < 16; ++k) {
+        uint64_t o = 0;
+        uint32_t rr = 0, gg = 0;
+        for (int b = 8; b < 12; ++b)
+            if ((k >> (b - 8)) & 1) {
+                o |= uint64_t(1) << z[b];
+                rr |= t.offs.rowmask[b];
+                gg |= t.offs.gatemask[b];
+            }
+        t.offs.koff[k] = o;
+        t.offs.krow[k] = rr;
+        t.offs.kgate[k] = gg;
+    }
     return t;
-}
-
-static bool tc_enabled()
-{
-    const char* e = std::getenv("Q1G_FUSED_KERNEL");
-    return !(e && std::string(e) == "simt");
 }
 
 void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n)
@@ -655,7 +682,7 @@ void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n)
         const double* m = mats + p->mat_off[g];
         for (size_t e = 0; e < dim * dim; ++e) gates[g].mat[e] = cd(m[2 * e], m[2 * e + 1]);
     }
-    const bool use_tc = s->prec == kC64 && s->nbits >= 12 && tc_enabled();
+    const bool use_tc = s->prec == kC64 && s->nbits >= 12 && p->tensor_cores;
     std::vector<GateOp> ops;
     std::vector<TcBlock> tcs;
     std::vector<int> tc_of(p->blocks.size(), -1);
@@ -747,11 +774,42 @@ void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n)
         }
     }
     if (!tcs.empty()) {
-        int flag = 0;
-        check_cuda(cudaMemcpyAsync(&flag, s->errbuf.p, sizeof(int), cudaMemcpyDeviceToHost, s->stream),
+        // per-column squared norms after the plan, then rescale each column to
+        // the norm it had before (the plan is unitary)
+        const uint64_t chunk = std::min<uint64_t>(s->N, 256);
+        const uint64_t nch = s->N / chunk;
+        s->dscratch.ensure((s->ncols * nch + 2 * s->ncols) * sizeof(double));
+        double* d_sums = s->dscratch.as<double>();
+        double* d_norm = d_sums + s->ncols * nch;
+        s->launch("norm_check", double(total * s->bsz()), [&] {
+            return launch_chunk_sums_dense(s->amps.p, s->prec, total, chunk, d_sums, s->stream);
+        });
+        check_cuda(launch_segment_sums(d_sums, s->ncols, nch, d_norm, s->stream), "segment_sums");
+        s->hstage.ensure(s->ncols * sizeof(double) + sizeof(int));
+        double* h_norm = s->hstage.as<double>();
+        int* h_flag = reinterpret_cast<int*>(h_norm + s->ncols);
+        check_cuda(cudaMemcpyAsync(h_norm, d_norm, s->ncols * sizeof(double), cudaMemcpyDeviceToHost, s->stream),
+                   "read norms");
+        check_cuda(cudaMemcpyAsync(h_flag, s->errbuf.p, sizeof(int), cudaMemcpyDeviceToHost, s->stream),
                    "read error flag");
         s->sync();
-        if (flag) throw Error(Q1G_ERR_TIMEOUT, "a tensor-core block kernel gave up waiting on its MMAs");
+        if (*h_flag) throw Error(Q1G_ERR_TIMEOUT, "a tensor-core block kernel gave up waiting on its MMAs");
+        std::vector<double> scale(s->ncols, 1.0);
+        bool any_scale = false;
+        for (uint64_t c = 0; c < s->ncols; ++c) {
+            if (h_norm[c] > 0.0) scale[c] = std::sqrt(s->norms[c] / h_norm[c]);
+            any_scale |= scale[c] != 1.0;
+        }
+        if (any_scale) {
+            double* d_scale = d_norm + s->ncols;
+            check_cuda(cudaMemcpyAsync(d_scale, scale.data(), s->ncols * sizeof(double), cudaMemcpyHostToDevice,
+                                       s->stream),
+                       "upload scales");
+            s->launch("renormalise", 2.0 * total * s->bsz(), [&] {
+                return launch_scale_columns(s->amps.p, s->prec, s->N, s->ncols, d_scale, s->stream);
+            });
+            s->sync();
+        }
     }
 }
 

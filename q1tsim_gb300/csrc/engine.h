@@ -79,6 +79,11 @@ struct q1g_state {
     // (the reference materialises them densely, src/vectorstate.rs:150-158).
     bool sparse = true;
     std::vector<uint64_t> basis{0};
+    // Squared norm each column should have.  Gates are unitary, so this only
+    // changes at construction and measurement; plans that ran on the tensor
+    // cores rescale their result to it (their FP32 accumulation rounds toward
+    // zero and shrinks the norm by ~1e-7 per block).
+    std::vector<double> norms{1.0};
 
     q1g::DevBuf amps, spare;
     q1g::DevBuf dscratch;   // doubles
@@ -152,6 +157,7 @@ struct q1g_state {
 struct q1g_plan {
     int nbits = 0;
     int width = 0;
+    int tensor_cores = 1;          // 1: complex64 dense blocks on tcgen05; 0: CUDA cores
     std::vector<std::vector<int>> gate_bits;
     std::vector<size_t> mat_off;   // offset (doubles) of each gate's matrix
     size_t mat_doubles = 0;

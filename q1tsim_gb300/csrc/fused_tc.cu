@@ -77,6 +77,16 @@ __device__ __forceinline__ float to_tf32(float x)
     return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
 }
 
+// Byte offset of tile coordinate j in the staging buffer: 16-byte chunks
+// (two amplitudes) XOR-swizzled by higher chunk bits, so that both the row
+// scatter and the linear read-out spread over the banks.
+__device__ __forceinline__ uint32_t stage_off(uint32_t j)
+{
+    const uint32_t c = j >> 1;
+    const uint32_t pc = c ^ ((c >> 3) & 7u) ^ ((c >> 6) & 7u);
+    return (pc << 4) | ((j & 1u) << 3);
+}
+
 __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
 {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
@@ -157,36 +167,55 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, IndexMap tilemap, TcOffsets 
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
 
-    // this thread's row offset
-    uint64_t row_off = 0;
+    // Tile coordinate j (12 bits) <-> tile positions tpos[b]; bit 0 of j is
+    // always position 0.  Thread tid moves the amplitude pairs
+    // j = 2*(tid + 128*k) + {0,1}, k = 0..15: consecutive threads touch
+    // consecutive 16-byte words of global memory.  (row t, gate g) of j is the
+    // OR of the contributions of its set bits.
+    uint64_t a_tid = 0;
+    uint32_t t_tid = 0, g_tid = 0;
+#pragma unroll
+    for (int b = 1; b < 8; ++b)
+        if ((tid >> (b - 1)) & 1) {
+            a_tid |= uint64_t(1) << offs.tpos[b];
+            t_tid |= offs.rowmask[b];
+            g_tid |= offs.gatemask[b];
+        }
+    const uint32_t t_e = offs.rowmask[0], g_e = offs.gatemask[0];
+    // tile coordinate of (row tid, g = 0), for staging the results
+    uint32_t jrow = 0;
 #pragma unroll
     for (int r = 0; r < 7; ++r)
-        if ((tid >> r) & 1) row_off |= uint64_t(1) << offs.rpos[r];
+        if ((tid >> r) & 1) jrow |= offs.row_tbit[r];
+    uint8_t* const stage = smem + kOffAlo;   // A_lo is free once the MMAs are done
 
-    const uint32_t swz = (uint32_t)(tid & 7);
-    const uint32_t row_byte = (uint32_t)(tid >> 3) * 1024u + (uint32_t)(tid & 7) * 128u;
-    float2 x[32];
+    float4 x[16];
     uint64_t tile = blockIdx.x;
-    uint64_t base = tile < ntiles ? expand_index(tile, tilemap) | row_off : 0;
+    uint64_t base = tile < ntiles ? expand_index(tile, tilemap) : 0;
     if (tile < ntiles) {
 #pragma unroll
-        for (int g = 0; g < 32; ++g) x[g] = a[base | offs.goff[g]];
+        for (int k = 0; k < 16; ++k) x[k] = *reinterpret_cast<const float4*>(a + (base | a_tid | offs.koff[k]));
     }
     uint32_t phase = 0;
     bool failed = false;
     for (; tile < ntiles; tile += gridDim.x) {
-        // operand A: hi and lo halves of this thread's row, swizzled
+        // operand A: hi and lo' halves, scattered into the swizzled K-major rows
 #pragma unroll
-        for (int c = 0; c < 16; ++c) {
-            const int g0 = 2 * c;
-            const float4 v = make_float4(x[g0].x, x[g0].y, x[g0 + 1].x, x[g0 + 1].y);
-            const float4 h = make_float4(to_tf32(v.x), to_tf32(v.y), to_tf32(v.z), to_tf32(v.w));
-            const float4 l = make_float4(to_tf32((v.x - h.x) * kLoScale), to_tf32((v.y - h.y) * kLoScale),
-                                         to_tf32((v.z - h.z) * kLoScale), to_tf32((v.w - h.w) * kLoScale));
-            const uint32_t atom = (uint32_t)(c >> 3) * kAtomA;
-            const uint32_t off = atom + row_byte + ((((uint32_t)c & 7u) ^ swz) << 4);
-            *(float4*)(smem + kOffAhi + off) = h;
-            *(float4*)(smem + kOffAlo + off) = l;
+        for (int k = 0; k < 16; ++k) {
+            const uint32_t tk = t_tid | offs.krow[k], gk = g_tid | offs.kgate[k];
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                const uint32_t t = e ? (tk | t_e) : tk;
+                const uint32_t g = e ? (gk | g_e) : gk;
+                const float vx = e ? x[k].z : x[k].x, vy = e ? x[k].w : x[k].y;
+                const float hx = to_tf32(vx), hy = to_tf32(vy);
+                const float2 h = make_float2(hx, hy);
+                const float2 l = make_float2(to_tf32((vx - hx) * kLoScale), to_tf32((vy - hy) * kLoScale));
+                const uint32_t off = (g >> 4) * kAtomA + (t >> 3) * 1024u + (t & 7u) * 128u +
+                                     ((((g & 15u) >> 1) ^ (t & 7u)) << 4) + (g & 1u) * 8u;
+                *(float2*)(smem + kOffAhi + off) = h;
+                *(float2*)(smem + kOffAlo + off) = l;
+            }
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
@@ -213,9 +242,10 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, IndexMap tilemap, TcOffsets 
         const uint64_t cur = base;
         const uint64_t next = tile + gridDim.x;
         if (next < ntiles) {
-            base = expand_index(next, tilemap) | row_off;
+            base = expand_index(next, tilemap);
 #pragma unroll
-            for (int g = 0; g < 32; ++g) x[g] = a[base | offs.goff[g]];
+            for (int k = 0; k < 16; ++k)
+                x[k] = *reinterpret_cast<const float4*>(a + (base | a_tid | offs.koff[k]));
         }
         uint32_t spins = 0;
         bool ok = true;
@@ -233,6 +263,7 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, IndexMap tilemap, TcOffsets 
         }
         phase ^= 1u;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        // row tid of D = D_main + 2^-11 D_corr, staged in tile-coordinate order
         const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
 #pragma unroll
         for (int half = 0; half < 2; ++half) {
@@ -246,10 +277,19 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, IndexMap tilemap, TcOffsets 
                 const float re = __fmaf_rn(__uint_as_float(dc[2 * j]), kLoUnscale, __uint_as_float(dm[2 * j]));
                 const float im =
                     __fmaf_rn(__uint_as_float(dc[2 * j + 1]), kLoUnscale, __uint_as_float(dm[2 * j + 1]));
-                a[cur | offs.goff[g]] = make_float2(re, im);
+                const uint32_t jc = jrow | offs.jgate[g];
+                *(float2*)(stage + stage_off(jc)) = make_float2(re, im);
             }
         }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            const uint32_t jc = 2u * (uint32_t)tid + 256u * (uint32_t)k;
+            *reinterpret_cast<float4*>(a + (cur | a_tid | offs.koff[k])) =
+                *reinterpret_cast<const float4*>(stage + stage_off(jc));
+        }
+        __syncthreads();   // staging read out before the next split overwrites it
     }
     if (failed) {
         // give the outstanding MMAs a second bounded chance to finish before

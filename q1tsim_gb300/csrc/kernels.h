@@ -29,11 +29,18 @@ cudaError_t launch_dense(void* amps, int prec, uint64_t total, const IndexMap& m
                          const DenseOffsets& offs, int tb, const void* dmat, cudaStream_t st);
 
 // ---- fused_tc.cu: 5-qubit fused blocks on the tensor cores (complex64)
-// rpos: the 7 row positions (ascending); goff[g]: offset of gate state g.
+// Geometry of a tile of 2^12 amplitudes (5 gate + 7 row positions).  Tile
+// coordinate bit b sits at position tpos[b]; it is row bit rowmask[b] or
+// gate bit gatemask[b] (one of the two is zero).
 struct TcOffsets {
-    int rpos[7];
-    int pad_;
-    uint64_t goff[32];
+    uint8_t tpos[12];
+    uint32_t rowmask[12];
+    uint32_t gatemask[12];
+    uint32_t row_tbit[7];    // tile-coordinate mask of row bit r
+    uint32_t jgate[32];      // tile coordinate of gate state g
+    uint64_t koff[16];       // address offset of tile bits 8..11 = k
+    uint32_t krow[16];       // row bits of tile bits 8..11 = k
+    uint32_t kgate[16];      // gate bits of tile bits 8..11 = k
 };
 uint32_t fused_tc_smem_bytes();
 // d_bimage: the block's 32 KB hi/lo image of the real 64x64 embedding in the
@@ -143,8 +150,12 @@ struct BatchArgs {
 };
 cudaError_t launch_batch(const BatchArgs& a, int sm_count, cudaStream_t st);
 
-// Per-block partials (6 doubles per block) comparing two states.
-cudaError_t launch_compare(const void* a, int prec_a, const void* b, int prec_b, uint64_t n,
+// Per-block partials (6 doubles per block) comparing two states; wa and wb
+// weight the probabilities in the total-variation term.
+cudaError_t launch_compare(const void* a, int prec_a, const void* b, int prec_b, uint64_t n, double wa, double wb,
                            double* part, unsigned blocks, cudaStream_t st);
+// Multiply column c by scales[c] (device array of ncols doubles).
+cudaError_t launch_scale_columns(void* amps, int prec, uint64_t col_len, uint64_t ncols, const double* d_scales,
+                                 cudaStream_t st);
 
 }  // namespace q1g

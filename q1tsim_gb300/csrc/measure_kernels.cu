@@ -200,10 +200,11 @@ k_sample(SampleArgs s)
 }
 
 // Per-block FP64 partials for comparing two states a, b of n amplitudes:
-// [sum|a|^2, sum|b|^2, Re<a|b>, Im<a|b>, sum||a|^2-|b|^2|, max|a-b|].
+// [sum|a|^2, sum|b|^2, Re<a|b>, Im<a|b>, sum|wa|a|^2 - wb|b|^2|, max|a-b|]
+// (wa, wb: 1/norms for the total variation of the outcome distributions).
 template <typename TA, typename TB>
 __global__ void __launch_bounds__(256)
-k_compare(const TA* __restrict__ a, const TB* __restrict__ b, uint64_t n, double* part)
+k_compare(const TA* __restrict__ a, const TB* __restrict__ b, uint64_t n, double wa, double wb, double* part)
 {
     __shared__ double red[32];
     double s[6] = {0, 0, 0, 0, 0, 0};
@@ -215,7 +216,7 @@ k_compare(const TA* __restrict__ a, const TB* __restrict__ b, uint64_t n, double
         s[1] += pb;
         s[2] += ar * br + ai * bi;
         s[3] += ar * bi - ai * br;
-        s[4] += fabs(pa - pb);
+        s[4] += fabs(pa * wa - pb * wb);
         const double dr = ar - br, di = ai - bi;
         s[5] = fmax(s[5], sqrt(dr * dr + di * di));
     }
@@ -232,6 +233,34 @@ k_compare(const TA* __restrict__ a, const TB* __restrict__ b, uint64_t n, double
         double mm = 0.0;
         for (int k = 0; k < (int)(blockDim.x >> 5); ++k) mm = fmax(mm, red[k]);
         part[uint64_t(blockIdx.x) * 6 + 5] = mm;
+    }
+}
+
+// Column c times scales[c]; col_len is a power of two (shift, no division),
+// and complex64 columns are scaled in FP32 with 16-byte accesses.
+__global__ void k_scale_columns_c64(float4* a, uint64_t n4, int col_shift4, const double* scales)
+{
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n4; i += stride) {
+        const float f = (float)scales[i >> col_shift4];
+        float4 v = a[i];
+        v.x *= f;
+        v.y *= f;
+        v.z *= f;
+        v.w *= f;
+        a[i] = v;
+    }
+}
+
+__global__ void k_scale_columns_c128(double2* a, uint64_t n, int col_shift, const double* scales)
+{
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const double f = scales[i >> col_shift];
+        double2 v = a[i];
+        v.x *= f;
+        v.y *= f;
+        a[i] = v;
     }
 }
 
@@ -322,17 +351,33 @@ cudaError_t launch_sorted_uniforms(uint64_t seed, uint64_t counter0, uint64_t m,
     return cudaGetLastError();
 }
 
-cudaError_t launch_compare(const void* a, int prec_a, const void* b, int prec_b, uint64_t n,
+cudaError_t launch_compare(const void* a, int prec_a, const void* b, int prec_b, uint64_t n, double wa, double wb,
                            double* part, unsigned blocks, cudaStream_t st)
 {
     if (prec_a == kC128 && prec_b == kC128)
-        k_compare<double2, double2><<<blocks, 256, 0, st>>>((const double2*)a, (const double2*)b, n, part);
+        k_compare<double2, double2><<<blocks, 256, 0, st>>>((const double2*)a, (const double2*)b, n, wa, wb, part);
     else if (prec_a == kC128)
-        k_compare<double2, float2><<<blocks, 256, 0, st>>>((const double2*)a, (const float2*)b, n, part);
+        k_compare<double2, float2><<<blocks, 256, 0, st>>>((const double2*)a, (const float2*)b, n, wa, wb, part);
     else if (prec_b == kC128)
-        k_compare<float2, double2><<<blocks, 256, 0, st>>>((const float2*)a, (const double2*)b, n, part);
+        k_compare<float2, double2><<<blocks, 256, 0, st>>>((const float2*)a, (const double2*)b, n, wa, wb, part);
     else
-        k_compare<float2, float2><<<blocks, 256, 0, st>>>((const float2*)a, (const float2*)b, n, part);
+        k_compare<float2, float2><<<blocks, 256, 0, st>>>((const float2*)a, (const float2*)b, n, wa, wb, part);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scale_columns(void* amps, int prec, uint64_t col_len, uint64_t ncols, const double* d_scales,
+                                 cudaStream_t st)
+{
+    int shift = 0;
+    while ((uint64_t(1) << shift) < col_len) ++shift;
+    if (prec == kC128) {
+        const uint64_t n = col_len * ncols;
+        k_scale_columns_c128<<<cap_grid((n + 255) / 256), 256, 0, st>>>((double2*)amps, n, shift, d_scales);
+    } else {
+        if (col_len < 2) return cudaErrorInvalidValue;   // pairs of amplitudes per float4
+        const uint64_t n4 = col_len * ncols / 2;
+        k_scale_columns_c64<<<cap_grid((n4 + 255) / 256), 256, 0, st>>>((float4*)amps, n4, shift - 1, d_scales);
+    }
     return cudaGetLastError();
 }
 

@@ -280,7 +280,7 @@ class VectorState:
 class Plan:
     """A gate sequence lowered once: structure, fusion grouping, passes."""
 
-    def __init__(self, nr_bits, gate_bits, fusion_width=0):
+    def __init__(self, nr_bits, gate_bits, fusion_width=0, tensor_cores=True):
         L = _lib.load()
         ks = np.asarray([len(b) for b in gate_bits], dtype=np.uint64)
         flat = np.asarray([q for b in gate_bits for q in b], dtype=np.uint64)
@@ -292,6 +292,8 @@ class Plan:
         self.nr_bits = nr_bits
         self.fusion_width = fusion_width
         self.ngates = len(ks)
+        self.tensor_cores = bool(tensor_cores)
+        check(L.q1g_plan_set_tensor_cores(h, 1 if tensor_cores else 0), "plan_set_tensor_cores")
 
     @property
     def handle(self):

@@ -477,3 +477,45 @@ def test_error_codes_on_gpu():
         s.apply_conditional_gate([1, 0, 1], G.X(), [0])
     with pytest.raises(_lib.InvalidQBit):
         s.measure_into(5, 0, np.zeros(4, dtype=np.uint64), Rng(0))
+
+
+def test_autotuned_circuit_matches_oracle():
+    """fusion_width="auto": the autotuner times the candidates and the chosen
+    plan gives the oracle's state."""
+    from q1tsim_gb300 import autotune, workloads
+    n = 13
+    c = workloads.brick(n, 6, 44, precision="c64", fusion_width="auto", measure=False)
+    st = VectorState(n, 1, "c64")
+    c.execute_with(1, Rng(1), st)
+    o = orc.OracleState.new(n, 1)
+    for op in c.ops:
+        o.apply_gate(op[1].matrix(), op[2])
+    ref, out = o.states()[:, 0], st.states()[:, 0]
+    assert 1 - abs(np.vdot(ref, out)) ** 2 / np.linalg.norm(out) ** 2 <= 1e-9
+    assert len(autotune.tune.last_timings) >= 5
+    assert autotune.tune.last_timings[0]["seconds"] <= autotune.tune.last_timings[-1]["seconds"]
+
+
+def test_fused_plan_renormalises_to_the_input_norm():
+    """After a tensor-core plan the column norms equal the input norms (an
+    unnormalised input keeps its norm)."""
+    rng = np.random.default_rng(17)
+    n = 14
+    amps = 1.7 * rand_state(n, rng)
+    gl = [random_gate(n, rng) for _ in range(60)]
+    mats = np.concatenate([np.ascontiguousarray(gt.matrix()).ravel() for gt, _ in gl]).view(np.float64)
+    g = VectorState.from_amplitudes(amps, 1, "c64")
+    g.apply_plan(Plan(n, [b for _, b in gl], 5), mats)
+    out = g.states()[:, 0]
+    assert abs(np.linalg.norm(out) ** 2 / 1.7 ** 2 - 1.0) <= 2e-6
+
+
+def test_compare_reports_normalised_tv():
+    rng = np.random.default_rng(2)
+    n = 12
+    amps = rand_state(n, rng)
+    a = VectorState.from_amplitudes(amps, 1, "c128")
+    b = VectorState.from_amplitudes(0.5 * amps, 1, "c64")
+    r = a.compare(b)
+    assert r["tv"] <= 1e-6 and r["infidelity"] <= 1e-12
+    assert abs(r["norm_b"] - 0.25) <= 1e-6
