@@ -299,6 +299,40 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def plain_kernel_leg(n, bits, mats, stream, barrier, ngates=120):
+    """The first `ngates` gates of the circuit, one pass per gate, in both
+    precisions: per kernel, launches, time per launch and achieved HBM
+    bandwidth (bytes of the amplitudes each launch touches, read and written)
+    against the measured peak."""
+    from q1tsim_gb300 import Plan, VectorState
+    peak, peak_kind = peaks()
+    sub = bits[:ngates]
+    ndbl = sum(2 * (1 << len(b)) ** 2 for b in sub)
+    out = {"gates": len(sub), "peak_gbs": peak, "peak_kind": peak_kind}
+    for prec in ("c64", "c128"):
+        st = VectorState(n, 1, prec)
+        st.set_stream(stream.cuda_stream)
+        plan = Plan(n, sub, 0)
+        st.apply_plan(plan, mats[:ndbl])      # warm-up: allocation, first touch
+        barrier()
+        st.profile(True)
+        st.profile_report(reset=True)
+        st.apply_plan(plan, mats[:ndbl])
+        prof = st.profile_report(reset=True)
+        st.profile(False)
+        ks = {}
+        for k, v in prof.items():
+            if not k.startswith(("pair", "phase", "dense")):
+                continue
+            gbs = v["bytes"] / (v["ms"] / 1e3) / 1e9
+            ks[k] = {"launches": v["launches"], "ms_per_launch": round(v["ms"] / v["launches"], 4),
+                     "gbs": round(gbs, 1), "frac": round(gbs / peak, 3)}
+        out[prec] = ks
+        del st
+        barrier()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -438,6 +472,9 @@ def main():
                       "fused_speedup": (ngates / (gate_ms_max / args.steps / 1e3)) / (ngates / (plain_ms / 1e3))}
         del plain
 
+    # ---- plain (unfused) gate kernels: the first layers, per-kernel profile
+    plain_kernels = None if args.no_plain else plain_kernel_leg(n, bits, mats, stream, barrier)
+
     # ---- end to end through the public Circuit API (host in, results out)
     circ = Circuit(n, n, precision="c64", fusion_width=args.fusion)
     for g, b in gates:
@@ -478,6 +515,7 @@ def main():
                        "parallelism": f"replicas{world}", "l2": "state 8 GiB > L2, no flush needed"},
             "shots_per_s": shots_per_s, "shot_sampling_ms": shot_ms / args.steps,
             "plain_c128": plain_info, "accuracy_c64_vs_c128": accuracy,
+            "plain_kernels": plain_kernels,
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                          "launch_ms": dom["ms"] / dom["launches"],

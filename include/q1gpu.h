@@ -157,6 +157,14 @@ int q1g_plan_info(const q1g_plan* p, size_t* ngates, size_t* nblocks);
  * the gates it absorbed, in application order (*ng in/out). */
 int q1g_plan_block(const q1g_plan* p, size_t i, size_t* qubits, size_t* nq, size_t* gates,
                    size_t* ng);
+/* The fused 2^m x 2^m matrix of block i (m = its qubit count, qubits
+ * ascending, first qubit the most significant index bit) for the gate
+ * matrices mats_flat, written row-major as (re, im) doubles into out
+ * (*n_out in: capacity in doubles, out: 2 * 4^m).  Host only, no device
+ * work.  No reference counterpart: it exposes the matrix the fusion pass
+ * (src/circuit.rs:651-653 runs the gates one by one) applies in one pass. */
+int q1g_plan_block_matrix(const q1g_plan* p, size_t i, const double* mats_flat, size_t n_doubles, double* out,
+                          size_t* n_out);
 /* mats_flat = all gates' matrices concatenated ((re, im) doubles). */
 int q1g_plan_run(q1g_plan* p, q1g_state* s, const double* mats_flat, size_t n_doubles);
 /* Kernel for dense complex64 blocks of >= 3 qubits on states of >= 12 qubits:

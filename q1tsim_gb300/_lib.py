@@ -135,6 +135,7 @@ def load():
     _proto(L, "q1g_plan_free", None, [_vp])
     _proto(L, "q1g_plan_info", _int, [_vp, _szp, _szp])
     _proto(L, "q1g_plan_block", _int, [_vp, _sz, _szp, _szp, _szp, _szp])
+    _proto(L, "q1g_plan_block_matrix", _int, [_vp, _sz, _dp, _sz, _dp, _szp])
     _proto(L, "q1g_plan_run", _int, [_vp, _vp, _dp, _sz])
     _proto(L, "q1g_plan_set_tensor_cores", _int, [_vp, _int])
     _proto(L, "q1g_profile_enable", _int, [_vp, _int])

@@ -420,6 +420,37 @@ int q1g_plan_block(const q1g_plan* p, size_t i, size_t* qubits, size_t* nq, size
     });
 }
 
+int q1g_plan_block_matrix(const q1g_plan* p, size_t i, const double* mats_flat, size_t n_doubles, double* out,
+                          size_t* n_out)
+{
+    return guarded([&] {
+        need(p, "plan");
+        need(n_out, "n_out");
+        if (n_doubles) need(mats_flat, "mats_flat");
+        if (i >= p->blocks.size()) throw Error(Q1G_ERR_INVALID_ARGUMENT, "block index out of range");
+        if (n_doubles != p->mat_doubles)
+            throw Error(Q1G_ERR_INVALID_ARGUMENT, "expected " + std::to_string(p->mat_doubles) + " matrix doubles");
+        const auto& b = p->blocks[i];
+        const size_t dim = size_t(1) << b.qubits.size();
+        if (*n_out < 2 * dim * dim) throw Error(Q1G_ERR_NOT_ENOUGH_SPACE, "output buffer too small");
+        need(out, "out");
+        std::vector<q1g::SeqGate> gates(p->gate_bits.size());
+        for (int gi : b.gates) {
+            const size_t gd = size_t(1) << p->gate_bits[gi].size();
+            gates[gi].bits = p->gate_bits[gi];
+            gates[gi].mat.resize(gd * gd);
+            const double* m = mats_flat + p->mat_off[gi];
+            for (size_t e = 0; e < gd * gd; ++e) gates[gi].mat[e] = q1g::cd(m[2 * e], m[2 * e + 1]);
+        }
+        const auto mat = q1g::block_matrix(b, gates);
+        for (size_t e = 0; e < mat.size(); ++e) {
+            out[2 * e] = mat[e].real();
+            out[2 * e + 1] = mat[e].imag();
+        }
+        *n_out = 2 * dim * dim;
+    });
+}
+
 int q1g_plan_set_tensor_cores(q1g_plan* p, int enable)
 {
     return guarded([&] {

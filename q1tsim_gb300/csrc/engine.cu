@@ -327,12 +327,14 @@ std::vector<double> q1g_state::zero_weights(size_t qbit)
     const uint64_t half = N / 2;
     const uint64_t chunk = std::min<uint64_t>(half, 4096);
     const uint64_t nchunks = ncols * (half / chunk);
-    dscratch.ensure((nchunks + ncols) * sizeof(double));
+    const uint64_t ntmp = segment_sums_tmp_doubles(ncols, half / chunk);
+    dscratch.ensure((nchunks + ncols + ntmp) * sizeof(double));
     double* d = dscratch.as<double>();
     launch("qubit_weights", double(ncols * half * bsz()), [&] {
         return launch_chunk_sums(amps.p, prec, ncols * half, chunk, m, d, stream);
     });
-    check_cuda(launch_segment_sums(d, ncols, half / chunk, d + nchunks, stream), "segment_sums");
+    check_cuda(launch_segment_sums(d, ncols, half / chunk, d + nchunks, d + nchunks + ncols, stream),
+               "segment_sums");
     hstage.ensure(ncols * sizeof(double));
     check_cuda(cudaMemcpyAsync(hstage.p, d + nchunks, ncols * sizeof(double), cudaMemcpyDeviceToHost, stream),
                "download weights");
@@ -595,75 +597,108 @@ q1g_plan::~q1g_plan()
 
 namespace q1g {
 
-// Tensor-core lowering of one fused block: the block matrix on its qubits,
-// padded with untouched qubits to five, the tile geometry and the 32 KB
-// operand image.
-struct TcBlock {
+// Tensor-core lowering of a pass: one or two fused blocks (each <= 5
+// qubits) whose positions fit in one 12-position tile.  Each block is padded
+// with untouched tile positions to five gate positions; its other seven tile
+// positions are its rows.
+struct TcPass {
     IndexMap tilemap{};
     TcOffsets offs{};
-    std::vector<float> image;
+    std::vector<float> images;   // nblocks x 32 KB
 };
 
-static TcBlock lower_tc(const std::vector<cd>& mat, const std::vector<int>& bits, int nbits)
+static std::vector<int> positions_of(const std::vector<int>& qubits, int nbits)
 {
-    // pad with the lowest-numbered (highest-position) qubits the block leaves alone
-    std::vector<int> q = bits;
-    for (int cand = 0; (int)q.size() < 5 && cand < nbits; ++cand)
-        if (std::find(q.begin(), q.end(), cand) == q.end()) q.push_back(cand);
-    std::sort(q.begin(), q.end());
-    const auto m32 = embed_matrix(mat, bits, q);
-    std::vector<double> md(2 * 32 * 32);
-    for (size_t e = 0; e < m32.size(); ++e) {
-        md[2 * e] = m32[e].real();
-        md[2 * e + 1] = m32[e].imag();
-    }
-    TcBlock t;
-    t.image.assign(16384 / 4 * 2, 0.0f);
-    build_tc_image(md.data(), t.image.data());
-    std::vector<int> gpos(5);
-    for (int j = 0; j < 5; ++j) gpos[j] = nbits - 1 - q[j];
-    std::vector<int> rows;
-    for (int p = 0; (int)rows.size() < 7; ++p)
-        if (std::find(gpos.begin(), gpos.end(), p) == gpos.end()) rows.push_back(p);
-    std::vector<int> z = gpos;
-    z.insert(z.end(), rows.begin(), rows.end());
-    std::sort(z.begin(), z.end());
+    std::vector<int> p;
+    for (int q : qubits) p.push_back(nbits - 1 - q);
+    std::sort(p.begin(), p.end());
+    return p;
+}
+
+// The tile of a pass: the blocks' positions plus the lowest other positions,
+// 12 in all, ascending.
+static std::vector<int> tile_positions(const std::vector<const std::vector<int>*>& bits, int nbits)
+{
+    std::vector<int> T;
+    for (auto* b : bits)
+        for (int p : positions_of(*b, nbits))
+            if (std::find(T.begin(), T.end(), p) == T.end()) T.push_back(p);
+    for (int p = 0; (int)T.size() < 12 && p < nbits; ++p)
+        if (std::find(T.begin(), T.end(), p) == T.end()) T.push_back(p);
+    std::sort(T.begin(), T.end());
+    return T;
+}
+
+// Tile bits 0..L-1 are positions 0..L-1: the tile is 2^(12-L) contiguous runs.
+static int tile_run_bits(const std::vector<int>& T)
+{
+    int L = 0;
+    while (L < (int)T.size() && T[L] == L) ++L;
+    return L;
+}
+
+// Shortest contiguous run a pass may copy (2^7 amplitudes = 1 KB): at most 32
+// runs per tile.
+constexpr int kMinTcRunBits = 7;
+
+static TcPass lower_tc_pass(const std::vector<const std::vector<cd>*>& mats,
+                            const std::vector<const std::vector<int>*>& bits, int nbits)
+{
+    TcPass t;
+    const std::vector<int> T = tile_positions(bits, nbits);
+    auto tbit = [&](int pos) { return (int)(std::find(T.begin(), T.end(), pos) - T.begin()); };
     t.tilemap.nz = 12;
-    for (int j = 0; j < 12; ++j) t.tilemap.zpos[j] = z[j];
+    for (int j = 0; j < 12; ++j) t.tilemap.zpos[j] = T[j];
     t.tilemap.setmask = 0;
-    // tile coordinate bit b <-> position z[b]
-    for (int b = 0; b < 12; ++b) {
-        t.offs.tpos[b] = (uint8_t)z[b];
-        t.offs.rowmask[b] = 0;
-        t.offs.gatemask[b] = 0;
-        for (int r = 0; r < 7; ++r)
-            if (rows[r] == z[b]) {
-                t.offs.rowmask[b] = 1u << r;
-                t.offs.row_tbit[r] = 1u << b;
-            }
-        for (int j = 0; j < 5; ++j)
-            if (gpos[j] == z[b]) t.offs.gatemask[b] = 1u << (4 - j);
-    }
-    for (int g = 0; g < 32; ++g) {
-        uint32_t jc = 0;
-        for (int b = 0; b < 12; ++b)
-            if (t.offs.gatemask[b] && (g & t.offs.gatemask[b])) jc |= 1u << b;
-        t.offs.jgate[g] = jc;
-    }
-    for (int k = 0; k < 16; ++k) {
+    const int L = tile_run_bits(T);
+    if (L < kMinTcRunBits) throw Error(Q1G_ERR_INVALID_ARGUMENT, "tensor-core tile with runs shorter than 128 amplitudes");
+    t.offs.run_bits = (uint32_t)L;
+    t.offs.nruns = 1u << (12 - L);
+    for (uint32_t r = 0; r < t.offs.nruns; ++r) {
         uint64_t o = 0;
-        uint32_t rr = 0, gg = 0;
-        for (int b = 8; b < 12; ++b)
-            if ((k >> (b - 8)) & 1) {
-                o |= uint64_t(1) << z[b];
-                rr |= t.offs.rowmask[b];
-                gg |= t.offs.gatemask[b];
-            }
-        t.offs.koff[k] = o;
-        t.offs.krow[k] = rr;
-        t.offs.kgate[k] = gg;
+        for (int b = L; b < 12; ++b)
+            if ((r >> (b - L)) & 1) o |= uint64_t(1) << T[b];
+        t.offs.run_off[r] = o;
     }
+    t.offs.nblocks = (uint32_t)mats.size();
+    t.images.assign(mats.size() * (32768 / 4), 0.0f);
+    for (size_t bi = 0; bi < mats.size(); ++bi) {
+        // gate qubits: the block's own, padded from the tile's highest positions
+        std::vector<int> gpos = positions_of(*bits[bi], nbits);
+        for (int j = 11; (int)gpos.size() < 5; --j)
+            if (std::find(gpos.begin(), gpos.end(), T[j]) == gpos.end()) gpos.push_back(T[j]);
+        std::vector<int> q;
+        for (int p : gpos) q.push_back(nbits - 1 - p);
+        std::sort(q.begin(), q.end());   // ascending qubits: q[0] is the matrix MSB
+        const auto m32 = embed_matrix(*mats[bi], *bits[bi], q);
+        std::vector<double> md(2 * 32 * 32);
+        for (size_t e = 0; e < m32.size(); ++e) {
+            md[2 * e] = m32[e].real();
+            md[2 * e + 1] = m32[e].imag();
+        }
+        build_tc_image(md.data(), t.images.data() + bi * (32768 / 4));
+        TcBlockGeom& G = t.offs.blk[bi];
+        int r = 0;
+        for (int j = 0; j < 12; ++j)
+            if (std::find(gpos.begin(), gpos.end(), T[j]) == gpos.end()) G.jrow_bit[r++] = 1u << j;
+        for (int g = 0; g < 32; ++g) {
+            uint32_t jc = 0;
+            for (int j = 0; j < 5; ++j)
+                if ((g >> (4 - j)) & 1) jc |= 1u << tbit(nbits - 1 - q[j]);
+            G.jgate[g] = jc;
+        }
+        G.vec2 = G.jgate[1] == 1u ? 1u : 0u;
+    }
+    tc_choose_padding(t.offs);
     return t;
+}
+
+static size_t union_size(const std::vector<int>& a, const std::vector<int>& b)
+{
+    std::vector<int> u = a;
+    for (int x : b)
+        if (std::find(u.begin(), u.end(), x) == u.end()) u.push_back(x);
+    return u.size();
 }
 
 void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n)
@@ -683,108 +718,127 @@ void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n)
         for (size_t e = 0; e < dim * dim; ++e) gates[g].mat[e] = cd(m[2 * e], m[2 * e + 1]);
     }
     const bool use_tc = s->prec == kC64 && s->nbits >= 12 && p->tensor_cores;
-    std::vector<GateOp> ops;
-    std::vector<TcBlock> tcs;
-    std::vector<int> tc_of(p->blocks.size(), -1);
-    ops.reserve(p->blocks.size());
-    for (size_t bi = 0; bi < p->blocks.size(); ++bi) {
+    const size_t nb = p->blocks.size();
+    // Blocks are lowered one pass ahead of the launches, so the host work of
+    // pass i+1 (block product, classification, tensor-core image) runs while
+    // the device executes pass i.
+    std::vector<GateOp> ops(nb);
+    std::vector<std::vector<cd>> bmats(nb);
+    std::vector<std::vector<int>> bbits(nb);
+    std::vector<char> ready(nb, 0);
+    auto prepare = [&](size_t bi) {
+        if (ready[bi]) return;
         const auto& b = p->blocks[bi];
-        std::vector<cd> m;
-        std::vector<int> bits;
         if (b.gates.size() == 1) {
-            m = gates[b.gates[0]].mat;
-            bits = gates[b.gates[0]].bits;
+            bmats[bi] = gates[b.gates[0]].mat;
+            bbits[bi] = gates[b.gates[0]].bits;
         } else {
-            m = block_matrix(b, gates);
-            bits = b.qubits;
+            bmats[bi] = block_matrix(b, gates);
+            bbits[bi] = b.qubits;
         }
-        ops.push_back(classify(m.data(), (int)bits.size(), bits.data(), s->nbits));
-        if (use_tc && ops.back().kind == GateOp::Dense && ops.back().t >= 3 && bits.size() <= 5) {
-            tc_of[bi] = (int)tcs.size();
-            tcs.push_back(lower_tc(m, bits, s->nbits));
-        }
-    }
-    // Stage every dense matrix and tensor-core image in one pinned upload.
-    size_t bytes = 0;
-    std::vector<size_t> off(ops.size(), 0);
-    const size_t esz = s->prec == kC128 ? 16 : 8;
-    for (size_t i = 0; i < ops.size(); ++i) {
-        size_t sz = 0;
-        if (tc_of[i] >= 0) sz = tcs[tc_of[i]].image.size() * sizeof(float);
-        else if (ops[i].kind == GateOp::Dense) sz = ops[i].dense.size() * esz;
-        if (!sz) continue;
-        off[i] = bytes;
-        bytes += (sz + 255) & ~size_t(255);
-    }
-    if (bytes) {
-        if (p->staged) check_cuda(cudaEventSynchronize(p->staged), "plan staging wait");
-        else check_cuda(cudaEventCreateWithFlags(&p->staged, cudaEventDisableTiming), "cudaEventCreate");
-        p->hmats.ensure(bytes);
-        p->dmats.ensure(bytes);
-        for (size_t i = 0; i < ops.size(); ++i) {
-            char* dst = p->hmats.as<char>() + off[i];
-            if (tc_of[i] >= 0) {
-                const auto& img = tcs[tc_of[i]].image;
-                std::memcpy(dst, img.data(), img.size() * sizeof(float));
-                continue;
-            }
-            if (ops[i].kind != GateOp::Dense) continue;
-            for (size_t e = 0; e < ops[i].dense.size(); ++e) {
-                if (s->prec == kC128) {
-                    double v[2] = {ops[i].dense[e].real(), ops[i].dense[e].imag()};
-                    std::memcpy(dst + e * 16, v, 16);
-                } else {
-                    float v[2] = {(float)ops[i].dense[e].real(), (float)ops[i].dense[e].imag()};
-                    std::memcpy(dst + e * 8, v, 8);
-                }
-            }
-        }
-        check_cuda(cudaMemcpyAsync(p->dmats.p, p->hmats.p, bytes, cudaMemcpyHostToDevice, s->stream),
-                   "upload plan matrices");
-        check_cuda(cudaEventRecord(p->staged, s->stream), "cudaEventRecord");
-    }
-    p->last_h2d_bytes = bytes;
-    bool any = false;
-    for (const auto& op : ops) any |= op.kind != GateOp::Noop;
-    if (!any) return;
-    s->ensure_dense();
-    const uint64_t total = s->total();
-    const double b2 = 2.0 * s->bsz();
-    if (!tcs.empty()) {
-        s->errbuf.ensure(sizeof(int));
-        check_cuda(cudaMemsetAsync(s->errbuf.p, 0, sizeof(int), s->stream), "clear error flag");
-    }
-    for (size_t i = 0; i < ops.size(); ++i) {
+        ops[bi] = classify(bmats[bi].data(), (int)bbits[bi].size(), bbits[bi].data(), s->nbits);
+        ready[bi] = 1;
+    };
+    // tensor-core eligible: dense blocks of >= 3 target qubits
+    auto eligible = [&](size_t bi) {
+        prepare(bi);
+        return use_tc && ops[bi].kind == GateOp::Dense && ops[bi].t >= 3 && bbits[bi].size() <= 5;
+    };
+    // Staging: every pass uploads its matrix or tensor-core image from its own
+    // slice of one pinned buffer (at most 32 KB per block).
+    if (p->staged) check_cuda(cudaEventSynchronize(p->staged), "plan staging wait");
+    else check_cuda(cudaEventCreateWithFlags(&p->staged, cudaEventDisableTiming), "cudaEventCreate");
+    p->hmats.ensure(std::max<size_t>(nb, 1) * 32768);
+    p->dmats.ensure(std::max<size_t>(nb, 1) * 32768);
+    size_t staged = 0;
+    auto stage = [&](const void* src, size_t sz) -> const void* {
+        char* h = p->hmats.as<char>() + staged;
+        char* d = p->dmats.as<char>() + staged;
+        std::memcpy(h, src, sz);
+        check_cuda(cudaMemcpyAsync(d, h, sz, cudaMemcpyHostToDevice, s->stream), "upload plan matrix");
+        staged += (sz + 255) & ~size_t(255);
+        return d;
+    };
+    bool launched = false, any_tc = false;
+    auto begin = [&] {
+        if (!launched) s->ensure_dense();
+        launched = true;
+    };
+    for (size_t i = 0; i < nb; ++i) {
+        prepare(i);
         const GateOp& op = ops[i];
-        if (tc_of[i] >= 0) {
-            const TcBlock& t = tcs[tc_of[i]];
-            const void* img = p->dmats.as<char>() + off[i];
-            const uint64_t ntiles = total >> 12;
+        if (op.kind == GateOp::Noop) continue;
+        if (eligible(i)) {
+            // two consecutive blocks share a pass when their qubits fit one
+            // 12-position tile with runs of >= 128 amplitudes
+            std::vector<const std::vector<cd>*> ms{&bmats[i]};
+            std::vector<const std::vector<int>*> bs{&bbits[i]};
+            if (i + 1 < nb && eligible(i + 1) &&
+                union_size(positions_of(bbits[i], s->nbits), positions_of(bbits[i + 1], s->nbits)) <= 12 &&
+                tile_run_bits(tile_positions({&bbits[i], &bbits[i + 1]}, s->nbits)) >= kMinTcRunBits) {
+                ms.push_back(&bmats[i + 1]);
+                bs.push_back(&bbits[i + 1]);
+            }
+            const TcPass t = lower_tc_pass(ms, bs, s->nbits);
+            begin();
+            if (!any_tc) {
+                s->errbuf.ensure(sizeof(int));
+                check_cuda(cudaMemsetAsync(s->errbuf.p, 0, sizeof(int), s->stream), "clear error flag");
+                any_tc = true;
+            }
+            const void* img = stage(t.images.data(), t.images.size() * sizeof(float));
+            const uint64_t total = s->total();
             s->launch("fused_tc_c64", 2.0 * total * s->bsz(), [&] {
-                return launch_fused_tc(s->amps.as<float2>(), ntiles, t.tilemap, t.offs, img,
+                return launch_fused_tc(s->amps.as<float2>(), total >> 12, t.tilemap, t.offs, img,
                                        s->errbuf.as<int>(), s->sm_count(), s->stream);
             });
+            if (ms.size() == 2) ++i;   // the next block rode in this pass
         } else if (op.kind == GateOp::Dense) {
-            const void* dm = p->dmats.as<char>() + off[i];
-            s->launch(s->prec == kC128 ? "dense_c128" : "dense_c64", b2 * op.touched(total), [&] {
+            begin();
+            const size_t d2 = op.dense.size();
+            const void* dm;
+            if (s->prec == kC128) {
+                std::vector<double> v(2 * d2);
+                for (size_t e = 0; e < d2; ++e) {
+                    v[2 * e] = op.dense[e].real();
+                    v[2 * e + 1] = op.dense[e].imag();
+                }
+                dm = stage(v.data(), v.size() * sizeof(double));
+            } else {
+                std::vector<float> v(2 * d2);
+                for (size_t e = 0; e < d2; ++e) {
+                    v[2 * e] = (float)op.dense[e].real();
+                    v[2 * e + 1] = (float)op.dense[e].imag();
+                }
+                dm = stage(v.data(), v.size() * sizeof(float));
+            }
+            const uint64_t total = s->total();
+            s->launch(s->prec == kC128 ? "dense_c128" : "dense_c64", 2.0 * s->bsz() * op.touched(total), [&] {
                 return launch_dense(s->amps.p, s->prec, total, op.map, op.offs, op.t, dm, s->stream);
             });
         } else {
-            s->apply_op(op, s->amps.as<char>(), total);
+            begin();
+            s->apply_op(op, s->amps.as<char>(), s->total());
         }
     }
-    if (!tcs.empty()) {
+    if (staged) check_cuda(cudaEventRecord(p->staged, s->stream), "cudaEventRecord");
+    p->last_h2d_bytes = staged;
+    if (!launched) return;
+    if (any_tc) {
         // per-column squared norms after the plan, then rescale each column to
         // the norm it had before (the plan is unitary)
+        const uint64_t total = s->total();
         const uint64_t chunk = std::min<uint64_t>(s->N, 256);
         const uint64_t nch = s->N / chunk;
-        s->dscratch.ensure((s->ncols * nch + 2 * s->ncols) * sizeof(double));
+        const uint64_t ntmp = segment_sums_tmp_doubles(s->ncols, nch);
+        s->dscratch.ensure((s->ncols * nch + 2 * s->ncols + ntmp) * sizeof(double));
         double* d_sums = s->dscratch.as<double>();
         double* d_norm = d_sums + s->ncols * nch;
         s->launch("norm_check", double(total * s->bsz()), [&] {
             return launch_chunk_sums_dense(s->amps.p, s->prec, total, chunk, d_sums, s->stream);
         });
-        check_cuda(launch_segment_sums(d_sums, s->ncols, nch, d_norm, s->stream), "segment_sums");
+        check_cuda(launch_segment_sums(d_sums, s->ncols, nch, d_norm, d_norm + 2 * s->ncols, s->stream),
+                   "segment_sums");
         s->hstage.ensure(s->ncols * sizeof(double) + sizeof(int));
         double* h_norm = s->hstage.as<double>();
         int* h_flag = reinterpret_cast<int*>(h_norm + s->ncols);

@@ -2,32 +2,50 @@
 //
 // A fused block is a dense 32x32 complex matrix M on five qubits (gate
 // positions p_0 > ... > p_4).  The state is cut into tiles of 2^12
-// amplitudes: the 5 gate positions plus the 7 lowest other positions
-// ("row" positions); the remaining positions enumerate the tiles.  In a tile,
-// row t (0..127) holds the 32 amplitudes of one group, so the update is the
-// real GEMM
+// amplitudes: the 5 gate positions plus 7 other positions ("row"
+// positions); the remaining positions enumerate the tiles.  In a tile, row t
+// (0..127) holds the 32 amplitudes of one group, so the update is the real
+// GEMM
 //     D[t][n] = sum_k A[t][k] * R[n][k],   A[t][2g+c] = component c of amp(t, g),
 // with R the 64x64 real embedding of M (R[2g'][2g] = Re M, R[2g'][2g+1] = -Im M,
 // R[2g'+1][2g] = Im M, R[2g'+1][2g+1] = Re M).  It runs on tcgen05.mma
-// kind::tf32 (M=128, N=64, K=8) with the accumulator in TMEM.  FP32 accuracy
-// comes from the 3xTF32 split (Ootomo & Yokota 2022): x = hi + lo with
-// hi = tf32(x), lo = tf32(x - hi), and D = A_hi*B_hi + (A_lo*B_hi + A_hi*B_lo).
-// The correction products go to a second TMEM accumulator with the lo halves
-// pre-scaled by 2^11 (exact), and the epilogue adds D_corr * 2^-11: summed in
-// one accumulator with the main products, the correction terms were lost.
+// kind::tf32 (M=128, K=8) with A and the accumulators in tensor memory and R
+// in shared memory.  FP32 accuracy comes from the 3xTF32 split (Ootomo &
+// Yokota 2022): x = hi + lo with hi = tf32(x), lo = tf32(x - hi), and
+// D = A_hi*B_hi + (A_lo*B_hi + A_hi*B_lo).  The correction products go to a
+// second accumulator with the lo halves pre-scaled by 2^11 (exact), and the
+// epilogue adds D_corr * 2^-11: summed in one accumulator with the main
+// products, the correction terms were lost.  B is stored as [B_hi; B_lo]
+// (128 rows), so A_hi*[B_hi; B_lo] is one N=128 product into
+// [D_main | D_corr] and A_lo*B_hi one N=64 product added to D_corr:
+// 16 MMAs per block and tile.
 //
-// One CTA = 4 warps; thread t owns row t: it loads its 32 amplitudes (for a
-// fixed g the warp reads 32 consecutive row positions, so loads and stores
-// are coalesced), writes the hi/lo halves into the K-major SWIZZLE_128B
-// operand tiles in shared memory, and after the MMAs reads its TMEM lane
-// back with tcgen05.ld and stores the 32 results in place.  The next tile's
-// loads are issued before waiting on the current tile's MMAs.  B (the block's
-// hi/lo image, 32 KB) is prepared on the host in the same swizzled layout.
-// Every mbarrier wait is bounded: on expiry the kernel records an error and
-// releases its TMEM before returning.
+// One CTA per SM, persistent over tiles, with 10 warps:
+//   warp 8   loader: cp.async.bulk copies of a tile's pieces into a ring of
+//            shared-memory stages, completing on the stage's `full` mbarrier;
+//   warp 9   storer: when a tile is done, bulk-stores it back and, once the
+//            copy has read the stage, frees it on its `empty` mbarrier;
+//   warps 0-3 and 4-7: two consumer groups taking alternate tiles.  Each
+//            thread owns one row t (its TMEM lane): it reads the row's 32
+//            amplitudes from the stage, writes hi/lo to its group's A columns
+//            with tcgen05.st, one thread issues the MMAs, and after the commit
+//            each thread reads its row of D with tcgen05.ld and writes the
+//            new amplitudes back into the stage.  While one group waits for
+//            its MMAs the other converts or writes back, so the tensor pipe,
+//            the ALUs and the copy engine work at the same time.
+// TMEM (512 columns): group g uses 256g + [0,64) A_hi, [64,128) A_lo,
+// [128,192) D_main, [192,256) D_corr.  Every wait is bounded; on expiry the
+// CTA records an error, lets its copies land and releases its TMEM before
+// returning.
 #include <cuda_runtime.h>
 
 #include <cstring>
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <set>
+#include <string>
+#include <unordered_map>
 
 #include "common.cuh"
 #include "kernels.h"
@@ -36,19 +54,30 @@ namespace q1g {
 
 namespace {
 
-constexpr int kTcThreads = 128;
-constexpr uint32_t kTmemCols = 128;   // D_main in columns 0-63, D_corr in 64-127
+constexpr int kGroupThreads = 128;
+constexpr int kConsumers = 2 * kGroupThreads;   // warps 0-7
+constexpr int kLoaderWarp = 8;
+constexpr int kStorerWarp = 9;
+constexpr int kTcThreads = kConsumers + 64;
+constexpr uint32_t kTileBytes = 4096 * 8;        // one tile (complex64), without padding
+constexpr uint32_t kTmemCols = 512;
 constexpr float kLoScale = 2048.0f;     // 2^11: lo halves are stored scaled up
 constexpr float kLoUnscale = 1.0f / 2048.0f;
-constexpr uint32_t kAtomA = 16384;   // 128 rows x 128 B
-constexpr uint32_t kAtomB = 8192;    // 64 rows x 128 B
-constexpr uint32_t kOffAhi = 0;
-constexpr uint32_t kOffAlo = 2 * kAtomA;
-constexpr uint32_t kOffBhi = 4 * kAtomA;
-constexpr uint32_t kOffBlo = 4 * kAtomA + 2 * kAtomB;
-constexpr uint32_t kOffBar = 4 * kAtomA + 4 * kAtomB;   // mbarrier (8 B) + TMEM slot (4 B)
-constexpr uint32_t kSmemBytes = kOffBar + 64 + 1024;     // + alignment slack
-constexpr uint32_t kSpinLimit = 1u << 26;
+constexpr uint32_t kBAtom = 16384;      // one K-atom of [B_hi; B_lo]: 128 rows x 128 B
+constexpr uint32_t kBImage = 2 * kBAtom;   // one block's image (K = 64)
+constexpr uint32_t kMaxStages = 8;
+// shared memory: [0, 1024) barriers, TMEM slot, abort flag, run offsets;
+// then nblocks B images; then the stages.
+constexpr uint32_t kOffFull = 0;        // 8 B per stage
+constexpr uint32_t kOffEmpty = 64;
+constexpr uint32_t kOffOut = 128;
+constexpr uint32_t kOffMma = 192;       // one per group
+constexpr uint32_t kOffSlot = 208;
+constexpr uint32_t kOffAbort = 212;
+constexpr uint32_t kOffRunOff = 256;    // 32 x u64
+constexpr uint32_t kOffB = 1024;
+constexpr uint32_t kAlignSlack = 1024;
+constexpr uint32_t kSpinLimit = 1u << 22;
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p)
 {
@@ -67,24 +96,19 @@ __device__ __forceinline__ uint64_t desc_sw128(uint32_t saddr)
     return d;
 }
 
-// Instruction descriptor, kind::tf32: D f32, A/B tf32, both K-major, N=64, M=128.
-constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
+// Instruction descriptor, kind::tf32: D f32, A/B tf32, both K-major, M=128.
+constexpr uint32_t idesc_tf32(uint32_t n)
+{
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((n >> 3) << 17) | ((128u >> 4) << 24);
+}
+constexpr uint32_t kIdescN128 = idesc_tf32(128);
+constexpr uint32_t kIdescN64 = idesc_tf32(64);
 
 // Nearest TF32 value (ties away from zero) as an FP32 with the 13 low
 // mantissa bits cleared, so that x - to_tf32(x) is the exact remainder.
 __device__ __forceinline__ float to_tf32(float x)
 {
     return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
-}
-
-// Byte offset of tile coordinate j in the staging buffer: 16-byte chunks
-// (two amplitudes) XOR-swizzled by higher chunk bits, so that both the row
-// scatter and the linear read-out spread over the banks.
-__device__ __forceinline__ uint32_t stage_off(uint32_t j)
-{
-    const uint32_t c = j >> 1;
-    const uint32_t pc = c ^ ((c >> 3) & 7u) ^ ((c >> 6) & 7u);
-    return (pc << 4) | ((j & 1u) << 3);
 }
 
 __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
@@ -105,13 +129,15 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
     return ok != 0;
 }
 
-__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t acc)
+// D (TMEM) (+)= A (TMEM) * B (SMEM descriptor)^T
+__device__ __forceinline__ void mma_tf32_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t b, uint32_t idesc,
+                                            uint32_t acc)
 {
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
         "setp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
-        "l"(a), "l"(b), "r"(kIdesc), "r"(acc));
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "r"(a_tmem), "l"(b), "r"(idesc), "r"(acc));
 }
 
 __device__ __forceinline__ void mma_commit(uint32_t bar)
@@ -134,25 +160,116 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t* v)
         : "r"(taddr));
 }
 
-__global__ void __launch_bounds__(kTcThreads, 2)
-k_fused_tc(float2* __restrict__ a, uint64_t ntiles, IndexMap tilemap, TcOffsets offs,
-           const uint4* __restrict__ bimage, int* __restrict__ err)
+__device__ __forceinline__ void tmem_st32(uint32_t taddr, const float* v)
+{
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], "
+        "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,"
+        "%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(taddr),
+        "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7]), "f"(v[8]),
+        "f"(v[9]), "f"(v[10]), "f"(v[11]), "f"(v[12]), "f"(v[13]), "f"(v[14]), "f"(v[15]), "f"(v[16]),
+        "f"(v[17]), "f"(v[18]), "f"(v[19]), "f"(v[20]), "f"(v[21]), "f"(v[22]), "f"(v[23]), "f"(v[24]),
+        "f"(v[25]), "f"(v[26]), "f"(v[27]), "f"(v[28]), "f"(v[29]), "f"(v[30]), "f"(v[31])
+        : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_tx(uint32_t bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void bulk_load(uint32_t dst_smem, const void* src, uint32_t bytes, uint32_t bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     dst_smem),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void bulk_store(void* dst, uint32_t src_smem, uint32_t bytes)
+{
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(src_smem), "r"(bytes)
+                 : "memory");
+}
+
+// Bounded wait on an mbarrier phase; gives up (returns false) when the CTA's
+// abort flag is set or after kSpinLimit polls, setting the flag.
+__device__ __forceinline__ bool wait_phase(uint32_t bar, uint32_t parity, volatile int* abort_flag)
+{
+    uint32_t spins = 0;
+    while (!mbar_try_wait(bar, parity)) {
+        if (*abort_flag) return false;
+        if (++spins > kSpinLimit) {
+            *abort_flag = 1;
+            return false;
+        }
+    }
+    return true;
+}
+
+// Named barrier over one consumer group (ids 1 and 2, 128 threads).
+__device__ __forceinline__ void group_sync(uint32_t id)
+{
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "n"(kGroupThreads) : "memory");
+}
+
+// OR of `fail` over one consumer group: every thread of the group takes the
+// same branch, so none can be left waiting at a barrier.
+__device__ __forceinline__ bool group_any(bool fail, uint32_t id)
+{
+    uint32_t any;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.or.pred q, %2, %3, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(any)
+        : "r"((uint32_t)fail), "r"(id), "n"(kGroupThreads)
+        : "memory");
+    return any != 0;
+}
+
+__device__ __forceinline__ void split_tf32(float x, float& hi, float& lo)
+{
+    hi = to_tf32(x);
+    lo = to_tf32((x - hi) * kLoScale);
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1)
+k_fused_tc(float2* __restrict__ a, uint64_t ntiles, const __grid_constant__ IndexMap tilemap,
+           const __grid_constant__ TcOffsets offs, const uint4* __restrict__ bimage, int* __restrict__ err)
 {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     const uint32_t sbase = smem_addr(smem);
-    const uint32_t bar = sbase + kOffBar;
-    uint32_t* tmem_slot = (uint32_t*)(smem + kOffBar + 8);
     const int tid = threadIdx.x;
-    const int warp = tid >> 5;
+    const int warp = tid >> 5, lane = tid & 31;
+    const uint32_t nst = offs.nstages, sbytes = offs.stage_bytes, nblocks = offs.nblocks;
+    const uint32_t raw0 = kOffB + nblocks * kBImage;      // stage 0
+    uint32_t* tmem_slot = (uint32_t*)(smem + kOffSlot);
+    volatile int* abort_flag = (volatile int*)(smem + kOffAbort);
+    uint64_t* run_off = (uint64_t*)(smem + kOffRunOff);
 
-    // B image (hi and lo, 32 KB) into shared memory.
     {
-        uint4* dst = (uint4*)(smem + kOffBhi);
-        for (int i = tid; i < (int)(4 * kAtomB / 16); i += kTcThreads) dst[i] = bimage[i];
+        uint4* dst = (uint4*)(smem + kOffB);
+        const uint32_t n16 = nblocks * kBImage / 16;
+        for (uint32_t i = tid; i < n16; i += kTcThreads) dst[i] = bimage[i];
+        if (tid < 32) run_off[tid] = offs.run_off[tid];
     }
     if (tid == 0) {
-        mbar_init(bar, 1);
+        for (uint32_t s = 0; s < nst; ++s) {
+            mbar_init(sbase + kOffFull + 8 * s, 1);
+            mbar_init(sbase + kOffEmpty + 8 * s, 1);
+            mbar_init(sbase + kOffOut + 8 * s, kGroupThreads);
+        }
+        mbar_init(sbase + kOffMma, 1);
+        mbar_init(sbase + kOffMma + 8, 1);
+        *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -166,150 +283,187 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, IndexMap tilemap, TcOffsets 
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
+    const uint64_t my_tiles = ntiles > blockIdx.x ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    const uint32_t pb = offs.piece_bits, np = offs.npieces, pad = offs.pad_shift, rb = offs.run_bits;
+    const uint32_t piece_bytes = 8u << pb;
+    const uint64_t run_mask = (uint64_t(1) << rb) - 1u;
 
-    // Tile coordinate j (12 bits) <-> tile positions tpos[b]; bit 0 of j is
-    // always position 0.  Thread tid moves the amplitude pairs
-    // j = 2*(tid + 128*k) + {0,1}, k = 0..15: consecutive threads touch
-    // consecutive 16-byte words of global memory.  (row t, gate g) of j is the
-    // OR of the contributions of its set bits.
-    uint64_t a_tid = 0;
-    uint32_t t_tid = 0, g_tid = 0;
-#pragma unroll
-    for (int b = 1; b < 8; ++b)
-        if ((tid >> (b - 1)) & 1) {
-            a_tid |= uint64_t(1) << offs.tpos[b];
-            t_tid |= offs.rowmask[b];
-            g_tid |= offs.gatemask[b];
-        }
-    const uint32_t t_e = offs.rowmask[0], g_e = offs.gatemask[0];
-    // tile coordinate of (row tid, g = 0), for staging the results
-    uint32_t jrow = 0;
-#pragma unroll
-    for (int r = 0; r < 7; ++r)
-        if ((tid >> r) & 1) jrow |= offs.row_tbit[r];
-    uint8_t* const stage = smem + kOffAlo;   // A_lo is free once the MMAs are done
-
-    float4 x[16];
-    uint64_t tile = blockIdx.x;
-    uint64_t base = tile < ntiles ? expand_index(tile, tilemap) : 0;
-    if (tile < ntiles) {
-#pragma unroll
-        for (int k = 0; k < 16; ++k) x[k] = *reinterpret_cast<const float4*>(a + (base | a_tid | offs.koff[k]));
-    }
-    uint32_t phase = 0;
-    bool failed = false;
-    for (; tile < ntiles; tile += gridDim.x) {
-        // operand A: hi and lo' halves, scattered into the swizzled K-major rows
-#pragma unroll
-        for (int k = 0; k < 16; ++k) {
-            const uint32_t tk = t_tid | offs.krow[k], gk = g_tid | offs.kgate[k];
-#pragma unroll
-            for (int e = 0; e < 2; ++e) {
-                const uint32_t t = e ? (tk | t_e) : tk;
-                const uint32_t g = e ? (gk | g_e) : gk;
-                const float vx = e ? x[k].z : x[k].x, vy = e ? x[k].w : x[k].y;
-                const float hx = to_tf32(vx), hy = to_tf32(vy);
-                const float2 h = make_float2(hx, hy);
-                const float2 l = make_float2(to_tf32((vx - hx) * kLoScale), to_tf32((vy - hy) * kLoScale));
-                const uint32_t off = (g >> 4) * kAtomA + (t >> 3) * 1024u + (t & 7u) * 128u +
-                                     ((((g & 15u) >> 1) ^ (t & 7u)) << 4) + (g & 1u) * 8u;
-                *(float2*)(smem + kOffAhi + off) = h;
-                *(float2*)(smem + kOffAlo + off) = l;
+    if (warp == kLoaderWarp) {
+        // ---------------------------------------------------------- loader
+        uint32_t s = 0, u = 0;
+        uint64_t issued = 0;
+        for (uint64_t i = 0; i < my_tiles; ++i) {
+            // use u of stage s waits until the store of use u-1 has read it
+            if (u > 0 && !wait_phase(sbase + kOffEmpty + 8 * s, (u - 1) & 1u, abort_flag)) break;
+            const uint64_t base = expand_index(blockIdx.x + i * gridDim.x, tilemap);
+            const uint32_t full = sbase + kOffFull + 8 * s;
+            if (lane == 0) mbar_arrive_tx(full, kTileBytes);
+            __syncwarp();
+            const uint32_t st = sbase + raw0 + s * sbytes;
+            for (uint32_t j = (uint32_t)lane; j < np; j += 32) {
+                const uint32_t x0 = j << pb;
+                bulk_load(st + 8u * x0 + ((x0 >> pad) << 4), a + ((base | run_off[x0 >> rb]) + (x0 & run_mask)),
+                          piece_bytes, full);
+            }
+            issued = i + 1;
+            if (++s == nst) {
+                s = 0;
+                ++u;
             }
         }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (tid == 0) {
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            // pass 0: D_main = A_hi B_hi; passes 1-2: D_corr = A_lo' B_hi + A_hi B_lo'
-            // (lo' = 2^11 lo), kept apart so the small terms never meet the large
-            // ones inside one accumulation.
-            const uint32_t apass[3] = {sbase + kOffAhi, sbase + kOffAlo, sbase + kOffAhi};
-            const uint32_t bpass[3] = {sbase + kOffBhi, sbase + kOffBhi, sbase + kOffBlo};
-            const uint32_t dcol[3] = {0u, 64u, 64u};
+        // every load issued has landed before the CTA can exit (the
+        // consumers waited for all of them unless the CTA gave up)
+        const uint64_t from = issued > nst ? issued - nst : 0;
+        for (uint64_t i = from; i < issued; ++i) {
+            uint32_t spins = 0;
+            while (!mbar_try_wait(sbase + kOffFull + 8 * (uint32_t)(i % nst), (uint32_t)((i / nst) & 1)) &&
+                   ++spins <= kSpinLimit) {
+            }
+        }
+    } else if (warp == kStorerWarp) {
+        // ---------------------------------------------------------- storer
+        uint32_t s = 0, u = 0, prev = 0xFFFFFFFFu;
+        for (uint64_t i = 0; i < my_tiles; ++i) {
+            if (!wait_phase(sbase + kOffOut + 8 * s, u & 1u, abort_flag)) break;
+            const uint64_t base = expand_index(blockIdx.x + i * gridDim.x, tilemap);
+            const uint32_t st = sbase + raw0 + s * sbytes;
+            for (uint32_t j = (uint32_t)lane; j < np; j += 32) {
+                const uint32_t x0 = j << pb;
+                bulk_store(a + ((base | run_off[x0 >> rb]) + (x0 & run_mask)), st + 8u * x0 + ((x0 >> pad) << 4),
+                           piece_bytes);
+            }
+            asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+            // all but this tile's copies have read their stages
+            asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+            __syncwarp();
+            if (prev != 0xFFFFFFFFu && lane == 0) mbar_arrive(sbase + kOffEmpty + 8 * prev);
+            prev = s;
+            if (++s == nst) {
+                s = 0;
+                ++u;
+            }
+        }
+        asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+        __syncwarp();
+        if (prev != 0xFFFFFFFFu && lane == 0) mbar_arrive(sbase + kOffEmpty + 8 * prev);
+        asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+    } else {
+        // ------------------------------------------------ consumer groups
+        const uint32_t g = (uint32_t)warp >> 2, q = (uint32_t)warp & 3u;
+        const uint32_t t = 32u * q + (uint32_t)lane;       // row = TMEM lane
+        const uint32_t gbar = 1u + g;
+        const uint32_t tm = tmem + 256u * g;                // the group's columns
+        const uint32_t tl = tm + ((32u * q) << 16);         // this warp's lanes
+        const uint32_t mbar = sbase + kOffMma + 8u * g;
+        uint32_t rowb0 = 0, rowb1 = 0;
 #pragma unroll
-            for (int pss = 0; pss < 3; ++pss)
+        for (int r = 0; r < 7; ++r)
+            if ((t >> r) & 1u) {
+                rowb0 += offs.blk[0].rowoff[r];
+                rowb1 += offs.blk[1].rowoff[r];
+            }
+        uint32_t s = g, u = 0, mph = 0;     // tile i lives in stage i % nst
+        for (uint64_t i = g; i < my_tiles; i += 2) {
+            if (group_any(!wait_phase(sbase + kOffFull + 8 * s, u & 1u, abort_flag), gbar)) break;
+            uint8_t* raw = smem + raw0 + s * sbytes;
+            bool stop = false;
 #pragma unroll
-                for (int ks = 0; ks < 8; ++ks) {
-                    const uint32_t ka = (uint32_t)(ks >> 2) * kAtomA + (uint32_t)(ks & 3) * 32u;
-                    const uint32_t kb = (uint32_t)(ks >> 2) * kAtomB + (uint32_t)(ks & 3) * 32u;
-                    const uint32_t acc = (pss == 2 || ks != 0) ? 1u : 0u;
-                    mma_tf32(tmem + dcol[pss], desc_sw128(apass[pss] + ka), desc_sw128(bpass[pss] + kb), acc);
+            for (int b = 0; b < 2; ++b) {
+                if ((uint32_t)b >= nblocks) break;
+                const TcBlockGeom& G = offs.blk[b];
+                const uint32_t rowb = b ? rowb1 : rowb0;
+                if (b > 0) group_sync(gbar);    // the previous block's results are all staged
+                // row t -> hi/lo operands, columns 2g+c, in TMEM
+#pragma unroll
+                for (int hh = 0; hh < 2; ++hh) {
+                    float hi[32], lo[32];
+                    if (G.vec2) {
+#pragma unroll
+                        for (int m = 0; m < 8; ++m) {
+                            const float4 v = *(const float4*)(raw + rowb + G.gateoff[16 * hh + 2 * m]);
+                            split_tf32(v.x, hi[4 * m], lo[4 * m]);
+                            split_tf32(v.y, hi[4 * m + 1], lo[4 * m + 1]);
+                            split_tf32(v.z, hi[4 * m + 2], lo[4 * m + 2]);
+                            split_tf32(v.w, hi[4 * m + 3], lo[4 * m + 3]);
+                        }
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) {
+                            const float2 v = *(const float2*)(raw + rowb + G.gateoff[16 * hh + j]);
+                            split_tf32(v.x, hi[2 * j], lo[2 * j]);
+                            split_tf32(v.y, hi[2 * j + 1], lo[2 * j + 1]);
+                        }
+                    }
+                    tmem_st32(tl + 32u * hh, hi);
+                    tmem_st32(tl + 64u + 32u * hh, lo);
                 }
-            mma_commit(bar);
-        }
-        // prefetch the next tile while the tensor cores work
-        const uint64_t cur = base;
-        const uint64_t next = tile + gridDim.x;
-        if (next < ntiles) {
-            base = expand_index(next, tilemap);
+                asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                group_sync(gbar);
+                if (t == 0) {
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t bb = sbase + kOffB + (uint32_t)b * kBImage;
+                    // [D_main | D_corr] = A_hi [B_hi; B_lo']^T, then D_corr += A_lo' B_hi^T
 #pragma unroll
-            for (int k = 0; k < 16; ++k)
-                x[k] = *reinterpret_cast<const float4*>(a + (base | a_tid | offs.koff[k]));
-        }
-        uint32_t spins = 0;
-        bool ok = true;
-        while (!mbar_try_wait(bar, phase)) {
-            if (++spins > kSpinLimit) {
-                ok = false;
-                break;
+                    for (int ks = 0; ks < 8; ++ks)
+                        mma_tf32_ts(tm + 128u, tm + 8u * ks,
+                                    desc_sw128(bb + (uint32_t)(ks >> 2) * kBAtom + (uint32_t)(ks & 3) * 32u),
+                                    kIdescN128, ks > 0 ? 1u : 0u);
+#pragma unroll
+                    for (int ks = 0; ks < 8; ++ks)
+                        mma_tf32_ts(tm + 192u, tm + 64u + 8u * ks,
+                                    desc_sw128(bb + (uint32_t)(ks >> 2) * kBAtom + (uint32_t)(ks & 3) * 32u),
+                                    kIdescN64, 1u);
+                    mma_commit(mbar);
+                }
+                if (group_any(!wait_phase(mbar, mph & 1u, abort_flag), gbar)) {
+                    stop = true;
+                    break;
+                }
+                ++mph;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                // D = D_main + 2^-11 D_corr for row t, back into the stage
+#pragma unroll
+                for (int hh = 0; hh < 2; ++hh) {
+                    uint32_t dm[32], dc[32];
+                    tmem_ld32(tl + 128u + 32u * hh, dm);
+                    tmem_ld32(tl + 192u + 32u * hh, dc);
+                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                    float o[32];
+#pragma unroll
+                    for (int j = 0; j < 32; ++j)
+                        o[j] = __fmaf_rn(__uint_as_float(dc[j]), kLoUnscale, __uint_as_float(dm[j]));
+                    if (G.vec2) {
+#pragma unroll
+                        for (int m = 0; m < 8; ++m)
+                            *(float4*)(raw + rowb + G.gateoff[16 * hh + 2 * m]) =
+                                make_float4(o[4 * m], o[4 * m + 1], o[4 * m + 2], o[4 * m + 3]);
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 16; ++j)
+                            *(float2*)(raw + rowb + G.gateoff[16 * hh + j]) = make_float2(o[2 * j], o[2 * j + 1]);
+                    }
+                }
+                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             }
-        }
-        // one decision for the whole CTA, so every thread leaves together
-        if (__syncthreads_or(!ok)) {
-            if (tid == 0) atomicExch(err, 1);
-            failed = true;
-            break;
-        }
-        phase ^= 1u;
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        // row tid of D = D_main + 2^-11 D_corr, staged in tile-coordinate order
-        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
-#pragma unroll
-        for (int half = 0; half < 2; ++half) {
-            uint32_t dm[32], dc[32];
-            tmem_ld32(taddr + 32u * half, dm);
-            tmem_ld32(taddr + 64u + 32u * half, dc);
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                const int g = 16 * half + j;
-                const float re = __fmaf_rn(__uint_as_float(dc[2 * j]), kLoUnscale, __uint_as_float(dm[2 * j]));
-                const float im =
-                    __fmaf_rn(__uint_as_float(dc[2 * j + 1]), kLoUnscale, __uint_as_float(dm[2 * j + 1]));
-                const uint32_t jc = jrow | offs.jgate[g];
-                *(float2*)(stage + stage_off(jc)) = make_float2(re, im);
+            if (stop) break;
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_arrive(sbase + kOffOut + 8 * s);
+            s += 2;
+            if (s >= nst) {
+                s -= nst;
+                ++u;
             }
-        }
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-        __syncthreads();
-#pragma unroll
-        for (int k = 0; k < 16; ++k) {
-            const uint32_t jc = 2u * (uint32_t)tid + 256u * (uint32_t)k;
-            *reinterpret_cast<float4*>(a + (cur | a_tid | offs.koff[k])) =
-                *reinterpret_cast<const float4*>(stage + stage_off(jc));
-        }
-        __syncthreads();   // staging read out before the next split overwrites it
-    }
-    if (failed) {
-        // give the outstanding MMAs a second bounded chance to finish before
-        // the accumulator is released
-        uint32_t spins = 0;
-        while (!mbar_try_wait(bar, phase) && ++spins <= kSpinLimit) {
         }
     }
     __syncthreads();
+    if (*abort_flag && tid == 0) atomicExch(err, 1);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (warp == 0)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
 }
 
-}  // namespace
-
-uint32_t fused_tc_smem_bytes() { return kSmemBytes; }
-
-namespace {
-// Round to TF32 the way cvt.rna.tf32.f32 does: nearest, ties away from zero.
+// Round to TF32 the way to_tf32 does: nearest, ties away from zero.
 float host_tf32(float x)
 {
     uint32_t u;
@@ -319,11 +473,140 @@ float host_tf32(float x)
     std::memcpy(&r, &u, 4);
     return r;
 }
+
+uint32_t staged_offset(uint32_t x, uint32_t pad)
+{
+    return 8u * x + ((pad < 31 ? (x >> pad) : 0u) << 4);
+}
+
+// Shared-memory wavefronts of one warp instruction over its rows (lanes =
+// rows 0..31 with row bit r at tile coordinate order[r], all at the same
+// gate), `width` bytes per lane.  Shared memory serves 8-byte accesses in
+// half-warp phases and 16-byte accesses in quarter-warp phases; a phase takes
+// as many wavefronts as the most distinct words any one bank holds.
+int warp_wavefronts(const uint32_t* order, uint32_t pad, int width)
+{
+    const uint32_t lanes_per_phase = width == 16 ? 8 : 16;
+    const uint32_t wpl = (uint32_t)width / 4;   // words per lane
+    int total = 0;
+    for (uint32_t ph = 0; ph < 32 / lanes_per_phase; ++ph) {
+        uint32_t words[64];
+        uint32_t nw = 0;
+        for (uint32_t l = ph * lanes_per_phase; l < (ph + 1) * lanes_per_phase; ++l) {
+            uint32_t x = 0;
+            for (int r = 0; r < 5; ++r)
+                if ((l >> r) & 1u) x |= order[r];
+            const uint32_t word0 = staged_offset(x, pad) / 4;
+            for (uint32_t w = 0; w < wpl; ++w) words[nw++] = word0 + w;
+        }
+        std::sort(words, words + nw);
+        int per_bank[32] = {0};
+        int m = 0;
+        for (uint32_t i = 0; i < nw; ++i)
+            if (i == 0 || words[i] != words[i - 1]) m = std::max(m, ++per_bank[words[i] % 32]);
+        total += m;
+    }
+    return total;
+}
+
+// The order of a block's 7 row bits (which tile coordinates the low lane
+// bits select) with the fewest wavefronts under padding `pad`.  Rows are
+// independent in the GEMM, so any order is correct; only the row bits that
+// vary inside one phase (3 for 16-byte, 4 for 8-byte accesses) matter.
+int best_row_order(const TcBlockGeom& G, uint32_t pad, uint32_t* order)
+{
+    const bool v2 = G.vec2 != 0;
+    const int width = v2 ? 16 : 8, k = v2 ? 3 : 4;
+    int best = -1;
+    for (uint32_t mask = 0; mask < 128; ++mask) {
+        if (__builtin_popcount(mask) != k) continue;
+        uint32_t cand[7];
+        int c = 0;
+        for (int r = 0; r < 7; ++r)
+            if ((mask >> r) & 1u) cand[c++] = G.jrow_bit[r];
+        for (int r = 0; r < 7; ++r)
+            if (!((mask >> r) & 1u)) cand[c++] = G.jrow_bit[r];
+        const int wf = warp_wavefronts(cand, pad, width);
+        if (best < 0 || wf < best) {
+            best = wf;
+            std::memcpy(order, cand, sizeof(cand));
+            if (best == width / 4) break;     // 32 lanes x width bytes in 128-byte wavefronts
+        }
+    }
+    return best;
+}
+
 }  // namespace
+
+void tc_choose_padding(TcOffsets& o)
+{
+    // The choice depends only on the tile geometry, which repeats from run to
+    // run of a plan: remember it.
+    struct Choice {
+        uint32_t pad;
+        uint32_t order[2][7];
+    };
+    static std::mutex mu;
+    static std::unordered_map<std::string, Choice> memo;
+    std::string key((const char*)&o.nblocks, sizeof(o.nblocks));
+    key.append((const char*)&o.run_bits, sizeof(o.run_bits));
+    for (uint32_t b = 0; b < o.nblocks; ++b) {
+        key.append((const char*)o.blk[b].jrow_bit, sizeof(o.blk[b].jrow_bit));
+        key.append((const char*)o.blk[b].jgate, sizeof(o.blk[b].jgate));
+    }
+    Choice ch{};
+    bool found = false;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        auto it = memo.find(key);
+        if (it != memo.end()) {
+            ch = it->second;
+            found = true;
+        }
+    }
+    if (!found) {
+        // candidates: unpadded, then 16 B every 2^pad amplitudes (fewest
+        // pieces first); per block the row order that suits the padding best
+        const uint32_t cands[] = {31, 11, 10, 9, 8, 7, 6, 5};
+        long best = -1, ideal = 0;
+        for (uint32_t b = 0; b < o.nblocks; ++b) ideal += o.blk[b].vec2 ? 16 * 4 : 32 * 2;
+        for (uint32_t pad : cands) {
+            long cost = 0;
+            uint32_t order[2][7] = {};
+            for (uint32_t b = 0; b < o.nblocks; ++b)
+                cost += (o.blk[b].vec2 ? 16 : 32) * best_row_order(o.blk[b], pad, order[b]);
+            if (best < 0 || cost < best) {
+                best = cost;
+                ch.pad = pad;
+                std::memcpy(ch.order, order, sizeof(order));
+                if (best == ideal) break;
+            }
+        }
+        std::lock_guard<std::mutex> lock(mu);
+        if (memo.size() > 4096) memo.clear();
+        memo.emplace(key, ch);
+    }
+    const uint32_t best_pad = ch.pad;
+    const auto& best_order = ch.order;
+    o.pad_shift = best_pad;
+    o.stage_bytes = kTileBytes + (best_pad < 31 ? 16u * (4096u >> best_pad) : 0u);
+    o.piece_bits = std::min(best_pad, o.run_bits);
+    o.npieces = 4096u >> o.piece_bits;
+    for (uint32_t b = 0; b < o.nblocks; ++b) {
+        TcBlockGeom& G = o.blk[b];
+        for (int r = 0; r < 7; ++r) {
+            G.jrow_bit[r] = best_order[b][r];
+            G.rowoff[r] = staged_offset(G.jrow_bit[r], best_pad);
+        }
+        for (int g = 0; g < 32; ++g) G.gateoff[g] = staged_offset(G.jgate[g], best_pad);
+    }
+}
 
 void build_tc_image(const double* m, float* image)
 {
-    // R[n][k]: n = 2g'+c' output component, k = 2g+c input component
+    // R[n][k]: n = 2g'+c' output component, k = 2g+c input component.  Rows
+    // n of B_hi and 64+n of B_lo' (= 2^11 lo), K-major, SWIZZLE_128B, one
+    // 16 KB atom per 32 values of k.
     for (int gp = 0; gp < 32; ++gp)
         for (int g = 0; g < 32; ++g) {
             const double re = m[2 * (gp * 32 + g)], im = m[2 * (gp * 32 + g) + 1];
@@ -335,29 +618,48 @@ void build_tc_image(const double* m, float* image)
                     const float hi = host_tf32(v);
                     const float lo = host_tf32((v - hi) * 2048.0f);
                     const int atom = k >> 5, kc = (k & 31) >> 2, e = k & 3;
-                    const size_t off = (size_t)atom * kAtomB + (size_t)(n >> 3) * 1024 + (size_t)(n & 7) * 128 +
-                                       (size_t)((kc ^ (n & 7)) << 4) + (size_t)e * 4;
-                    image[off / 4] = hi;
-                    image[(2 * kAtomB + off) / 4] = lo;
+                    for (int half = 0; half < 2; ++half) {
+                        const int row = n + 64 * half;
+                        const size_t off = (size_t)atom * kBAtom + (size_t)(row >> 3) * 1024 +
+                                           (size_t)(row & 7) * 128 + (size_t)((kc ^ (row & 7)) << 4) + (size_t)e * 4;
+                        image[off / 4] = half ? lo : hi;
+                    }
                 }
         }
 }
 
-cudaError_t launch_fused_tc(float2* amps, uint64_t ntiles, const IndexMap& tilemap, const TcOffsets& offs,
+cudaError_t launch_fused_tc(float2* amps, uint64_t ntiles, const IndexMap& tilemap, const TcOffsets& offs_in,
                             const void* d_bimage, int* d_err, int sm_count, cudaStream_t st)
 {
-    static bool configured = false;
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(k_fused_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)kSmemBytes);
-        if (e != cudaSuccess) return e;
-        configured = true;
+    static std::mutex mu;
+    static int optin[64] = {0};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        if (!optin[dev]) {
+            int v = 0;
+            e = cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+            if (e != cudaSuccess) return e;
+            e = cudaFuncSetAttribute(k_fused_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+            if (e != cudaSuccess) return e;
+            optin[dev] = v;
+        }
     }
-    uint64_t grid = (uint64_t)sm_count * 2;
+    TcOffsets offs = offs_in;
+    const uint32_t fixed = kAlignSlack + kOffB + offs.nblocks * kBImage;
+    if (offs.nblocks < 1 || offs.nblocks > 2 || offs.stage_bytes < kTileBytes ||
+        (uint32_t)optin[dev] < fixed + 3 * offs.stage_bytes)
+        return cudaErrorInvalidConfiguration;
+    offs.nstages = std::min(kMaxStages, ((uint32_t)optin[dev] - fixed) / offs.stage_bytes);
+    const uint32_t smem = fixed + offs.nstages * offs.stage_bytes;
+    uint64_t grid = (uint64_t)sm_count;
     if (grid > ntiles) grid = ntiles;
     if (grid == 0) return cudaSuccess;
-    k_fused_tc<<<(unsigned)grid, kTcThreads, kSmemBytes, st>>>(amps, ntiles, tilemap, offs,
-                                                               (const uint4*)d_bimage, d_err);
+    k_fused_tc<<<(unsigned)grid, kTcThreads, smem, st>>>(amps, ntiles, tilemap, offs, (const uint4*)d_bimage,
+                                                         d_err);
     return cudaGetLastError();
 }
 

@@ -141,21 +141,60 @@ std::vector<cd> embed_matrix(const std::vector<cd>& mat, const std::vector<int>&
 
 std::vector<cd> block_matrix(const FusedBlock& b, const std::vector<SeqGate>& gates)
 {
-    const int dim = 1 << b.qubits.size();
-    std::vector<cd> acc((size_t)dim * dim, cd(0.0, 0.0));
-    for (int i = 0; i < dim; ++i) acc[(size_t)i * dim + i] = 1.0;
-    std::vector<cd> tmp((size_t)dim * dim);
+    // acc = G_last ... G_first, each gate applied to the rows of acc as a
+    // k-qubit operator on its bits (32 * 2^k multiply-adds per column, not a
+    // dense product with the embedded matrix).
+    const int m = (int)b.qubits.size();
+    const int dim = 1 << m;
+    std::vector<double> acc(2 * (size_t)dim * dim, 0.0);   // row-major (re, im)
+    for (int i = 0; i < dim; ++i) acc[2 * ((size_t)i * dim + i)] = 1.0;
+    double vin[2 * 32], vout[2 * 32];
+    int rowof[32];
     for (int gi : b.gates) {
-        const auto e = embed_matrix(gates[gi].mat, gates[gi].bits, b.qubits);
-        for (int r = 0; r < dim; ++r)
+        const auto& g = gates[gi];
+        const int k = (int)g.bits.size();
+        const int gdim = 1 << k;
+        int bpos[5], gmask = 0;
+        for (int j = 0; j < k; ++j) {
+            auto it = std::find(b.qubits.begin(), b.qubits.end(), g.bits[j]);
+            bpos[j] = m - 1 - (int)(it - b.qubits.begin());
+            gmask |= 1 << bpos[j];
+        }
+        for (int gs = 0; gs < gdim; ++gs) {
+            int r = 0;
+            for (int j = 0; j < k; ++j) r |= ((gs >> (k - 1 - j)) & 1) << bpos[j];
+            rowof[gs] = r;
+        }
+        const double* gm = reinterpret_cast<const double*>(g.mat.data());
+        for (int base = 0; base < dim; ++base) {
+            if (base & gmask) continue;
             for (int c = 0; c < dim; ++c) {
-                cd s(0.0, 0.0);
-                for (int q = 0; q < dim; ++q) s += e[(size_t)r * dim + q] * acc[(size_t)q * dim + c];
-                tmp[(size_t)r * dim + c] = s;
+                for (int gs = 0; gs < gdim; ++gs) {
+                    const double* a = &acc[2 * ((size_t)(base | rowof[gs]) * dim + c)];
+                    vin[2 * gs] = a[0];
+                    vin[2 * gs + 1] = a[1];
+                }
+                for (int go = 0; go < gdim; ++go) {
+                    double re = 0.0, im = 0.0;
+                    const double* row = gm + 2 * (size_t)go * gdim;
+                    for (int gs = 0; gs < gdim; ++gs) {
+                        re += row[2 * gs] * vin[2 * gs] - row[2 * gs + 1] * vin[2 * gs + 1];
+                        im += row[2 * gs] * vin[2 * gs + 1] + row[2 * gs + 1] * vin[2 * gs];
+                    }
+                    vout[2 * go] = re;
+                    vout[2 * go + 1] = im;
+                }
+                for (int go = 0; go < gdim; ++go) {
+                    double* a = &acc[2 * ((size_t)(base | rowof[go]) * dim + c)];
+                    a[0] = vout[2 * go];
+                    a[1] = vout[2 * go + 1];
+                }
             }
-        acc.swap(tmp);
+        }
     }
-    return acc;
+    std::vector<cd> out((size_t)dim * dim);
+    for (size_t e = 0; e < out.size(); ++e) out[e] = cd(acc[2 * e], acc[2 * e + 1]);
+    return out;
 }
 
 namespace {

@@ -29,22 +29,44 @@ cudaError_t launch_dense(void* amps, int prec, uint64_t total, const IndexMap& m
                          const DenseOffsets& offs, int tb, const void* dmat, cudaStream_t st);
 
 // ---- fused_tc.cu: 5-qubit fused blocks on the tensor cores (complex64)
-// Geometry of a tile of 2^12 amplitudes (5 gate + 7 row positions).  Tile
-// coordinate bit b sits at position tpos[b]; it is row bit rowmask[b] or
-// gate bit gatemask[b] (one of the two is zero).
-struct TcOffsets {
-    uint8_t tpos[12];
-    uint32_t rowmask[12];
-    uint32_t gatemask[12];
-    uint32_t row_tbit[7];    // tile-coordinate mask of row bit r
+// Geometry of one tensor-core pass over tiles of 2^12 amplitudes.  Tile
+// coordinate x enumerates the tile's 12 positions in ascending order; its low
+// run_bits bits are positions 0..run_bits-1, so a tile is nruns contiguous
+// runs of 2^run_bits amplitudes at run_off[r] from the tile base.  A pass
+// applies nblocks (1 or 2) 5-qubit blocks in turn to each staged tile; block
+// b's 5 gate positions and 7 row positions all lie in the tile.
+//
+// In shared memory a staged tile keeps coordinate x at byte
+// 8x + 16 (x >> pad_shift) (pad_shift 31: unpadded).  The padding moves rows
+// that are a multiple of 32 amplitudes apart onto different banks; it is
+// chosen per pass by tc_choose_padding.  Tiles are copied in npieces pieces
+// of 2^piece_bits amplitudes (contiguous in both memories).
+struct TcBlockGeom {
+    uint32_t jrow_bit[7];    // tile coordinate of row bit r (any order: rows are independent)
+    uint32_t vec2;           // 1 if gate bit 0 is tile bit 0 (gate pairs adjacent)
     uint32_t jgate[32];      // tile coordinate of gate state g
-    uint64_t koff[16];       // address offset of tile bits 8..11 = k
-    uint32_t krow[16];       // row bits of tile bits 8..11 = k
-    uint32_t kgate[16];      // gate bits of tile bits 8..11 = k
+    uint32_t rowoff[7];      // staged byte offset of row bit r
+    uint32_t pad0_;
+    uint32_t gateoff[32];    // staged byte offset of gate state g
 };
-uint32_t fused_tc_smem_bytes();
-// d_bimage: the block's 32 KB hi/lo image of the real 64x64 embedding in the
-// kernel's swizzled layout; d_err: set to 1 if a bounded wait expired.
+struct TcOffsets {
+    uint32_t run_bits;
+    uint32_t nruns;
+    uint32_t nblocks;
+    uint32_t pad_shift;
+    uint32_t piece_bits;
+    uint32_t npieces;
+    uint32_t nstages;        // filled in by launch_fused_tc
+    uint32_t stage_bytes;
+    uint64_t run_off[32];
+    TcBlockGeom blk[2];
+};
+// Picks pad_shift (and piece_bits, npieces, stage_bytes, the blocks' staged
+// offsets) that minimise shared-memory bank conflicts of the per-row reads.
+void tc_choose_padding(TcOffsets& offs);
+// d_bimage: nblocks consecutive 32 KB hi/lo images of the blocks' real 64x64
+// embeddings in the kernel's swizzled layout; d_err: set to 1 if a bounded
+// wait expired.
 cudaError_t launch_fused_tc(float2* amps, uint64_t ntiles, const IndexMap& tilemap, const TcOffsets& offs,
                             const void* d_bimage, int* d_err, int sm_count, cudaStream_t st);
 // Host: the 32 KB image for the 32x32 complex matrix m (row-major (re, im)).
@@ -79,7 +101,9 @@ cudaError_t launch_chunk_sums(const void* amps, int prec, uint64_t units, uint64
 cudaError_t launch_chunk_sums_dense(const void* amps, int prec, uint64_t total, uint64_t chunk, double* out,
                                     cudaStream_t st);
 // Deterministic per-segment reduction: out[s] = sum of in[s*len .. (s+1)*len).
-cudaError_t launch_segment_sums(const double* in, uint64_t nseg, uint64_t len, double* out,
+// tmp: segment_sums_tmp_doubles(nseg, len) doubles (none for short segments).
+uint64_t segment_sums_tmp_doubles(uint64_t nseg, uint64_t len);
+cudaError_t launch_segment_sums(const double* in, uint64_t nseg, uint64_t len, double* out, double* tmp,
                                 cudaStream_t st);
 // In-place exclusive prefix sum of n doubles; *total_out (device) = the sum.
 // `tmp` must hold scan_tmp_doubles(n) doubles.

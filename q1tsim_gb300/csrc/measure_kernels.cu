@@ -65,6 +65,24 @@ k_segment_sums(const double* __restrict__ in, uint64_t len, double* out)
     if (threadIdx.x == 0) out[blockIdx.x] = s;
 }
 
+// First level of a long segment reduction: block b sums part b % parts of
+// segment b / parts (kSegPart values, the last part shorter).
+constexpr uint64_t kSegPart = 8192;
+
+__global__ void __launch_bounds__(256)
+k_segment_parts(const double* __restrict__ in, uint64_t len, uint64_t parts, double* __restrict__ tmp)
+{
+    __shared__ double red[32];
+    const uint64_t seg = blockIdx.x / parts, part = blockIdx.x % parts;
+    const uint64_t p0 = part * kSegPart;
+    const uint64_t n = len - p0 < kSegPart ? len - p0 : kSegPart;
+    const double* src = in + seg * len + p0;
+    double acc = 0.0;
+    for (uint64_t j = threadIdx.x; j < n; j += blockDim.x) acc += src[j];
+    const double s = block_sum(acc, red);
+    if (threadIdx.x == 0) tmp[blockIdx.x] = s;
+}
+
 // ------------------------------------------------------------- scans
 
 constexpr int kScanThreads = 512;
@@ -296,11 +314,26 @@ cudaError_t launch_chunk_sums_dense(const void* amps, int prec, uint64_t total, 
     return cudaGetLastError();
 }
 
-cudaError_t launch_segment_sums(const double* in, uint64_t nseg, uint64_t len, double* out,
+uint64_t segment_sums_tmp_doubles(uint64_t nseg, uint64_t len)
+{
+    return len > kSegPart ? nseg * ((len + kSegPart - 1) / kSegPart) : 0;
+}
+
+cudaError_t launch_segment_sums(const double* in, uint64_t nseg, uint64_t len, double* out, double* tmp,
                                 cudaStream_t st)
 {
     if (nseg == 0) return cudaSuccess;
-    k_segment_sums<<<(unsigned)nseg, 256, 0, st>>>(in, len, out);
+    if (len <= kSegPart) {
+        k_segment_sums<<<(unsigned)nseg, 256, 0, st>>>(in, len, out);
+        return cudaGetLastError();
+    }
+    // two levels, each in a fixed order: parts of kSegPart values, then the
+    // parts of each segment
+    const uint64_t parts = (len + kSegPart - 1) / kSegPart;
+    k_segment_parts<<<(unsigned)(nseg * parts), 256, 0, st>>>(in, len, parts, tmp);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_segment_sums<<<(unsigned)nseg, 256, 0, st>>>(tmp, parts, out);
     return cudaGetLastError();
 }
 

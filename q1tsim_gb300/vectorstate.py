@@ -305,6 +305,17 @@ class Plan:
         check(_lib.load().q1g_plan_info(self._h, None, ctypes.byref(nb)))
         return nb.value
 
+    def block_matrix(self, i, mats_flat):
+        """The fused matrix of block i for these gate matrices (host only)."""
+        L = _lib.load()
+        mats = np.ascontiguousarray(mats_flat, dtype=np.float64)
+        out = np.zeros(2 * 32 * 32, dtype=np.float64)
+        n = ctypes.c_size_t(out.size)
+        check(L.q1g_plan_block_matrix(self._h, i, _dptr(mats), mats.size, _dptr(out), ctypes.byref(n)),
+              "plan_block_matrix")
+        dim = int(round((n.value // 2) ** 0.5))
+        return out[:n.value].view(np.complex128).reshape(dim, dim)
+
     def blocks(self):
         """[(qubits, gate indices)] of every pass, in launch order."""
         L = _lib.load()

@@ -109,6 +109,34 @@ def test_fusion_product_equals_sequence(lib):
     assert p.nblocks < len(gates) // 2
 
 
+@pytest.mark.parametrize("width", [3, 5])
+def test_block_matrix_is_the_product_of_its_gates(lib, width):
+    """The engine's own fused matrix of every block (q1g_plan_block_matrix)
+    equals the numpy product of the block's gates, with 1-, 2- and 3-qubit
+    gates, controls and bits in any order."""
+    n = 9
+    rng = np.random.default_rng(11 + width)
+    gates = []
+    for _ in range(80):
+        r = rng.random()
+        if r < 0.45:
+            gates.append((G.U3(*rng.uniform(0, 6.28, 3)), [int(rng.integers(n))]))
+        elif r < 0.8:
+            a, b = (int(v) for v in rng.choice(n, 2, replace=False))
+            gates.append((G.Kron(G.U3(*rng.uniform(0, 6.28, 3)), G.RY(rng.uniform(0, 6.28))), [a, b]))
+        else:
+            bits = [int(v) for v in rng.choice(n, 3, replace=False)]
+            gates.append((G.CCX() if r < 0.9 else G.CU3(*rng.uniform(0, 6.28, 3)), bits[:3] if r < 0.9 else bits[:2]))
+    mats = np.concatenate([np.ascontiguousarray(g.matrix()).ravel() for g, _ in gates]).view(np.float64)
+    p = Plan(n, [b for _, b in gates], fusion_width=width)
+    for i, (qb, gs) in enumerate(p.blocks()):
+        blk = np.eye(1 << len(qb), dtype=complex)
+        for gi in gs:
+            g, b = gates[gi]
+            blk = G.embed(g.matrix(), [qb.index(q) for q in b], len(qb)) @ blk
+        np.testing.assert_allclose(p.block_matrix(i, mats), blk, atol=1e-13)
+
+
 def test_plain_plan_is_one_pass_per_gate(lib):
     gb = brick(8, 3)
     p = Plan(8, gb, fusion_width=0)

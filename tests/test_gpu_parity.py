@@ -175,6 +175,25 @@ def test_measure_into_identical_outcomes(prec):
 
 
 @pytest.mark.parametrize("prec", ["c128", "c64"])
+def test_measure_into_large_state_two_level_weights(prec):
+    """23 qubits: the qubit weights reduce 2^14 chunk sums per column in two
+    levels; outcomes and collapsed states still match the oracle."""
+    rng = np.random.default_rng(23)
+    n, shots = 23, 16
+    o, g = pair(n, shots, rand_state(n, rng), prec)
+    ro = np.zeros(shots, dtype=np.uint64)
+    rg = np.zeros(shots, dtype=np.uint64)
+    for q in (0, 22):
+        u = rng.random(len(o.counts))
+        o.measure_into(q, q % 8, ro, uniforms=u)
+        g.measure_into(q, q % 8, rg, uniforms=u)
+        assert np.array_equal(ro, rg)
+        assert g.counts == o.counts
+    tol = TOL128 if prec == "c128" else 1e-6
+    np.testing.assert_allclose(g.states(), o.states(), rtol=0, atol=tol)
+
+
+@pytest.mark.parametrize("prec", ["c128", "c64"])
 @pytest.mark.parametrize("n", [1, 4, 10, 14])
 def test_measure_all_identical_outcomes(prec, n):
     rng = np.random.default_rng(30 + n)
@@ -300,6 +319,85 @@ def test_tensor_core_block_is_exact_on_split_values():
     o.apply_gate(P, [0, 1, 2])
     out, ref = g.states()[:, 0], o.states()[:, 0]
     assert np.array_equal(out, ref), float(np.max(np.abs(out - ref)))
+
+
+def cyclic_perm(k, shift):
+    d = 1 << k
+    P = np.zeros((d, d), dtype=np.complex128)
+    for s in range(d):
+        P[(s + shift) % d, s] = 1.0
+    return P
+
+
+def split_exact_amps(n):
+    k = np.arange(1 << n) % 4096
+    return ((1.0 + k * 2.0 ** -20) / 64.0 * (1 + 1j * (k % 3 == 0))).astype(np.complex128)
+
+
+@pytest.mark.parametrize("n,qubits", [
+    (12, [7, 8, 9, 10, 11]),      # lowest positions: gate pairs adjacent, padded stage
+    (12, [0, 1, 2, 3, 4]),
+    (14, [9, 10, 11, 12, 13]),
+    (14, [1, 3, 5, 7, 9]),
+    (14, [8, 9, 10, 11]),
+    (15, [2, 7, 13]),
+    (16, [0, 5, 10, 14, 15]),
+])
+def test_tensor_core_block_exact_any_layout(n, qubits):
+    """Permutation blocks through the tensor cores on every tile layout (gate
+    bits low or high, staged rows padded or not): hi + lo recover each
+    amplitude, so the result equals the oracle's exactly."""
+    amps = split_exact_amps(n)
+    P = cyclic_perm(len(qubits), 3)
+    g = VectorState.from_amplitudes(amps, 1, "c64")
+    g.profile(True)
+    g.apply_plan(Plan(n, [qubits], 5), P.ravel().view(np.float64))
+    assert g.profile_report()["fused_tc_c64"]["launches"] == 1
+    o = orc.OracleState.from_amplitudes(amps, 1)
+    o.apply_gate(P, qubits)
+    out, ref = g.states()[:, 0], o.states()[:, 0]
+    assert np.array_equal(out, ref), float(np.max(np.abs(out - ref)))
+
+
+def test_two_blocks_share_one_tensor_core_pass():
+    """Consecutive blocks whose qubits fit one 12-position tile run in one
+    pass over the state; results stay exact."""
+    n = 14
+    amps = split_exact_amps(n)
+    seq = [([0, 1, 2], cyclic_perm(3, 1)), ([11, 12, 13], cyclic_perm(3, 5)), ([5, 6, 7], cyclic_perm(3, 2))]
+    mats = np.concatenate([m.ravel() for _, m in seq]).view(np.float64)
+    g = VectorState.from_amplitudes(amps, 1, "c64")
+    g.profile(True)
+    g.apply_plan(Plan(n, [b for b, _ in seq], 3), mats)
+    o = orc.OracleState.from_amplitudes(amps, 1)
+    for b, m in seq:
+        o.apply_gate(m, b)
+    out, ref = g.states()[:, 0], o.states()[:, 0]
+    assert np.array_equal(out, ref), float(np.max(np.abs(out - ref)))
+    rep = g.profile_report()
+    assert rep["fused_tc_c64"]["launches"] == 2, rep
+
+
+def test_two_block_passes_random_circuit():
+    """A 16-qubit random circuit fused to 5-qubit blocks (many of them paired
+    into one pass) against the oracle."""
+    rng = np.random.default_rng(21)
+    n = 16
+    amps = rand_state(n, rng)
+    gl = [random_gate(n, rng) for _ in range(120)]
+    mats = np.concatenate([np.ascontiguousarray(gt.matrix()).ravel() for gt, _ in gl]).view(np.float64)
+    o = orc.OracleState.from_amplitudes(amps, 1)
+    for gt, b in gl:
+        o.apply_gate(gt.matrix(), b)
+    ref = o.states()[:, 0]
+    g = VectorState.from_amplitudes(amps, 1, "c64")
+    g.profile(True)
+    p = Plan(n, [b for _, b in gl], 5)
+    g.apply_plan(p, mats)
+    out = g.states()[:, 0]
+    assert np.max(np.abs(out - ref)) <= TOL64
+    assert 1 - abs(np.vdot(ref, out)) ** 2 / np.linalg.norm(out) ** 2 <= 1e-9
+    assert g.profile_report()["fused_tc_c64"]["launches"] < p.nblocks
 
 
 def test_plan_rerun_with_new_parameters():
