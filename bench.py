@@ -57,6 +57,20 @@ def world_aggregate(local_ms, local_units, dist, device):
     return float(ms[0]), float(units[0])
 
 
+def dram_traffic(kernel, qubits):
+    """DRAM bytes per launch of `kernel` at `qubits` from the ncu summaries in
+    profiles/dram_traffic.txt (None when no capture covers it)."""
+    p = os.path.join(ROOT, "profiles", "dram_traffic.txt")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        for line in f:
+            parts = line.split()
+            if len(parts) >= 3 and not line.startswith("#") and parts[0] == kernel and int(parts[1]) == qubits:
+                return float(parts[2])
+    return None
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -300,18 +314,21 @@ def run_reference(args, rank, world):
 
 
 def plain_kernel_leg(n, bits, mats, stream, barrier, ngates=120):
-    """The first `ngates` gates of the circuit, one pass per gate, in both
-    precisions: per kernel, launches, time per launch and achieved HBM
-    bandwidth (bytes of the amplitudes each launch touches, read and written)
-    against the measured peak."""
+    """The first `ngates` gates of the circuit, one pass per gate, in
+    complex64, complex128 (double-float arithmetic, the default) and
+    complex128 with FP64 arithmetic: per kernel, launches, time per launch and
+    achieved HBM bandwidth (bytes of the amplitudes each launch touches, read
+    and written) against the measured peak."""
     from q1tsim_gb300 import Plan, VectorState
     peak, peak_kind = peaks()
     sub = bits[:ngates]
     ndbl = sum(2 * (1 << len(b)) ** 2 for b in sub)
     out = {"gates": len(sub), "peak_gbs": peak, "peak_kind": peak_kind}
-    for prec in ("c64", "c128"):
+    for label, prec, exact in (("c64", "c64", False), ("c128", "c128", False), ("c128_fp64", "c128", True)):
         st = VectorState(n, 1, prec)
         st.set_stream(stream.cuda_stream)
+        if exact:
+            st.set_fp64_exact()
         plan = Plan(n, sub, 0)
         st.apply_plan(plan, mats[:ndbl])      # warm-up: allocation, first touch
         barrier()
@@ -327,7 +344,7 @@ def plain_kernel_leg(n, bits, mats, stream, barrier, ngates=120):
             gbs = v["bytes"] / (v["ms"] / 1e3) / 1e9
             ks[k] = {"launches": v["launches"], "ms_per_launch": round(v["ms"] / v["launches"], 4),
                      "gbs": round(gbs, 1), "frac": round(gbs / peak, 3)}
-        out[prec] = ks
+        out[label] = ks
         del st
         barrier()
     return out
@@ -445,11 +462,9 @@ def main():
     dom = gate_kernels[dom_name]
     achieved = (dom["bytes"] / dom["launches"]) / (dom["ms"] / dom["launches"] / 1e3) / 1e9
     peak, peak_kind = peaks()
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tpath):
-        with open(tpath) as f:
-            traffic = json.load(f).get(dom_name)
+    traffic = dram_traffic(dom_name, n)
+    # fused blocks of >= 3 qubits run on the tensor cores, one or two per launch
+    tc_blocks = sum(1 for qb, _ in plan.blocks() if len(qb) >= 3)
 
     # ---- plain complex128 run of the same circuit, and the accuracy of c64
     plain_info, accuracy = None, None
@@ -519,7 +534,9 @@ def main():
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                          "launch_ms": dom["ms"] / dom["launches"],
-                         "bytes_per_launch": dom["bytes"] / dom["launches"]},
+                         "bytes_per_launch": dom["bytes"] / dom["launches"],
+                         "blocks_per_launch": (round(tc_blocks / dom["launches"], 3)
+                                               if dom_name.startswith("fused") else 1)},
             "kernels_per_step": {k: {"launches": v["launches"], "ms": round(v["ms"], 4)} for k, v in prof.items()},
             "gpu_launches": launches_per_step * args.steps,
             "e2e": {"value": e2e_value, "unit": "gates/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},

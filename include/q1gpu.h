@@ -92,6 +92,12 @@ void q1g_state_free(q1g_state* s);
 
 /* Run the state's work on a caller-owned cudaStream_t (NULL: the state's own). */
 int q1g_state_set_stream(q1g_state* s, void* cuda_stream);
+/* complex128 arithmetic of 1-qubit and diagonal updates: 0 (default) =
+ * double-float pairs on the FP32 pipe (about 47 significant bits, within the
+ * 1e-12 amplitude contract; GB300's FP64 pipe is a third of the HBM rate),
+ * 1 = FP64 (the reference's own rounding, src/gates.rs:121-152).  No
+ * reference counterpart. */
+int q1g_state_set_fp64_exact(q1g_state* s, int exact);
 int q1g_state_synchronize(q1g_state* s);
 /* nr_bits, nr_shots, number of state columns, precision.  Any pointer may be NULL. */
 int q1g_state_info(const q1g_state* s, size_t* nr_bits, size_t* nr_shots, size_t* ncols,

@@ -117,6 +117,7 @@ def load():
     _proto(L, "q1g_state_from_amplitudes", _int, [_dp, _sz, _sz, _int, ctypes.POINTER(_vp)])
     _proto(L, "q1g_state_free", None, [_vp])
     _proto(L, "q1g_state_set_stream", _int, [_vp, _vp])
+    _proto(L, "q1g_state_set_fp64_exact", _int, [_vp, _int])
     _proto(L, "q1g_state_synchronize", _int, [_vp])
     _proto(L, "q1g_state_info", _int, [_vp, _szp, _szp, _szp, ctypes.POINTER(_int)])
     _proto(L, "q1g_state_counts", _int, [_vp, _u64p, _sz])

@@ -156,6 +156,14 @@ int q1g_state_from_amplitudes(const double* amps, size_t nr_bits, size_t nr_shot
 
 void q1g_state_free(q1g_state* s) { delete s; }
 
+int q1g_state_set_fp64_exact(q1g_state* s, int exact)
+{
+    return guarded([&] {
+        need(s, "state");
+        s->fp64_exact = exact != 0;
+    });
+}
+
 int q1g_state_set_stream(q1g_state* s, void* cuda_stream)
 {
     return guarded([&] {

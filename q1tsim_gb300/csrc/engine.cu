@@ -174,13 +174,15 @@ void q1g_state::apply_op(const GateOp& op, char* base, uint64_t total_amps)
         case GateOp::Noop:
             return;
         case GateOp::Pair:
-            launch(prec == kC128 ? "pair_c128" : "pair_c64", b2 * op.touched(total_amps), [&] {
-                return launch_pair(base, prec, total_amps, op.map, op.o0, op.o1, op.m2, stream);
+            launch(prec == kC128 ? (fp64_exact ? "pair_c128_fp64" : "pair_c128") : "pair_c64",
+                   b2 * op.touched(total_amps), [&] {
+                return launch_pair(base, prec, total_amps, op.map, op.o0, op.o1, op.m2, stream, fp64_exact);
             });
             return;
         case GateOp::Phase:
-            launch(prec == kC128 ? "phase_c128" : "phase_c64", b2 * op.touched(total_amps), [&] {
-                return launch_phase(base, prec, total_amps, op.map, op.ph[0], op.ph[1], stream);
+            launch(prec == kC128 ? (fp64_exact ? "phase_c128_fp64" : "phase_c128") : "phase_c64",
+                   b2 * op.touched(total_amps), [&] {
+                return launch_phase(base, prec, total_amps, op.map, op.ph[0], op.ph[1], stream, fp64_exact);
             });
             return;
         case GateOp::Dense: {
@@ -604,6 +606,7 @@ namespace q1g {
 struct TcPass {
     IndexMap tilemap{};
     TcOffsets offs{};
+    TcTileBox box{};             // the tile as a tensor-map box
     std::vector<float> images;   // nblocks x 32 KB
 };
 
@@ -637,12 +640,17 @@ static int tile_run_bits(const std::vector<int>& T)
     return L;
 }
 
-// Shortest contiguous run a pass may copy (2^7 amplitudes = 1 KB): at most 32
-// runs per tile.
+// Shortest contiguous run a pass may copy in pieces (2^7 amplitudes = 1 KB):
+// at most 32 runs per tile.  Shorter runs need the tile to be one
+// tensor-map box, unpadded.
 constexpr int kMinTcRunBits = 7;
+// At most this many tile positions at or above 2 MB strides (position 18 of
+// complex64): a tile then touches at most 32 large pages.
+constexpr int kMaxTcHighPositions = 5;
+constexpr int kHighPosition = 18;
 
 static TcPass lower_tc_pass(const std::vector<const std::vector<cd>*>& mats,
-                            const std::vector<const std::vector<int>*>& bits, int nbits)
+                            const std::vector<const std::vector<int>*>& bits, int nbits, uint64_t ncols)
 {
     TcPass t;
     const std::vector<int> T = tile_positions(bits, nbits);
@@ -651,10 +659,12 @@ static TcPass lower_tc_pass(const std::vector<const std::vector<cd>*>& mats,
     for (int j = 0; j < 12; ++j) t.tilemap.zpos[j] = T[j];
     t.tilemap.setmask = 0;
     const int L = tile_run_bits(T);
-    if (L < kMinTcRunBits) throw Error(Q1G_ERR_INVALID_ARGUMENT, "tensor-core tile with runs shorter than 128 amplitudes");
+    t.box = tc_tile_box(T.data(), nbits, ncols);
+    if (L < kMinTcRunBits && !t.box.usable)
+        throw Error(Q1G_ERR_INVALID_ARGUMENT, "tensor-core tile with runs shorter than 128 amplitudes");
     t.offs.run_bits = (uint32_t)L;
     t.offs.nruns = 1u << (12 - L);
-    for (uint32_t r = 0; r < t.offs.nruns; ++r) {
+    for (uint32_t r = 0; r < t.offs.nruns && r < 32; ++r) {
         uint64_t o = 0;
         for (int b = L; b < 12; ++b)
             if ((r >> (b - L)) & 1) o |= uint64_t(1) << T[b];
@@ -689,7 +699,7 @@ static TcPass lower_tc_pass(const std::vector<const std::vector<cd>*>& mats,
         }
         G.vec2 = G.jgate[1] == 1u ? 1u : 0u;
     }
-    tc_choose_padding(t.offs);
+    tc_choose_padding(t.offs, t.box.usable != 0);
     return t;
 }
 
@@ -771,15 +781,22 @@ void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n)
         if (eligible(i)) {
             // two consecutive blocks share a pass when their qubits fit one
             // 12-position tile with runs of >= 128 amplitudes
-            std::vector<const std::vector<cd>*> ms{&bmats[i]};
-            std::vector<const std::vector<int>*> bs{&bbits[i]};
+            TcPass t;
+            bool paired = false;
             if (i + 1 < nb && eligible(i + 1) &&
-                union_size(positions_of(bbits[i], s->nbits), positions_of(bbits[i + 1], s->nbits)) <= 12 &&
-                tile_run_bits(tile_positions({&bbits[i], &bbits[i + 1]}, s->nbits)) >= kMinTcRunBits) {
-                ms.push_back(&bmats[i + 1]);
-                bs.push_back(&bbits[i + 1]);
+                union_size(positions_of(bbits[i], s->nbits), positions_of(bbits[i + 1], s->nbits)) <= 12) {
+                const auto T2 = tile_positions({&bbits[i], &bbits[i + 1]}, s->nbits);
+                int high = 0;
+                for (int p : T2) high += p >= kHighPosition;
+                const int L2 = tile_run_bits(T2);
+                if (high <= kMaxTcHighPositions &&
+                    (L2 >= kMinTcRunBits || tc_tile_box(T2.data(), s->nbits, s->ncols).usable)) {
+                    t = lower_tc_pass({&bmats[i], &bmats[i + 1]}, {&bbits[i], &bbits[i + 1]}, s->nbits, s->ncols);
+                    // short runs only as one unpadded tensor-map copy
+                    paired = L2 >= kMinTcRunBits || t.offs.pad_shift >= 31;
+                }
             }
-            const TcPass t = lower_tc_pass(ms, bs, s->nbits);
+            if (!paired) t = lower_tc_pass({&bmats[i]}, {&bbits[i]}, s->nbits, s->ncols);
             begin();
             if (!any_tc) {
                 s->errbuf.ensure(sizeof(int));
@@ -789,10 +806,10 @@ void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n)
             const void* img = stage(t.images.data(), t.images.size() * sizeof(float));
             const uint64_t total = s->total();
             s->launch("fused_tc_c64", 2.0 * total * s->bsz(), [&] {
-                return launch_fused_tc(s->amps.as<float2>(), total >> 12, t.tilemap, t.offs, img,
+                return launch_fused_tc(s->amps.as<float2>(), total >> 12, t.tilemap, t.offs, t.box, img,
                                        s->errbuf.as<int>(), s->sm_count(), s->stream);
             });
-            if (ms.size() == 2) ++i;   // the next block rode in this pass
+            if (paired) ++i;   // the next block rode in this pass
         } else if (op.kind == GateOp::Dense) {
             begin();
             const size_t d2 = op.dense.size();

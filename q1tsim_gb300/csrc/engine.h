@@ -72,6 +72,7 @@ struct q1g_state {
     int nbits = 0;
     uint64_t nshots = 0;
     int prec = q1g::kC128;
+    bool fp64_exact = false;   // complex128: FP64 arithmetic instead of double-float pairs
     uint64_t N = 1;
     uint64_t ncols = 1;
     std::vector<uint64_t> counts;

@@ -20,23 +20,32 @@
 // [D_main | D_corr] and A_lo*B_hi one N=64 product added to D_corr:
 // 16 MMAs per block and tile.
 //
-// One CTA per SM, persistent over tiles, with 10 warps:
-//   warp 8   loader: cp.async.bulk copies of a tile's pieces into a ring of
-//            shared-memory stages, completing on the stage's `full` mbarrier;
-//   warp 9   storer: when a tile is done, bulk-stores it back and, once the
-//            copy has read the stage, frees it on its `empty` mbarrier;
+// One CTA per SM, persistent over tiles, with 11 warps:
+//   warp 8   loader: copies a tile into a ring of shared-memory stages,
+//            completing on the stage's `full` mbarrier.  An unpadded tile is
+//            one box of a rank-5 tensor map over the state (one
+//            cp.async.bulk.tensor per tile); a padded one goes in pieces of
+//            2^piece_bits amplitudes with cp.async.bulk (many small copies
+//            cost bandwidth: 32 x 1 KB reach about 75% of one 32 KB copy);
+//   warps 9-10  storers, alternate tiles: when a tile is done, store it back
+//            and, once the copy has read the stage, free it on its `empty`
+//            mbarrier (two storers keep two stores in flight while each
+//            frees its stage without delay);
 //   warps 0-3 and 4-7: two consumer groups taking alternate tiles.  Each
 //            thread owns one row t (its TMEM lane): it reads the row's 32
 //            amplitudes from the stage, writes hi/lo to its group's A columns
 //            with tcgen05.st, one thread issues the MMAs, and after the commit
 //            each thread reads its row of D with tcgen05.ld and writes the
-//            new amplitudes back into the stage.  While one group waits for
+//            new amplitudes back into the stage.  (Two warps per lane quarter,
+//            each with half a row, measured no faster: the TMEM stores of the
+//            split, not per-thread latency, bound this phase.)  While one group waits for
 //            its MMAs the other converts or writes back, so the tensor pipe,
 //            the ALUs and the copy engine work at the same time.
 // TMEM (512 columns): group g uses 256g + [0,64) A_hi, [64,128) A_lo,
-// [128,192) D_main, [192,256) D_corr.  Every wait is bounded; on expiry the
-// CTA records an error, lets its copies land and releases its TMEM before
-// returning.
+// [128,192) D_main, [192,256) D_corr.  Every wait is bounded (in wall-clock
+// time, %globaltimer); on expiry the CTA records an error, lets its copies
+// land and releases its TMEM before returning.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -46,6 +55,7 @@
 #include <set>
 #include <string>
 #include <unordered_map>
+#include <vector>
 
 #include "common.cuh"
 #include "kernels.h"
@@ -54,11 +64,11 @@ namespace q1g {
 
 namespace {
 
-constexpr int kGroupThreads = 128;
+constexpr int kGroupThreads = 128;              // 4 warps: one per TMEM lane quarter
 constexpr int kConsumers = 2 * kGroupThreads;   // warps 0-7
 constexpr int kLoaderWarp = 8;
-constexpr int kStorerWarp = 9;
-constexpr int kTcThreads = kConsumers + 64;
+constexpr int kStorerWarp0 = 9;                 // storers: warps 9 and 10
+constexpr int kTcThreads = kConsumers + 96;
 constexpr uint32_t kTileBytes = 4096 * 8;        // one tile (complex64), without padding
 constexpr uint32_t kTmemCols = 512;
 constexpr float kLoScale = 2048.0f;     // 2^11: lo halves are stored scaled up
@@ -77,7 +87,10 @@ constexpr uint32_t kOffAbort = 212;
 constexpr uint32_t kOffRunOff = 256;    // 32 x u64
 constexpr uint32_t kOffB = 1024;
 constexpr uint32_t kAlignSlack = 1024;
-constexpr uint32_t kSpinLimit = 1u << 22;
+// Longest any wait may last: about 10^4 times a launch's normal duration, so
+// that profiler replays (which slow a launch by orders of magnitude) do not
+// trip it, and still a bound.
+constexpr uint64_t kWaitLimitNs = 4000000000ull;
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p)
 {
@@ -197,14 +210,50 @@ __device__ __forceinline__ void bulk_store(void* dst, uint32_t src_smem, uint32_
                  : "memory");
 }
 
+// One box of the tensor map `map` at coordinates c into shared memory,
+// completing on `bar`.
+__device__ __forceinline__ void tma_load_5d(uint32_t dst, const CUtensorMap* map, const int* c, uint32_t bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, "
+        "%6}], [%7];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c[0]), "r"(c[1]), "r"(c[2]), "r"(c[3]), "r"(c[4]), "r"(bar)
+        : "memory");
+}
+
+__device__ __forceinline__ void tma_store_5d(const CUtensorMap* map, const int* c, uint32_t src)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.5d.global.shared::cta.tile.bulk_group [%0, {%1, %2, %3, %4, %5}], [%6];" ::"l"(
+            reinterpret_cast<uint64_t>(map)),
+        "r"(c[0]), "r"(c[1]), "r"(c[2]), "r"(c[3]), "r"(c[4]), "r"(src)
+        : "memory");
+}
+
+// Tensor-map coordinates of a tile.
+__device__ __forceinline__ void tile_coords(uint64_t tile, const TcOffsets& o, int* c)
+{
+#pragma unroll
+    for (int d = 0; d < 5; ++d) c[d] = (int)((uint32_t)(tile >> o.tshift[d]) & o.tmask[d]);
+}
+
+__device__ __forceinline__ uint64_t global_ns()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 // Bounded wait on an mbarrier phase; gives up (returns false) when the CTA's
-// abort flag is set or after kSpinLimit polls, setting the flag.
+// abort flag is set or after kWaitLimitNs, setting the flag.
 __device__ __forceinline__ bool wait_phase(uint32_t bar, uint32_t parity, volatile int* abort_flag)
 {
-    uint32_t spins = 0;
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = global_ns();
+    uint32_t polls = 0;
     while (!mbar_try_wait(bar, parity)) {
         if (*abort_flag) return false;
-        if (++spins > kSpinLimit) {
+        if ((++polls & 255u) == 0 && global_ns() - t0 > kWaitLimitNs) {
             *abort_flag = 1;
             return false;
         }
@@ -240,9 +289,62 @@ __device__ __forceinline__ void split_tf32(float x, float& hi, float& lo)
     lo = to_tf32((x - hi) * kLoScale);
 }
 
+// Gates 16*HH .. 16*HH+15 of row `rowb` -> hi/lo operands (columns
+// 32*HH.. of A_hi and 64+32*HH.. of A_lo at TMEM address tl).
+template <int HH>
+__device__ __forceinline__ void split_half(const uint8_t* raw, uint32_t rowb, const TcBlockGeom& G, uint32_t tl)
+{
+    float hi[32], lo[32];
+    if (G.vec2) {
+#pragma unroll
+        for (int m = 0; m < 8; ++m) {
+            const float4 v = *(const float4*)(raw + rowb + G.gateoff[16 * HH + 2 * m]);
+            split_tf32(v.x, hi[4 * m], lo[4 * m]);
+            split_tf32(v.y, hi[4 * m + 1], lo[4 * m + 1]);
+            split_tf32(v.z, hi[4 * m + 2], lo[4 * m + 2]);
+            split_tf32(v.w, hi[4 * m + 3], lo[4 * m + 3]);
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            const float2 v = *(const float2*)(raw + rowb + G.gateoff[16 * HH + j]);
+            split_tf32(v.x, hi[2 * j], lo[2 * j]);
+            split_tf32(v.y, hi[2 * j + 1], lo[2 * j + 1]);
+        }
+    }
+    tmem_st32(tl + 32u * HH, hi);
+    tmem_st32(tl + 64u + 32u * HH, lo);
+}
+
+// D = D_main + 2^-11 D_corr for gates 16*HH .. 16*HH+15 of row `rowb`, back
+// into the stage.
+template <int HH>
+__device__ __forceinline__ void writeback_half(uint8_t* raw, uint32_t rowb, const TcBlockGeom& G, uint32_t tl)
+{
+    uint32_t dm[32], dc[32];
+    tmem_ld32(tl + 128u + 32u * HH, dm);
+    tmem_ld32(tl + 192u + 32u * HH, dc);
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int j = 0; j < 32; ++j) dm[j] = __float_as_uint(__fmaf_rn(__uint_as_float(dc[j]), kLoUnscale, __uint_as_float(dm[j])));
+    if (G.vec2) {
+#pragma unroll
+        for (int m = 0; m < 8; ++m)
+            *(float4*)(raw + rowb + G.gateoff[16 * HH + 2 * m]) =
+                make_float4(__uint_as_float(dm[4 * m]), __uint_as_float(dm[4 * m + 1]), __uint_as_float(dm[4 * m + 2]),
+                            __uint_as_float(dm[4 * m + 3]));
+    } else {
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+            *(float2*)(raw + rowb + G.gateoff[16 * HH + j]) =
+                make_float2(__uint_as_float(dm[2 * j]), __uint_as_float(dm[2 * j + 1]));
+    }
+}
+
 __global__ void __launch_bounds__(kTcThreads, 1)
 k_fused_tc(float2* __restrict__ a, uint64_t ntiles, const __grid_constant__ IndexMap tilemap,
-           const __grid_constant__ TcOffsets offs, const uint4* __restrict__ bimage, int* __restrict__ err)
+           const __grid_constant__ TcOffsets offs, const __grid_constant__ CUtensorMap tmap,
+           const uint4* __restrict__ bimage, int* __restrict__ err)
 {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -295,16 +397,27 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, const __grid_constant__ Inde
         for (uint64_t i = 0; i < my_tiles; ++i) {
             // use u of stage s waits until the store of use u-1 has read it
             if (u > 0 && !wait_phase(sbase + kOffEmpty + 8 * s, (u - 1) & 1u, abort_flag)) break;
-            const uint64_t base = expand_index(blockIdx.x + i * gridDim.x, tilemap);
+            const uint64_t tile = blockIdx.x + i * gridDim.x;
             const uint32_t full = sbase + kOffFull + 8 * s;
-            if (lane == 0) mbar_arrive_tx(full, kTileBytes);
-            __syncwarp();
             const uint32_t st = sbase + raw0 + s * sbytes;
-            for (uint32_t j = (uint32_t)lane; j < np; j += 32) {
-                const uint32_t x0 = j << pb;
-                bulk_load(st + 8u * x0 + ((x0 >> pad) << 4), a + ((base | run_off[x0 >> rb]) + (x0 & run_mask)),
-                          piece_bytes, full);
+            if (offs.use_tma) {
+                if (lane == 0) {
+                    int c[5];
+                    tile_coords(tile, offs, c);
+                    mbar_arrive_tx(full, kTileBytes);
+                    tma_load_5d(st, &tmap, c, full);
+                }
+            } else {
+                const uint64_t base = expand_index(tile, tilemap);
+                if (lane == 0) mbar_arrive_tx(full, kTileBytes);
+                __syncwarp();
+                for (uint32_t j = (uint32_t)lane; j < np; j += 32) {
+                    const uint32_t x0 = j << pb;
+                    bulk_load(st + 8u * x0 + ((x0 >> pad) << 4),
+                              a + ((base | run_off[x0 >> rb]) + (x0 & run_mask)), piece_bytes, full);
+                }
             }
+            __syncwarp();
             issued = i + 1;
             if (++s == nst) {
                 s = 0;
@@ -314,43 +427,53 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, const __grid_constant__ Inde
         // every load issued has landed before the CTA can exit (the
         // consumers waited for all of them unless the CTA gave up)
         const uint64_t from = issued > nst ? issued - nst : 0;
+        const uint64_t t0 = global_ns();
         for (uint64_t i = from; i < issued; ++i) {
-            uint32_t spins = 0;
             while (!mbar_try_wait(sbase + kOffFull + 8 * (uint32_t)(i % nst), (uint32_t)((i / nst) & 1)) &&
-                   ++spins <= kSpinLimit) {
+                   global_ns() - t0 <= kWaitLimitNs) {
             }
         }
-    } else if (warp == kStorerWarp) {
-        // ---------------------------------------------------------- storer
-        uint32_t s = 0, u = 0, prev = 0xFFFFFFFFu;
-        for (uint64_t i = 0; i < my_tiles; ++i) {
+    } else if (warp >= kStorerWarp0) {
+        // --------------------------------------------------------- storers
+        // storer w takes tiles w, w+2, ...; after its store has read the
+        // stage it frees the stage at once
+        const uint32_t w = (uint32_t)(warp - kStorerWarp0);
+        uint32_t s = w, u = 0;
+        for (uint64_t i = w; i < my_tiles; i += 2) {
             if (!wait_phase(sbase + kOffOut + 8 * s, u & 1u, abort_flag)) break;
-            const uint64_t base = expand_index(blockIdx.x + i * gridDim.x, tilemap);
+            const uint64_t tile = blockIdx.x + i * gridDim.x;
             const uint32_t st = sbase + raw0 + s * sbytes;
-            for (uint32_t j = (uint32_t)lane; j < np; j += 32) {
-                const uint32_t x0 = j << pb;
-                bulk_store(a + ((base | run_off[x0 >> rb]) + (x0 & run_mask)), st + 8u * x0 + ((x0 >> pad) << 4),
-                           piece_bytes);
+            if (offs.use_tma) {
+                if (lane == 0) {
+                    int c[5];
+                    tile_coords(tile, offs, c);
+                    tma_store_5d(&tmap, c, st);
+                }
+            } else {
+                const uint64_t base = expand_index(tile, tilemap);
+                for (uint32_t j = (uint32_t)lane; j < np; j += 32) {
+                    const uint32_t x0 = j << pb;
+                    bulk_store(a + ((base | run_off[x0 >> rb]) + (x0 & run_mask)),
+                               st + 8u * x0 + ((x0 >> pad) << 4), piece_bytes);
+                }
             }
             asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-            // all but this tile's copies have read their stages
-            asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+            asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
             __syncwarp();
-            if (prev != 0xFFFFFFFFu && lane == 0) mbar_arrive(sbase + kOffEmpty + 8 * prev);
-            prev = s;
-            if (++s == nst) {
-                s = 0;
+            if (lane == 0) mbar_arrive(sbase + kOffEmpty + 8 * s);
+            s += 2;
+            if (s >= nst) {
+                s -= nst;
                 ++u;
             }
         }
-        asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
-        __syncwarp();
-        if (prev != 0xFFFFFFFFu && lane == 0) mbar_arrive(sbase + kOffEmpty + 8 * prev);
         asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
     } else {
         // ------------------------------------------------ consumer groups
+        // group g = warps 4g..4g+3; warp's lane quarter q (rows 32q..32q+31)
         const uint32_t g = (uint32_t)warp >> 2, q = (uint32_t)warp & 3u;
         const uint32_t t = 32u * q + (uint32_t)lane;       // row = TMEM lane
+        const bool issuer = t == 0;
         const uint32_t gbar = 1u + g;
         const uint32_t tm = tmem + 256u * g;                // the group's columns
         const uint32_t tl = tm + ((32u * q) << 16);         // this warp's lanes
@@ -374,33 +497,12 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, const __grid_constant__ Inde
                 const uint32_t rowb = b ? rowb1 : rowb0;
                 if (b > 0) group_sync(gbar);    // the previous block's results are all staged
                 // row t -> hi/lo operands, columns 2g+c, in TMEM
-#pragma unroll
-                for (int hh = 0; hh < 2; ++hh) {
-                    float hi[32], lo[32];
-                    if (G.vec2) {
-#pragma unroll
-                        for (int m = 0; m < 8; ++m) {
-                            const float4 v = *(const float4*)(raw + rowb + G.gateoff[16 * hh + 2 * m]);
-                            split_tf32(v.x, hi[4 * m], lo[4 * m]);
-                            split_tf32(v.y, hi[4 * m + 1], lo[4 * m + 1]);
-                            split_tf32(v.z, hi[4 * m + 2], lo[4 * m + 2]);
-                            split_tf32(v.w, hi[4 * m + 3], lo[4 * m + 3]);
-                        }
-                    } else {
-#pragma unroll
-                        for (int j = 0; j < 16; ++j) {
-                            const float2 v = *(const float2*)(raw + rowb + G.gateoff[16 * hh + j]);
-                            split_tf32(v.x, hi[2 * j], lo[2 * j]);
-                            split_tf32(v.y, hi[2 * j + 1], lo[2 * j + 1]);
-                        }
-                    }
-                    tmem_st32(tl + 32u * hh, hi);
-                    tmem_st32(tl + 64u + 32u * hh, lo);
-                }
+                split_half<0>(raw, rowb, G, tl);
+                split_half<1>(raw, rowb, G, tl);
                 asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
                 asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
                 group_sync(gbar);
-                if (t == 0) {
+                if (issuer) {
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                     const uint32_t bb = sbase + kOffB + (uint32_t)b * kBImage;
                     // [D_main | D_corr] = A_hi [B_hi; B_lo']^T, then D_corr += A_lo' B_hi^T
@@ -422,28 +524,8 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, const __grid_constant__ Inde
                 }
                 ++mph;
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                // D = D_main + 2^-11 D_corr for row t, back into the stage
-#pragma unroll
-                for (int hh = 0; hh < 2; ++hh) {
-                    uint32_t dm[32], dc[32];
-                    tmem_ld32(tl + 128u + 32u * hh, dm);
-                    tmem_ld32(tl + 192u + 32u * hh, dc);
-                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                    float o[32];
-#pragma unroll
-                    for (int j = 0; j < 32; ++j)
-                        o[j] = __fmaf_rn(__uint_as_float(dc[j]), kLoUnscale, __uint_as_float(dm[j]));
-                    if (G.vec2) {
-#pragma unroll
-                        for (int m = 0; m < 8; ++m)
-                            *(float4*)(raw + rowb + G.gateoff[16 * hh + 2 * m]) =
-                                make_float4(o[4 * m], o[4 * m + 1], o[4 * m + 2], o[4 * m + 3]);
-                    } else {
-#pragma unroll
-                        for (int j = 0; j < 16; ++j)
-                            *(float2*)(raw + rowb + G.gateoff[16 * hh + j]) = make_float2(o[2 * j], o[2 * j + 1]);
-                    }
-                }
+                writeback_half<0>(raw, rowb, G, tl);
+                writeback_half<1>(raw, rowb, G, tl);
                 asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             }
             if (stop) break;
@@ -538,7 +620,7 @@ int best_row_order(const TcBlockGeom& G, uint32_t pad, uint32_t* order)
 
 }  // namespace
 
-void tc_choose_padding(TcOffsets& o)
+void tc_choose_padding(TcOffsets& o, bool tma_ok)
 {
     // The choice depends only on the tile geometry, which repeats from run to
     // run of a plan: remember it.
@@ -548,7 +630,8 @@ void tc_choose_padding(TcOffsets& o)
     };
     static std::mutex mu;
     static std::unordered_map<std::string, Choice> memo;
-    std::string key((const char*)&o.nblocks, sizeof(o.nblocks));
+    std::string key(1, tma_ok ? 'T' : 'P');
+    key.append((const char*)&o.nblocks, sizeof(o.nblocks));
     key.append((const char*)&o.run_bits, sizeof(o.run_bits));
     for (uint32_t b = 0; b < o.nblocks; ++b) {
         key.append((const char*)o.blk[b].jrow_bit, sizeof(o.blk[b].jrow_bit));
@@ -571,6 +654,7 @@ void tc_choose_padding(TcOffsets& o)
         long best = -1, ideal = 0;
         for (uint32_t b = 0; b < o.nblocks; ++b) ideal += o.blk[b].vec2 ? 16 * 4 : 32 * 2;
         for (uint32_t pad : cands) {
+            if (pad < 31 && tma_ok && best >= 0 && best <= 2 * ideal) break;   // keep the tensor-map copy
             long cost = 0;
             uint32_t order[2][7] = {};
             for (uint32_t b = 0; b < o.nblocks; ++b)
@@ -628,8 +712,95 @@ void build_tc_image(const double* m, float* image)
         }
 }
 
+TcTileBox tc_tile_box(const int* tile_pos, int nbits, uint64_t ncols)
+{
+    TcTileBox b{};
+    std::vector<char> in_tile(nbits, 0);
+    for (int j = 0; j < 12; ++j) in_tile[tile_pos[j]] = 1;
+    int nd = 0;
+    uint32_t below = 0;      // tile-index bits used by the dimensions so far
+    bool top_outside = false;
+    auto add = [&](int first, int len, bool tile) {
+        if (nd == 5) {
+            nd = 6;
+            return;
+        }
+        b.gdim[nd] = uint64_t(1) << len;
+        b.gstride[nd] = uint64_t(8) << first;
+        b.box[nd] = tile ? (1u << len) : 1u;
+        b.tshift[nd] = tile ? 0u : below;
+        b.tmask[nd] = tile ? 0u : (uint32_t)((uint64_t(1) << len) - 1);
+        if (!tile) below += (uint32_t)len;
+        ++nd;
+    };
+    for (int p = 0; p < nbits && nd <= 5;) {
+        int q = p;
+        while (q < nbits && in_tile[q] == in_tile[p]) ++q;
+        if (in_tile[p]) {
+            for (int f = p; f < q; f += 8) add(f, std::min(8, q - f), true);   // box dims <= 256
+        } else {
+            add(p, q - p, false);
+        }
+        top_outside = !in_tile[p];
+        p = q;
+    }
+    if (nd <= 5 && ncols > 1) {
+        if (top_outside) {
+            // the column index continues the top dimension
+            b.gdim[nd - 1] *= ncols;
+            b.tmask[nd - 1] = 0xFFFFFFFFu;
+        } else {
+            add(nbits, 0, false);
+            if (nd <= 5) {
+                b.gdim[nd - 1] = ncols;
+                b.tmask[nd - 1] = 0xFFFFFFFFu;
+            }
+        }
+    }
+    // dimension 0 must be a tile dimension (its coordinate, the innermost
+    // one, is then always 0) and the box must be the whole tile
+    b.usable = nd >= 1 && nd <= 5 && b.tmask[0] == 0;
+    uint64_t elems = 1;
+    for (int d = 0; d < nd && b.usable; ++d) {
+        if (b.gdim[d] > (uint64_t(1) << 32)) b.usable = 0;
+        elems *= b.box[d];
+    }
+    if (elems != 4096) b.usable = 0;
+    if (!b.usable) return b;
+    for (int d = nd; d < 5; ++d) {
+        b.gdim[d] = 1;
+        b.gstride[d] = b.gstride[d - 1] * b.gdim[d - 1];
+        b.box[d] = 1;
+        b.tshift[d] = 0;
+        b.tmask[d] = 0;
+    }
+    return b;
+}
+
+namespace {
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_tiled()
+{
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    });
+    return fn;
+}
+}  // namespace
+
 cudaError_t launch_fused_tc(float2* amps, uint64_t ntiles, const IndexMap& tilemap, const TcOffsets& offs_in,
-                            const void* d_bimage, int* d_err, int sm_count, cudaStream_t st)
+                            const TcTileBox& box, const void* d_bimage, int* d_err, int sm_count,
+                            cudaStream_t st)
 {
     static std::mutex mu;
     static int optin[64] = {0};
@@ -655,11 +826,37 @@ cudaError_t launch_fused_tc(float2* amps, uint64_t ntiles, const IndexMap& tilem
         return cudaErrorInvalidConfiguration;
     offs.nstages = std::min(kMaxStages, ((uint32_t)optin[dev] - fixed) / offs.stage_bytes);
     const uint32_t smem = fixed + offs.nstages * offs.stage_bytes;
+    // unpadded tiles: one tensor-map box per tile
+    CUtensorMap tmap;
+    std::memset(&tmap, 0, sizeof(tmap));
+    offs.use_tma = 0;
+    EncodeTiledFn enc = encode_tiled();
+    if (offs.pad_shift >= 31 && box.usable && enc) {
+        cuuint64_t gdim[5], gstride[4];
+        cuuint32_t bdim[5], estride[5] = {1, 1, 1, 1, 1};
+        for (int d = 0; d < 5; ++d) {
+            gdim[d] = box.gdim[d];
+            bdim[d] = box.box[d];
+            if (d > 0) gstride[d - 1] = box.gstride[d];
+        }
+        if (enc(&tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 5, amps, gdim, gstride, bdim, estride,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS) {
+            offs.use_tma = 1;
+            for (int d = 0; d < 5; ++d) {
+                offs.tshift[d] = box.tshift[d];
+                offs.tmask[d] = box.tmask[d];
+            }
+        }
+    }
+    // the piece path has a table of 32 runs: a tile of more runs must go as
+    // one tensor-map box
+    if (!offs.use_tma && (offs.nruns > 32 || offs.npieces > 4096u >> 5)) return cudaErrorInvalidConfiguration;
     uint64_t grid = (uint64_t)sm_count;
     if (grid > ntiles) grid = ntiles;
     if (grid == 0) return cudaSuccess;
-    k_fused_tc<<<(unsigned)grid, kTcThreads, smem, st>>>(amps, ntiles, tilemap, offs, (const uint4*)d_bimage,
-                                                         d_err);
+    k_fused_tc<<<(unsigned)grid, kTcThreads, smem, st>>>(amps, ntiles, tilemap, offs, tmap,
+                                                         (const uint4*)d_bimage, d_err);
     return cudaGetLastError();
 }
 

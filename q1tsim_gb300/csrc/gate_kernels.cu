@@ -14,6 +14,7 @@
 // loads are issued before any store, consecutive threads own consecutive
 // units (coalesced), and complex64 states use 16-byte vector accesses.
 #include "common.cuh"
+#include "df64.cuh"
 #include "kernels.h"
 
 namespace q1g {
@@ -122,6 +123,111 @@ k_pair_adj(float2* __restrict__ a, uint64_t units, IndexMap map, Mat2<float2> m)
     }
 }
 
+// ------------------------------------------------- exact unit shuffles
+//
+// A 2x2 matrix with one entry of 0, +-1 or +-i per row and column (X, Y,
+// CX, CY, CCX, Swap ...) moves and re-signs amplitudes; no arithmetic.
+// Unit code u: 0 -> x, 1 -> i x, 2 -> -x, 3 -> -i x.
+template <typename T>
+__device__ __forceinline__ T unit_times(int u, T x)
+{
+    switch (u) {
+        case 1: return T{-x.y, x.x};
+        case 2: return T{-x.x, -x.y};
+        case 3: return T{x.y, -x.x};
+        default: return x;
+    }
+}
+
+// out0 = u0 * x[s0], out1 = u1 * x[s1] (s0 != s1)
+template <typename T, int U>
+__global__ void __launch_bounds__(kThreads)
+k_pair_mono(T* __restrict__ a, uint64_t units, IndexMap map, uint64_t o0, uint64_t o1, int swap, int u0, int u1)
+{
+    uint64_t base = (uint64_t(blockIdx.x) * U) * blockDim.x + threadIdx.x;
+    T x0[U], x1[U];
+    uint64_t idx[U];
+#pragma unroll
+    for (int k = 0; k < U; ++k) {
+        const uint64_t u = base + uint64_t(k) * blockDim.x;
+        idx[k] = u < units ? expand_index(u, map) : ~uint64_t(0);
+        if (u < units) {
+            x0[k] = a[idx[k] | o0];
+            x1[k] = a[idx[k] | o1];
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < U; ++k) {
+        if (idx[k] != ~uint64_t(0)) {
+            a[idx[k] | o0] = unit_times(u0, swap ? x1[k] : x0[k]);
+            a[idx[k] | o1] = unit_times(u1, swap ? x0[k] : x1[k]);
+        }
+    }
+}
+
+// ------------------------------------- complex128 without the FP64 pipe
+
+struct Mat2DF {
+    DF re[4], im[4];   // m00, m01, m10, m11
+};
+
+__host__ inline DF host_split(double v)
+{
+    uint64_t b;
+    std::memcpy(&b, &v, 8);
+    DF d{0.0f, 0.0f};
+    if (!split_f64(b, d)) {
+        // outside the split's range: nearest float pair
+        d.h = (float)v;
+        d.l = (float)(v - (double)d.h);
+    }
+    return d;
+}
+
+// out0 = m00 x0 + m01 x1, out1 = m10 x0 + m11 x1 on double-float pairs; a
+// unit with an amplitude outside the split's range is done in FP64 (md).
+template <int U>
+__global__ void __launch_bounds__(kThreads)
+k_pair_c128x(double2* __restrict__ a, uint64_t units, IndexMap map, uint64_t o0, uint64_t o1, Mat2DF m,
+             Mat2<double2> md)
+{
+    uint64_t base = (uint64_t(blockIdx.x) * U) * blockDim.x + threadIdx.x;
+    ulonglong2 x0[U], x1[U];
+    uint64_t idx[U];
+    ulonglong2* ab = reinterpret_cast<ulonglong2*>(a);
+#pragma unroll
+    for (int k = 0; k < U; ++k) {
+        const uint64_t u = base + uint64_t(k) * blockDim.x;
+        idx[k] = u < units ? expand_index(u, map) : ~uint64_t(0);
+        if (u < units) {
+            x0[k] = ab[idx[k] | o0];
+            x1[k] = ab[idx[k] | o1];
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < U; ++k) {
+        if (idx[k] == ~uint64_t(0)) continue;
+        DF v[4];   // x0.re, x0.im, x1.re, x1.im
+        const bool ok = split_f64(x0[k].x, v[0]) & split_f64(x0[k].y, v[1]) & split_f64(x1[k].x, v[2]) &
+                        split_f64(x1[k].y, v[3]);
+        if (ok) {
+            const DF nim0{-m.im[0].h, -m.im[0].l}, nim1{-m.im[1].h, -m.im[1].l};
+            const DF nim2{-m.im[2].h, -m.im[2].l}, nim3{-m.im[3].h, -m.im[3].l};
+            const DF ar0[4] = {m.re[0], nim0, m.re[1], nim1}, br0[4] = {v[0], v[1], v[2], v[3]};
+            const DF ai0[4] = {m.re[0], m.im[0], m.re[1], m.im[1]}, bi[4] = {v[1], v[0], v[3], v[2]};
+            const DF ar1[4] = {m.re[2], nim2, m.re[3], nim3};
+            const DF ai1[4] = {m.re[2], m.im[2], m.re[3], m.im[3]};
+            ab[idx[k] | o0] = make_ulonglong2(join_f64(dot<4>(ar0, br0)), join_f64(dot<4>(ai0, bi)));
+            ab[idx[k] | o1] = make_ulonglong2(join_f64(dot<4>(ar1, br0)), join_f64(dot<4>(ai1, bi)));
+        } else {
+            const double2 y0 = *reinterpret_cast<const double2*>(&x0[k]);
+            const double2 y1 = *reinterpret_cast<const double2*>(&x1[k]);
+            a[idx[k] | o0] = cmuladd2(md.m00, y0, md.m01, y1);
+            a[idx[k] | o1] = cmuladd2(md.m10, y0, md.m11, y1);
+        }
+    }
+}
+
 // --------------------------------------------------------------- PHASE
 
 template <typename T, int U>
@@ -162,6 +268,54 @@ k_phase_vec2(float2* __restrict__ a, uint64_t units, IndexMap map, float2 ph)
             float2 q = cmul(ph, make_float2(x[k].z, x[k].w));
             *reinterpret_cast<float4*>(a + idx[k]) = make_float4(p.x, p.y, q.x, q.y);
         }
+}
+
+// x -> u x for a unit u in {1, i, -1, -i} (code as unit_times)
+template <typename T, int U>
+__global__ void __launch_bounds__(kThreads)
+k_phase_mono(T* __restrict__ a, uint64_t units, IndexMap map, int code)
+{
+    uint64_t base = (uint64_t(blockIdx.x) * U) * blockDim.x + threadIdx.x;
+    T x[U];
+    uint64_t idx[U];
+#pragma unroll
+    for (int k = 0; k < U; ++k) {
+        const uint64_t u = base + uint64_t(k) * blockDim.x;
+        idx[k] = u < units ? expand_index(u, map) : ~uint64_t(0);
+        if (u < units) x[k] = a[idx[k]];
+    }
+#pragma unroll
+    for (int k = 0; k < U; ++k)
+        if (idx[k] != ~uint64_t(0)) a[idx[k]] = unit_times(code, x[k]);
+}
+
+// complex128 phase on double-float pairs (FP64 for out-of-range amplitudes)
+template <int U>
+__global__ void __launch_bounds__(kThreads)
+k_phase_c128x(double2* __restrict__ a, uint64_t units, IndexMap map, DF pr, DF pi, double2 pd)
+{
+    uint64_t base = (uint64_t(blockIdx.x) * U) * blockDim.x + threadIdx.x;
+    ulonglong2 x[U];
+    uint64_t idx[U];
+    ulonglong2* ab = reinterpret_cast<ulonglong2*>(a);
+#pragma unroll
+    for (int k = 0; k < U; ++k) {
+        const uint64_t u = base + uint64_t(k) * blockDim.x;
+        idx[k] = u < units ? expand_index(u, map) : ~uint64_t(0);
+        if (u < units) x[k] = ab[idx[k]];
+    }
+#pragma unroll
+    for (int k = 0; k < U; ++k) {
+        if (idx[k] == ~uint64_t(0)) continue;
+        DF v[2];
+        if (split_f64(x[k].x, v[0]) & split_f64(x[k].y, v[1])) {
+            const DF ar[2] = {pr, DF{-pi.h, -pi.l}}, ai[2] = {pr, pi};
+            const DF br[2] = {v[0], v[1]}, bi[2] = {v[1], v[0]};
+            ab[idx[k]] = make_ulonglong2(join_f64(dot<2>(ar, br)), join_f64(dot<2>(ai, bi)));
+        } else {
+            a[idx[k]] = cmul(pd, *reinterpret_cast<const double2*>(&x[k]));
+        }
+    }
 }
 
 // --------------------------------------------------------------- DENSE
@@ -205,15 +359,62 @@ inline unsigned grid_for(uint64_t units, int per_block)
 
 }  // namespace
 
+namespace {
+// Unit code of (re, im) if it is 1, i, -1 or -i (as unit_times), -1 for 0,
+// -2 otherwise.
+int unit_code(double re, double im)
+{
+    if (re == 0.0 && im == 0.0) return -1;
+    if (re == 1.0 && im == 0.0) return 0;
+    if (re == 0.0 && im == 1.0) return 1;
+    if (re == -1.0 && im == 0.0) return 2;
+    if (re == 0.0 && im == -1.0) return 3;
+    return -2;
+}
+
+// A 2x2 matrix with one unit entry per row and column: (swap, u0, u1).
+bool mono_pair(const double* m, int& swap, int& u0, int& u1)
+{
+    const int c00 = unit_code(m[0], m[1]), c01 = unit_code(m[2], m[3]);
+    const int c10 = unit_code(m[4], m[5]), c11 = unit_code(m[6], m[7]);
+    if (c00 >= 0 && c11 >= 0 && c01 == -1 && c10 == -1) {
+        swap = 0, u0 = c00, u1 = c11;
+        return true;
+    }
+    if (c01 >= 0 && c10 >= 0 && c00 == -1 && c11 == -1) {
+        swap = 1, u0 = c01, u1 = c10;
+        return true;
+    }
+    return false;
+}
+}  // namespace
+
 cudaError_t launch_pair(void* amps, int prec, uint64_t total, const IndexMap& map,
-                        uint64_t o0, uint64_t o1, const double* m, cudaStream_t st)
+                        uint64_t o0, uint64_t o1, const double* m, cudaStream_t st, bool fp64_exact)
 {
     const uint64_t pairs = total >> map.nz;
     if (pairs == 0) return cudaSuccess;
-    if (prec == kC128) {
-        auto mm = make_mat2<double2>(m);
+    int swap = 0, u0 = 0, u1 = 0;
+    if (mono_pair(m, swap, u0, u1)) {
+        if (prec == kC128)
+            k_pair_mono<double2, kUnroll><<<grid_for(pairs, kThreads * kUnroll), kThreads, 0, st>>>(
+                (double2*)amps, pairs, map, o0, o1, swap, u0, u1);
+        else
+            k_pair_mono<float2, kUnroll><<<grid_for(pairs, kThreads * kUnroll), kThreads, 0, st>>>(
+                (float2*)amps, pairs, map, o0, o1, swap, u0, u1);
+        return cudaGetLastError();
+    }
+    if (prec == kC128 && fp64_exact) {
         k_pair<double2, kUnroll><<<grid_for(pairs, kThreads * kUnroll), kThreads, 0, st>>>(
-            (double2*)amps, pairs, map, o0, o1, mm);
+            (double2*)amps, pairs, map, o0, o1, make_mat2<double2>(m));
+    } else if (prec == kC128) {
+        Mat2DF mx;
+        for (int e = 0; e < 4; ++e) {
+            mx.re[e] = host_split(m[2 * e]);
+            mx.im[e] = host_split(m[2 * e + 1]);
+        }
+        k_pair_c128x<kUnroll><<<grid_for(pairs, kThreads * kUnroll), kThreads, 0, st>>>(
+            (double2*)amps, pairs, map, o0, o1, mx, make_mat2<double2>(m));
     } else {
         auto mm = make_mat2<float2>(m);
         const bool pos0_free = map.nz == 0 || map.zpos[0] > 0;
@@ -233,13 +434,26 @@ cudaError_t launch_pair(void* amps, int prec, uint64_t total, const IndexMap& ma
 }
 
 cudaError_t launch_phase(void* amps, int prec, uint64_t total, const IndexMap& map,
-                         double ph_re, double ph_im, cudaStream_t st)
+                         double ph_re, double ph_im, cudaStream_t st, bool fp64_exact)
 {
     const uint64_t units = total >> map.nz;
     if (units == 0) return cudaSuccess;
-    if (prec == kC128) {
+    const int code = unit_code(ph_re, ph_im);
+    if (code >= 0) {
+        if (prec == kC128)
+            k_phase_mono<double2, kUnroll><<<grid_for(units, kThreads * kUnroll), kThreads, 0, st>>>(
+                (double2*)amps, units, map, code);
+        else
+            k_phase_mono<float2, kUnroll><<<grid_for(units, kThreads * kUnroll), kThreads, 0, st>>>(
+                (float2*)amps, units, map, code);
+        return cudaGetLastError();
+    }
+    if (prec == kC128 && fp64_exact) {
         k_phase<double2, kUnroll><<<grid_for(units, kThreads * kUnroll), kThreads, 0, st>>>(
             (double2*)amps, units, map, make_double2(ph_re, ph_im));
+    } else if (prec == kC128) {
+        k_phase_c128x<kUnroll><<<grid_for(units, kThreads * kUnroll), kThreads, 0, st>>>(
+            (double2*)amps, units, map, host_split(ph_re), host_split(ph_im), make_double2(ph_re, ph_im));
     } else {
         const bool pos0_free = map.nz == 0 || map.zpos[0] > 0;
         if (pos0_free && (map.setmask & 1) == 0 && units >= 2) {

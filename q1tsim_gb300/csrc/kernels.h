@@ -19,11 +19,13 @@ struct DenseOffsets {
 };
 
 // ---- gate_kernels.cu: one gate per pass over `total` amplitudes
+// complex128 updates run on double-float pairs (df64.cuh) unless
+// fp64_exact, which keeps FP64 arithmetic.
 cudaError_t launch_pair(void* amps, int prec, uint64_t total, const IndexMap& map,
                         uint64_t o0, uint64_t o1, const double* m /*2x2 (re,im)*/,
-                        cudaStream_t st);
+                        cudaStream_t st, bool fp64_exact = false);
 cudaError_t launch_phase(void* amps, int prec, uint64_t total, const IndexMap& map,
-                         double ph_re, double ph_im, cudaStream_t st);
+                         double ph_re, double ph_im, cudaStream_t st, bool fp64_exact = false);
 // dmat: device matrix 2^tb x 2^tb, complex in the state's precision.
 cudaError_t launch_dense(void* amps, int prec, uint64_t total, const IndexMap& map,
                          const DenseOffsets& offs, int tb, const void* dmat, cudaStream_t st);
@@ -58,17 +60,39 @@ struct TcOffsets {
     uint32_t npieces;
     uint32_t nstages;        // filled in by launch_fused_tc
     uint32_t stage_bytes;
+    uint32_t use_tma;        // 1: one tensor-map copy per tile (set by launch_fused_tc)
+    uint32_t tshift[5];      // tensor-map coordinate d = (tile >> tshift[d]) & tmask[d]
+    uint32_t tmask[5];
+    uint32_t pad1_;
     uint64_t run_off[32];
     TcBlockGeom blk[2];
 };
+// A tile as a box of a rank-5 tensor map over the state: dimensions follow
+// the runs of tile / non-tile positions (tile runs split every 8 positions,
+// the column index merged into the top dimension).  usable = 0 when more
+// than 5 dimensions would be needed.
+struct TcTileBox {
+    int usable;
+    uint64_t gdim[5];
+    uint64_t gstride[5];     // bytes, dimensions 1..4
+    uint32_t box[5];
+    uint32_t tshift[5];
+    uint32_t tmask[5];
+};
+TcTileBox tc_tile_box(const int* tile_pos /* 12, ascending */, int nbits, uint64_t ncols);
 // Picks pad_shift (and piece_bits, npieces, stage_bytes, the blocks' staged
 // offsets) that minimise shared-memory bank conflicts of the per-row reads.
-void tc_choose_padding(TcOffsets& offs);
+// With tma_ok (the tile is one tensor-map box) an unpadded tile is kept when
+// its conflicts stay within twice the minimum: one tensor copy per tile beats
+// padded piece copies.
+void tc_choose_padding(TcOffsets& offs, bool tma_ok);
 // d_bimage: nblocks consecutive 32 KB hi/lo images of the blocks' real 64x64
 // embeddings in the kernel's swizzled layout; d_err: set to 1 if a bounded
 // wait expired.
+// box: the tile as a tensor-map box (used for unpadded passes when usable).
 cudaError_t launch_fused_tc(float2* amps, uint64_t ntiles, const IndexMap& tilemap, const TcOffsets& offs,
-                            const void* d_bimage, int* d_err, int sm_count, cudaStream_t st);
+                            const TcTileBox& box, const void* d_bimage, int* d_err, int sm_count,
+                            cudaStream_t st);
 // Host: the 32 KB image for the 32x32 complex matrix m (row-major (re, im)).
 void build_tc_image(const double* m, float* image);
 

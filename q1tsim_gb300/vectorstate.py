@@ -165,6 +165,11 @@ class VectorState:
         return {"max_abs_diff": float(out[0]), "infidelity": float(out[1]), "tv": float(out[2]),
                 "norm_a": float(out[3]), "norm_b": float(out[4])}
 
+    def set_fp64_exact(self, exact=True):
+        """complex128: FP64 arithmetic (the reference's rounding) instead of
+        the default double-float pairs (within the 1e-12 contract)."""
+        check(_lib.load().q1g_state_set_fp64_exact(self._h, 1 if exact else 0))
+
     def set_stream(self, stream):
         """Run on a caller-owned cudaStream_t (an int handle), None = own."""
         check(_lib.load().q1g_state_set_stream(self._h, ctypes.c_void_p(stream) if stream else None))

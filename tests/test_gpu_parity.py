@@ -69,14 +69,21 @@ def random_gate(n, rng):
 
 # ------------------------------------------------------------------ KATs
 
-@pytest.mark.parametrize("prec,tol", [("c128", 1e-14), ("c64", TOL64)])
+# complex128 in FP64 (the reference's rounding) and in the default
+# double-float arithmetic (about 47 bits; contract 1e-12)
+MODES = [("c128", True, 1e-14), ("c128", False, 1e-13), ("c64", False, TOL64)]
+
+
+@pytest.mark.parametrize("prec,exact,tol", MODES, ids=["c128-fp64", "c128", "c64"])
 @pytest.mark.parametrize("case", K["vectorstate"], ids=lambda c: c["name"])
-def test_vectorstate_kats_on_gpu(case, prec, tol):
+def test_vectorstate_kats_on_gpu(case, prec, exact, tol):
     init = case["init"]
     if init["kind"] == "new":
         s = VectorState(init["nr_bits"], init["nr_shots"], prec)
     else:
         s = VectorState.from_qubit_coefs(dec(init["coefs"]), init["nr_shots"], prec)
+    if exact:
+        s.set_fp64_exact()
     for op in case["ops"]:
         if op["op"] == "gate":
             s.apply_gate(dec(op["mat"]), op["bits"])
@@ -88,27 +95,72 @@ def test_vectorstate_kats_on_gpu(case, prec, tol):
     np.testing.assert_allclose(s.states(), dec(case["expect"]["states"]), rtol=0, atol=tol)
 
 
+@pytest.mark.parametrize("exact,tol", [(True, 1e-14), (False, 1e-13)], ids=["fp64", "df64"])
 @pytest.mark.parametrize("case", K["apply"], ids=lambda c: c["gate"] + "@" + c["source"])
-def test_gate_apply_kats_on_gpu(case):
+def test_gate_apply_kats_on_gpu(case, exact, tol):
     state, expect, mat = dec(case["state"]), dec(case["expect"]), dec(case["mat"])
     for c in range(state.shape[1]):
         s = VectorState.from_amplitudes(state[:, c], 1)
+        if exact:
+            s.set_fp64_exact()
         s.apply_gate(mat, case["bits"])
-        np.testing.assert_allclose(s.states()[:, 0], expect[:, c], rtol=0, atol=1e-14)
+        np.testing.assert_allclose(s.states()[:, 0], expect[:, c], rtol=0, atol=tol)
 
 
 # ------------------------------------------------------ random circuits
 
+@pytest.mark.parametrize("exact", [False, True], ids=["df64", "fp64"])
 @pytest.mark.parametrize("n", [1, 2, 3, 5, 8, 11, 13])
-def test_random_gates_c128_match_oracle(n):
+def test_random_gates_c128_match_oracle(n, exact):
     rng = np.random.default_rng(100 + n)
     amps = rand_state(n, rng)
     o, g = pair(n, 64, amps)
+    if exact:
+        g.set_fp64_exact()
     for _ in range(60):
         gate, bits = random_gate(n, rng)
         o.apply_gate(gate.matrix(), bits)
         g.apply_gate(gate, bits)
     same(o, g)
+
+
+def test_c128_gates_on_extreme_magnitudes():
+    """complex128 pair and phase updates run on split double-float pairs;
+    amplitudes outside that range (below 2^-74, above 2^126) take the FP64
+    path per pair, exact zeros stay exact.  All within 1e-12 of the oracle,
+    relative to each amplitude's scale."""
+    rng = np.random.default_rng(77)
+    n = 10
+    amps = rand_state(n, rng)
+    amps[rng.random(1 << n) < 0.2] = 0.0
+    tiny = rng.random(1 << n) < 0.1
+    amps[tiny] *= 1e-30
+    big = rng.random(1 << n) < 0.05
+    amps[big] *= 1e140
+    o, g = pair(n, 1, amps)
+    gates = [(G.U3(0.3, 1.1, -0.4), [2]), (G.H(), [9]), (G.T(), [4]), (G.CU1(0.77), [1, 8]), (G.RX(2.2), [0]),
+             (G.X(), [5]), (G.Y(), [3]), (G.CX(), [6, 7]), (G.S(), [2]), (G.Swap(), [0, 9])]
+    for gt, b in gates:
+        o.apply_gate(gt.matrix(), b)
+        g.apply_gate(gt, b)
+    so, sg = o.states()[:, 0], g.states()[:, 0]
+    err = np.abs(sg - so) / np.maximum(np.abs(so), 1.0)
+    assert float(np.max(err)) <= 1e-12, float(np.max(err))
+    assert np.array_equal(so == 0, sg == 0)
+
+
+def test_c128_unit_matrices_move_amplitudes_exactly():
+    """X, Y, CX, CY, Swap, Z, S and controlled forms only move and re-sign
+    amplitudes: bit-identical to the oracle."""
+    rng = np.random.default_rng(78)
+    n = 9
+    amps = rand_state(n, rng)
+    o, g = pair(n, 1, amps)
+    for gt, b in [(G.X(), [0]), (G.Y(), [4]), (G.CX(), [2, 5]), (G.CY(), [8, 1]), (G.Swap(), [3, 6]),
+                  (G.Z(), [7]), (G.S(), [2]), (G.Sdg(), [5]), (G.CZ(), [0, 4]), (G.CCX(), [1, 2, 3])]:
+        o.apply_gate(gt.matrix(), b)
+        g.apply_gate(gt, b)
+    assert np.array_equal(o.states(), g.states())
 
 
 @pytest.mark.parametrize("n", [2, 6, 12])
@@ -376,6 +428,27 @@ def test_two_blocks_share_one_tensor_core_pass():
     assert np.array_equal(out, ref), float(np.max(np.abs(out - ref)))
     rep = g.profile_report()
     assert rep["fused_tc_c64"]["launches"] == 2, rep
+
+
+@pytest.mark.parametrize("n,first,second", [
+    (22, [1, 2, 3, 4, 5], [5, 6, 7, 8, 9]),        # tile runs of 8 amplitudes
+    (20, [0, 1, 2, 3, 4], [3, 4, 5, 6, 7]),        # tile runs of 8, top position in the tile
+])
+def test_short_run_pair_goes_as_one_tensor_map_box(n, first, second):
+    """Two overlapping 5-qubit blocks on high positions: their tile has short
+    contiguous runs, so the pass copies it as one tensor-map box; exact."""
+    amps = split_exact_amps(n)
+    seq = [(first, cyclic_perm(5, 7)), (second, cyclic_perm(5, 11))]
+    mats = np.concatenate([m.ravel() for _, m in seq]).view(np.float64)
+    g = VectorState.from_amplitudes(amps, 1, "c64")
+    g.profile(True)
+    g.apply_plan(Plan(n, [b for b, _ in seq], 5), mats)
+    o = orc.OracleState.from_amplitudes(amps, 1)
+    for b, m in seq:
+        o.apply_gate(m, b)
+    out, ref = g.states()[:, 0], o.states()[:, 0]
+    assert np.array_equal(out, ref), float(np.max(np.abs(out - ref)))
+    assert g.profile_report()["fused_tc_c64"]["launches"] == 1
 
 
 def test_two_block_passes_random_circuit():
