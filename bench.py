@@ -189,6 +189,55 @@ def qft_leg(args):
     return out
 
 
+def cfg2_leg(args):
+    """configs[2]: 32-qubit U3/CX brick, depth 24, complex64 with fused
+    5-qubit 3xTF32 tensor-core blocks, then 10^6 Z-basis shots; 1 - F and
+    outcome TV against a complex128 run of the same circuit on the GPU
+    (32 GiB + 64 GiB of HBM).  Opt-in (--cfg2): the complex128 run alone
+    takes tens of seconds."""
+    import torch
+    from q1tsim_gb300 import Plan, Rng, VectorState
+    from q1tsim_gb300 import gates as G
+    n = 32
+    gl = brick_gates(n, 24, args.seed + 11)
+    gates = [(G.by_name(nm, p), b) for nm, p, b in gl]
+    bits = [b for _, b in gates]
+    mats = np.concatenate([np.ascontiguousarray(g.matrix()).ravel() for g, _ in gates]).view(np.float64)
+    out = {"workload": f"random U3/CX brick circuit, {n} qubits, depth 24 ({len(gates)} gates), complex64 fused "
+                       f"k<={args.fusion}, then 1000000 Z shots; complex128 run on the GPU as the reference",
+           "gates": len(gates)}
+    fused = VectorState(n, 1, "c64")
+    plan = Plan(n, bits, args.fusion)
+    fused.apply_plan(plan, mats)            # warm-up
+    fused.reset_all()
+    fused.synchronize()
+    t0 = time.perf_counter()
+    fused.apply_plan(plan, mats)
+    fused.synchronize()
+    dt = time.perf_counter() - t0
+    res = np.zeros(1_000_000, dtype=np.uint64)
+    fused.peek_all_into(list(range(n)), res, rng=Rng(args.seed + 13))
+    fused.synchronize()
+    t1 = time.perf_counter()
+    fused.peek_all_into(list(range(n)), res, rng=Rng(args.seed + 14))
+    fused.synchronize()
+    st = time.perf_counter() - t1
+    out["c64"] = {"ms": dt * 1e3, "passes": plan.nblocks, "gates_per_s": len(gates) / dt,
+                  "shots_per_s": 1e6 / st}
+    plain = VectorState(n, 1, "c128")
+    pplan = Plan(n, bits, 0)
+    plain.synchronize()
+    t0 = time.perf_counter()
+    plain.apply_plan(pplan, mats)
+    plain.synchronize()
+    dt = time.perf_counter() - t0
+    out["c128"] = {"ms": dt * 1e3, "passes": pplan.nblocks, "gates_per_s": len(gates) / dt}
+    out["accuracy_c64_vs_c128"] = plain.compare(fused)
+    del plain, fused
+    torch.cuda.empty_cache()
+    return out
+
+
 def cfg0_leg(args):
     """configs[0]: 16-qubit U3/CX brick, 20 layers, measure_all over 8192
     runs, histogram -- on the GPU (complex128 plain and complex64 fused) and
@@ -371,6 +420,7 @@ def main():
     ap.add_argument("--no-qft", action="store_true", help="skip the 28-qubit QFT accuracy leg")
     ap.add_argument("--no-cfg0", action="store_true", help="skip the 16-qubit CPU-runnable leg")
     ap.add_argument("--qft-qubits", type=int, default=28)
+    ap.add_argument("--cfg2", action="store_true", help="add the 32-qubit complex64 vs complex128 leg")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -517,6 +567,7 @@ def main():
     serving = None if args.no_serve else serving_leg(args)
     qft = None if args.no_qft else qft_leg(args)
     cfg0 = None if args.no_cfg0 else cfg0_leg(args)
+    cfg2 = cfg2_leg(args) if args.cfg2 else None
 
     if rank == 0:
         line = {
@@ -546,6 +597,7 @@ def main():
             "serving": serving,
             "qft_random_state": qft,
             "cpu_runnable_16q": cfg0,
+            "brick_32q": cfg2,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:

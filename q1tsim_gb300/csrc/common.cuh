@@ -48,6 +48,27 @@ __host__ __device__ __forceinline__ uint64_t expand_index(uint64_t j, const Inde
     return j | m.setmask;
 }
 
+// expand_index for a map of exactly NZ zero positions, unrolled without
+// predicates (NZ = 0: any count up to kMaxMapBits, as expand_index).  A
+// predicated iteration still issues, so small maps use the exact form.
+template <int NZ>
+__host__ __device__ __forceinline__ uint64_t expand_nz(uint64_t j, const IndexMap& m)
+{
+    if constexpr (NZ == 0) {
+        return expand_index(j, m);
+    } else {
+#ifdef __CUDA_ARCH__
+#pragma unroll
+#endif
+        for (int q = 0; q < NZ; ++q) {
+            const int p = m.zpos[q];
+            const uint64_t low = j & ((uint64_t(1) << p) - 1);
+            j = ((j >> p) << (p + 1)) | low;
+        }
+        return j | m.setmask;
+    }
+}
+
 template <typename R> struct Cplx;
 template <> struct Cplx<double> { using T = double2; };
 template <> struct Cplx<float> { using T = float2; };

@@ -87,10 +87,12 @@ constexpr uint32_t kOffAbort = 212;
 constexpr uint32_t kOffRunOff = 256;    // 32 x u64
 constexpr uint32_t kOffB = 1024;
 constexpr uint32_t kAlignSlack = 1024;
-// Longest any wait may last: about 10^4 times a launch's normal duration, so
-// that profiler replays (which slow a launch by orders of magnitude) do not
-// trip it, and still a bound.
-constexpr uint64_t kWaitLimitNs = 4000000000ull;
+// Longest any wait may last.  Normal waits last microseconds; profiler
+// replays with instrumented instructions slow a launch by four orders of
+// magnitude or more and must not trip the limit.  A CTA that does give up
+// sets the abort flag, every other wait then returns at once, and the
+// launch ends within about this time.
+constexpr uint64_t kWaitLimitNs = 60000000000ull;
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p)
 {
@@ -253,7 +255,8 @@ __device__ __forceinline__ bool wait_phase(uint32_t bar, uint32_t parity, volati
     uint32_t polls = 0;
     while (!mbar_try_wait(bar, parity)) {
         if (*abort_flag) return false;
-        if ((++polls & 255u) == 0 && global_ns() - t0 > kWaitLimitNs) {
+        if (++polls > 64) __nanosleep(64);   // long waits leave issue slots to the warps waited for
+        if ((polls & 255u) == 0 && global_ns() - t0 > kWaitLimitNs) {
             *abort_flag = 1;
             return false;
         }

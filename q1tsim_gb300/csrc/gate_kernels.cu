@@ -13,6 +13,8 @@
 // All are streaming kernels: each thread owns U independent units whose
 // loads are issued before any store, consecutive threads own consecutive
 // units (coalesced), and complex64 states use 16-byte vector accesses.
+#include <type_traits>
+
 #include "common.cuh"
 #include "df64.cuh"
 #include "kernels.h"
@@ -43,7 +45,7 @@ __host__ Mat2<T> make_mat2(const double* m)
 
 // Scalar form: one pair per unit (complex128, or complex64 when the pair
 // members are not 16-byte neighbours).
-template <typename T, int U>
+template <typename T, int U, int NZ>
 __global__ void __launch_bounds__(kThreads)
 k_pair(T* __restrict__ a, uint64_t units, IndexMap map, uint64_t o0, uint64_t o1, Mat2<T> m)
 {
@@ -53,7 +55,7 @@ k_pair(T* __restrict__ a, uint64_t units, IndexMap map, uint64_t o0, uint64_t o1
 #pragma unroll
     for (int k = 0; k < U; ++k) {
         const uint64_t u = base + uint64_t(k) * blockDim.x;
-        idx[k] = u < units ? expand_index(u, map) : ~uint64_t(0);
+        idx[k] = u < units ? expand_nz<NZ>(u, map) : ~uint64_t(0);
         if (u < units) {
             x0[k] = a[idx[k] | o0];
             x1[k] = a[idx[k] | o1];
@@ -70,7 +72,7 @@ k_pair(T* __restrict__ a, uint64_t units, IndexMap map, uint64_t o0, uint64_t o1
 
 // complex64, no gate bit at position 0: unit = two neighbouring pairs, so
 // both members are loaded as float4 (two amplitudes each).
-template <int U>
+template <int U, int NZ>
 __global__ void __launch_bounds__(kThreads)
 k_pair_vec2(float2* __restrict__ a, uint64_t units, IndexMap map, uint64_t o0, uint64_t o1, Mat2<float2> m)
 {
@@ -80,7 +82,7 @@ k_pair_vec2(float2* __restrict__ a, uint64_t units, IndexMap map, uint64_t o0, u
 #pragma unroll
     for (int k = 0; k < U; ++k) {
         const uint64_t u = base + uint64_t(k) * blockDim.x;
-        idx[k] = u < units ? expand_index(u * 2, map) : ~uint64_t(0);
+        idx[k] = u < units ? expand_nz<NZ>(u * 2, map) : ~uint64_t(0);
         if (u < units) {
             x0[k] = *reinterpret_cast<const float4*>(a + (idx[k] | o0));
             x1[k] = *reinterpret_cast<const float4*>(a + (idx[k] | o1));
@@ -100,7 +102,7 @@ k_pair_vec2(float2* __restrict__ a, uint64_t units, IndexMap map, uint64_t o0, u
 }
 
 // complex64, pair members are the neighbours (i, i+1): one float4 per unit.
-template <int U>
+template <int U, int NZ>
 __global__ void __launch_bounds__(kThreads)
 k_pair_adj(float2* __restrict__ a, uint64_t units, IndexMap map, Mat2<float2> m)
 {
@@ -110,7 +112,7 @@ k_pair_adj(float2* __restrict__ a, uint64_t units, IndexMap map, Mat2<float2> m)
 #pragma unroll
     for (int k = 0; k < U; ++k) {
         const uint64_t u = base + uint64_t(k) * blockDim.x;
-        idx[k] = u < units ? expand_index(u, map) : ~uint64_t(0);
+        idx[k] = u < units ? expand_nz<NZ>(u, map) : ~uint64_t(0);
         if (u < units) x[k] = *reinterpret_cast<const float4*>(a + idx[k]);
     }
 #pragma unroll
@@ -140,7 +142,7 @@ __device__ __forceinline__ T unit_times(int u, T x)
 }
 
 // out0 = u0 * x[s0], out1 = u1 * x[s1] (s0 != s1)
-template <typename T, int U>
+template <typename T, int U, int NZ>
 __global__ void __launch_bounds__(kThreads)
 k_pair_mono(T* __restrict__ a, uint64_t units, IndexMap map, uint64_t o0, uint64_t o1, int swap, int u0, int u1)
 {
@@ -150,7 +152,7 @@ k_pair_mono(T* __restrict__ a, uint64_t units, IndexMap map, uint64_t o0, uint64
 #pragma unroll
     for (int k = 0; k < U; ++k) {
         const uint64_t u = base + uint64_t(k) * blockDim.x;
-        idx[k] = u < units ? expand_index(u, map) : ~uint64_t(0);
+        idx[k] = u < units ? expand_nz<NZ>(u, map) : ~uint64_t(0);
         if (u < units) {
             x0[k] = a[idx[k] | o0];
             x1[k] = a[idx[k] | o1];
@@ -167,8 +169,12 @@ k_pair_mono(T* __restrict__ a, uint64_t units, IndexMap map, uint64_t o0, uint64
 
 // ------------------------------------- complex128 without the FP64 pipe
 
+// Coefficients of out_j = m_j0 x0 + m_j1 x1 for the packed dot products:
+// lane 0 is Re out_j, lane 1 Im out_j, with terms
+//   k=0: (m_j0r, m_j0r) * (x0r, x0i)    k=1: (m_j1r, m_j1r) * (x1r, x1i)
+//   k=2: (-m_j0i, m_j0i) * (x0i, x0r)   k=3: (-m_j1i, m_j1i) * (x1i, x1r)
 struct Mat2DF {
-    DF re[4], im[4];   // m00, m01, m10, m11
+    float2 h[2][4], l[2][4];
 };
 
 __host__ inline DF host_split(double v)
@@ -186,7 +192,7 @@ __host__ inline DF host_split(double v)
 
 // out0 = m00 x0 + m01 x1, out1 = m10 x0 + m11 x1 on double-float pairs; a
 // unit with an amplitude outside the split's range is done in FP64 (md).
-template <int U>
+template <int U, int NZ>
 __global__ void __launch_bounds__(kThreads)
 k_pair_c128x(double2* __restrict__ a, uint64_t units, IndexMap map, uint64_t o0, uint64_t o1, Mat2DF m,
              Mat2<double2> md)
@@ -198,7 +204,7 @@ k_pair_c128x(double2* __restrict__ a, uint64_t units, IndexMap map, uint64_t o0,
 #pragma unroll
     for (int k = 0; k < U; ++k) {
         const uint64_t u = base + uint64_t(k) * blockDim.x;
-        idx[k] = u < units ? expand_index(u, map) : ~uint64_t(0);
+        idx[k] = u < units ? expand_nz<NZ>(u, map) : ~uint64_t(0);
         if (u < units) {
             x0[k] = ab[idx[k] | o0];
             x1[k] = ab[idx[k] | o1];
@@ -208,17 +214,27 @@ k_pair_c128x(double2* __restrict__ a, uint64_t units, IndexMap map, uint64_t o0,
     for (int k = 0; k < U; ++k) {
         if (idx[k] == ~uint64_t(0)) continue;
         DF v[4];   // x0.re, x0.im, x1.re, x1.im
-        const bool ok = split_f64(x0[k].x, v[0]) & split_f64(x0[k].y, v[1]) & split_f64(x1[k].x, v[2]) &
-                        split_f64(x1[k].y, v[3]);
+        bool ok;
+        if (split_fast_ok(x0[k].x) & split_fast_ok(x0[k].y) & split_fast_ok(x1[k].x) & split_fast_ok(x1[k].y)) {
+            v[0] = split_fast(x0[k].x);
+            v[1] = split_fast(x0[k].y);
+            v[2] = split_fast(x1[k].x);
+            v[3] = split_fast(x1[k].y);
+            ok = true;
+        } else {
+            ok = split_f64(x0[k].x, v[0]) & split_f64(x0[k].y, v[1]) & split_f64(x1[k].x, v[2]) &
+                 split_f64(x1[k].y, v[3]);
+        }
         if (ok) {
-            const DF nim0{-m.im[0].h, -m.im[0].l}, nim1{-m.im[1].h, -m.im[1].l};
-            const DF nim2{-m.im[2].h, -m.im[2].l}, nim3{-m.im[3].h, -m.im[3].l};
-            const DF ar0[4] = {m.re[0], nim0, m.re[1], nim1}, br0[4] = {v[0], v[1], v[2], v[3]};
-            const DF ai0[4] = {m.re[0], m.im[0], m.re[1], m.im[1]}, bi[4] = {v[1], v[0], v[3], v[2]};
-            const DF ar1[4] = {m.re[2], nim2, m.re[3], nim3};
-            const DF ai1[4] = {m.re[2], m.im[2], m.re[3], m.im[3]};
-            ab[idx[k] | o0] = make_ulonglong2(join_f64(dot<4>(ar0, br0)), join_f64(dot<4>(ai0, bi)));
-            ab[idx[k] | o1] = make_ulonglong2(join_f64(dot<4>(ar1, br0)), join_f64(dot<4>(ai1, bi)));
+            const float2 bh[4] = {make_float2(v[0].h, v[1].h), make_float2(v[2].h, v[3].h),
+                                  make_float2(v[1].h, v[0].h), make_float2(v[3].h, v[2].h)};
+            const float2 bl[4] = {make_float2(v[0].l, v[1].l), make_float2(v[2].l, v[3].l),
+                                  make_float2(v[1].l, v[0].l), make_float2(v[3].l, v[2].l)};
+            float2 h0, l0, h1, l1;
+            dot_x2<4>(m.h[0], m.l[0], bh, bl, h0, l0);
+            dot_x2<4>(m.h[1], m.l[1], bh, bl, h1, l1);
+            ab[idx[k] | o0] = make_ulonglong2(join_f64(DF{h0.x, l0.x}), join_f64(DF{h0.y, l0.y}));
+            ab[idx[k] | o1] = make_ulonglong2(join_f64(DF{h1.x, l1.x}), join_f64(DF{h1.y, l1.y}));
         } else {
             const double2 y0 = *reinterpret_cast<const double2*>(&x0[k]);
             const double2 y1 = *reinterpret_cast<const double2*>(&x1[k]);
@@ -230,7 +246,7 @@ k_pair_c128x(double2* __restrict__ a, uint64_t units, IndexMap map, uint64_t o0,
 
 // --------------------------------------------------------------- PHASE
 
-template <typename T, int U>
+template <typename T, int U, int NZ>
 __global__ void __launch_bounds__(kThreads)
 k_phase(T* __restrict__ a, uint64_t units, IndexMap map, T ph)
 {
@@ -240,7 +256,7 @@ k_phase(T* __restrict__ a, uint64_t units, IndexMap map, T ph)
 #pragma unroll
     for (int k = 0; k < U; ++k) {
         const uint64_t u = base + uint64_t(k) * blockDim.x;
-        idx[k] = u < units ? expand_index(u, map) : ~uint64_t(0);
+        idx[k] = u < units ? expand_nz<NZ>(u, map) : ~uint64_t(0);
         if (u < units) x[k] = a[idx[k]];
     }
 #pragma unroll
@@ -248,7 +264,7 @@ k_phase(T* __restrict__ a, uint64_t units, IndexMap map, T ph)
         if (idx[k] != ~uint64_t(0)) a[idx[k]] = cmul(ph, x[k]);
 }
 
-template <int U>
+template <int U, int NZ>
 __global__ void __launch_bounds__(kThreads)
 k_phase_vec2(float2* __restrict__ a, uint64_t units, IndexMap map, float2 ph)
 {
@@ -258,7 +274,7 @@ k_phase_vec2(float2* __restrict__ a, uint64_t units, IndexMap map, float2 ph)
 #pragma unroll
     for (int k = 0; k < U; ++k) {
         const uint64_t u = base + uint64_t(k) * blockDim.x;
-        idx[k] = u < units ? expand_index(u * 2, map) : ~uint64_t(0);
+        idx[k] = u < units ? expand_nz<NZ>(u * 2, map) : ~uint64_t(0);
         if (u < units) x[k] = *reinterpret_cast<const float4*>(a + idx[k]);
     }
 #pragma unroll
@@ -271,7 +287,7 @@ k_phase_vec2(float2* __restrict__ a, uint64_t units, IndexMap map, float2 ph)
 }
 
 // x -> u x for a unit u in {1, i, -1, -i} (code as unit_times)
-template <typename T, int U>
+template <typename T, int U, int NZ>
 __global__ void __launch_bounds__(kThreads)
 k_phase_mono(T* __restrict__ a, uint64_t units, IndexMap map, int code)
 {
@@ -281,7 +297,7 @@ k_phase_mono(T* __restrict__ a, uint64_t units, IndexMap map, int code)
 #pragma unroll
     for (int k = 0; k < U; ++k) {
         const uint64_t u = base + uint64_t(k) * blockDim.x;
-        idx[k] = u < units ? expand_index(u, map) : ~uint64_t(0);
+        idx[k] = u < units ? expand_nz<NZ>(u, map) : ~uint64_t(0);
         if (u < units) x[k] = a[idx[k]];
     }
 #pragma unroll
@@ -290,7 +306,7 @@ k_phase_mono(T* __restrict__ a, uint64_t units, IndexMap map, int code)
 }
 
 // complex128 phase on double-float pairs (FP64 for out-of-range amplitudes)
-template <int U>
+template <int U, int NZ>
 __global__ void __launch_bounds__(kThreads)
 k_phase_c128x(double2* __restrict__ a, uint64_t units, IndexMap map, DF pr, DF pi, double2 pd)
 {
@@ -301,17 +317,30 @@ k_phase_c128x(double2* __restrict__ a, uint64_t units, IndexMap map, DF pr, DF p
 #pragma unroll
     for (int k = 0; k < U; ++k) {
         const uint64_t u = base + uint64_t(k) * blockDim.x;
-        idx[k] = u < units ? expand_index(u, map) : ~uint64_t(0);
+        idx[k] = u < units ? expand_nz<NZ>(u, map) : ~uint64_t(0);
         if (u < units) x[k] = ab[idx[k]];
     }
 #pragma unroll
     for (int k = 0; k < U; ++k) {
         if (idx[k] == ~uint64_t(0)) continue;
         DF v[2];
-        if (split_f64(x[k].x, v[0]) & split_f64(x[k].y, v[1])) {
-            const DF ar[2] = {pr, DF{-pi.h, -pi.l}}, ai[2] = {pr, pi};
-            const DF br[2] = {v[0], v[1]}, bi[2] = {v[1], v[0]};
-            ab[idx[k]] = make_ulonglong2(join_f64(dot<2>(ar, br)), join_f64(dot<2>(ai, bi)));
+        bool ok;
+        if (split_fast_ok(x[k].x) & split_fast_ok(x[k].y)) {
+            v[0] = split_fast(x[k].x);
+            v[1] = split_fast(x[k].y);
+            ok = true;
+        } else {
+            ok = split_f64(x[k].x, v[0]) & split_f64(x[k].y, v[1]);
+        }
+        if (ok) {
+            // lane 0: pr xr - pi xi, lane 1: pr xi + pi xr
+            const float2 ah[2] = {make_float2(pr.h, pr.h), make_float2(-pi.h, pi.h)};
+            const float2 al[2] = {make_float2(pr.l, pr.l), make_float2(-pi.l, pi.l)};
+            const float2 bh[2] = {make_float2(v[0].h, v[1].h), make_float2(v[1].h, v[0].h)};
+            const float2 bl[2] = {make_float2(v[0].l, v[1].l), make_float2(v[1].l, v[0].l)};
+            float2 h, l;
+            dot_x2<2>(ah, al, bh, bl, h, l);
+            ab[idx[k]] = make_ulonglong2(join_f64(DF{h.x, l.x}), join_f64(DF{h.y, l.y}));
         } else {
             a[idx[k]] = cmul(pd, *reinterpret_cast<const double2*>(&x[k]));
         }
@@ -350,6 +379,19 @@ k_dense(T* __restrict__ a, uint64_t units, IndexMap map, DenseOffsets offs, cons
 }
 
 constexpr int kUnroll = 4;
+
+// Calls f with a compile-time map size: the exact count for 1-3 zero
+// positions, 0 (generic) otherwise.
+template <typename F>
+void with_nz(int nz, F&& f)
+{
+    switch (nz) {
+        case 1: f(std::integral_constant<int, 1>{}); break;
+        case 2: f(std::integral_constant<int, 2>{}); break;
+        case 3: f(std::integral_constant<int, 3>{}); break;
+        default: f(std::integral_constant<int, 0>{}); break;
+    }
+}
 
 inline unsigned grid_for(uint64_t units, int per_block)
 {
@@ -394,42 +436,49 @@ cudaError_t launch_pair(void* amps, int prec, uint64_t total, const IndexMap& ma
 {
     const uint64_t pairs = total >> map.nz;
     if (pairs == 0) return cudaSuccess;
+    const unsigned grid = grid_for(pairs, kThreads * kUnroll);
     int swap = 0, u0 = 0, u1 = 0;
-    if (mono_pair(m, swap, u0, u1)) {
-        if (prec == kC128)
-            k_pair_mono<double2, kUnroll><<<grid_for(pairs, kThreads * kUnroll), kThreads, 0, st>>>(
-                (double2*)amps, pairs, map, o0, o1, swap, u0, u1);
-        else
-            k_pair_mono<float2, kUnroll><<<grid_for(pairs, kThreads * kUnroll), kThreads, 0, st>>>(
-                (float2*)amps, pairs, map, o0, o1, swap, u0, u1);
-        return cudaGetLastError();
-    }
-    if (prec == kC128 && fp64_exact) {
-        k_pair<double2, kUnroll><<<grid_for(pairs, kThreads * kUnroll), kThreads, 0, st>>>(
-            (double2*)amps, pairs, map, o0, o1, make_mat2<double2>(m));
-    } else if (prec == kC128) {
-        Mat2DF mx;
-        for (int e = 0; e < 4; ++e) {
-            mx.re[e] = host_split(m[2 * e]);
-            mx.im[e] = host_split(m[2 * e + 1]);
+    const bool mono = mono_pair(m, swap, u0, u1);
+    Mat2DF mx{};
+    if (!mono && prec == kC128 && !fp64_exact)
+        for (int j = 0; j < 2; ++j) {
+            const DF r0 = host_split(m[4 * j]), i0 = host_split(m[4 * j + 1]);
+            const DF r1 = host_split(m[4 * j + 2]), i1 = host_split(m[4 * j + 3]);
+            const DF c[4][2] = {{r0, r0}, {r1, r1}, {DF{-i0.h, -i0.l}, i0}, {DF{-i1.h, -i1.l}, i1}};
+            for (int k = 0; k < 4; ++k) {
+                mx.h[j][k] = make_float2(c[k][0].h, c[k][1].h);
+                mx.l[j][k] = make_float2(c[k][0].l, c[k][1].l);
+            }
         }
-        k_pair_c128x<kUnroll><<<grid_for(pairs, kThreads * kUnroll), kThreads, 0, st>>>(
-            (double2*)amps, pairs, map, o0, o1, mx, make_mat2<double2>(m));
-    } else {
-        auto mm = make_mat2<float2>(m);
-        const bool pos0_free = map.nz == 0 || map.zpos[0] > 0;
-        if (pos0_free && (map.setmask & 1) == 0 && ((o0 | o1) & 1) == 0 && pairs >= 2) {
-            const uint64_t units = pairs / 2;
-            k_pair_vec2<kUnroll><<<grid_for(units, kThreads * kUnroll), kThreads, 0, st>>>(
-                (float2*)amps, units, map, o0, o1, mm);
-        } else if (o0 == 0 && o1 == 1 && (map.setmask & 1) == 0) {
-            k_pair_adj<kUnroll><<<grid_for(pairs, kThreads * kUnroll), kThreads, 0, st>>>(
-                (float2*)amps, pairs, map, mm);
+    with_nz(map.nz, [&](auto nzc) {
+        constexpr int NZ = decltype(nzc)::value;
+        if (mono) {
+            if (prec == kC128)
+                k_pair_mono<double2, kUnroll, NZ><<<grid, kThreads, 0, st>>>((double2*)amps, pairs, map, o0, o1,
+                                                                            swap, u0, u1);
+            else
+                k_pair_mono<float2, kUnroll, NZ><<<grid, kThreads, 0, st>>>((float2*)amps, pairs, map, o0, o1, swap,
+                                                                           u0, u1);
+        } else if (prec == kC128 && fp64_exact) {
+            k_pair<double2, kUnroll, NZ><<<grid, kThreads, 0, st>>>((double2*)amps, pairs, map, o0, o1,
+                                                                   make_mat2<double2>(m));
+        } else if (prec == kC128) {
+            k_pair_c128x<kUnroll, NZ><<<grid, kThreads, 0, st>>>((double2*)amps, pairs, map, o0, o1, mx,
+                                                                make_mat2<double2>(m));
         } else {
-            k_pair<float2, kUnroll><<<grid_for(pairs, kThreads * kUnroll), kThreads, 0, st>>>(
-                (float2*)amps, pairs, map, o0, o1, mm);
+            auto mm = make_mat2<float2>(m);
+            const bool pos0_free = map.nz == 0 || map.zpos[0] > 0;
+            if (pos0_free && (map.setmask & 1) == 0 && ((o0 | o1) & 1) == 0 && pairs >= 2) {
+                const uint64_t units = pairs / 2;
+                k_pair_vec2<kUnroll, NZ><<<grid_for(units, kThreads * kUnroll), kThreads, 0, st>>>(
+                    (float2*)amps, units, map, o0, o1, mm);
+            } else if (o0 == 0 && o1 == 1 && (map.setmask & 1) == 0) {
+                k_pair_adj<kUnroll, NZ><<<grid, kThreads, 0, st>>>((float2*)amps, pairs, map, mm);
+            } else {
+                k_pair<float2, kUnroll, NZ><<<grid, kThreads, 0, st>>>((float2*)amps, pairs, map, o0, o1, mm);
+            }
         }
-    }
+    });
     return cudaGetLastError();
 }
 
@@ -438,32 +487,32 @@ cudaError_t launch_phase(void* amps, int prec, uint64_t total, const IndexMap& m
 {
     const uint64_t units = total >> map.nz;
     if (units == 0) return cudaSuccess;
+    const unsigned grid = grid_for(units, kThreads * kUnroll);
     const int code = unit_code(ph_re, ph_im);
-    if (code >= 0) {
-        if (prec == kC128)
-            k_phase_mono<double2, kUnroll><<<grid_for(units, kThreads * kUnroll), kThreads, 0, st>>>(
-                (double2*)amps, units, map, code);
-        else
-            k_phase_mono<float2, kUnroll><<<grid_for(units, kThreads * kUnroll), kThreads, 0, st>>>(
-                (float2*)amps, units, map, code);
-        return cudaGetLastError();
-    }
-    if (prec == kC128 && fp64_exact) {
-        k_phase<double2, kUnroll><<<grid_for(units, kThreads * kUnroll), kThreads, 0, st>>>(
-            (double2*)amps, units, map, make_double2(ph_re, ph_im));
-    } else if (prec == kC128) {
-        k_phase_c128x<kUnroll><<<grid_for(units, kThreads * kUnroll), kThreads, 0, st>>>(
-            (double2*)amps, units, map, host_split(ph_re), host_split(ph_im), make_double2(ph_re, ph_im));
-    } else {
-        const bool pos0_free = map.nz == 0 || map.zpos[0] > 0;
-        if (pos0_free && (map.setmask & 1) == 0 && units >= 2) {
-            k_phase_vec2<kUnroll><<<grid_for(units / 2, kThreads * kUnroll), kThreads, 0, st>>>(
-                (float2*)amps, units / 2, map, make_float2((float)ph_re, (float)ph_im));
+    with_nz(map.nz, [&](auto nzc) {
+        constexpr int NZ = decltype(nzc)::value;
+        if (code >= 0) {
+            if (prec == kC128)
+                k_phase_mono<double2, kUnroll, NZ><<<grid, kThreads, 0, st>>>((double2*)amps, units, map, code);
+            else
+                k_phase_mono<float2, kUnroll, NZ><<<grid, kThreads, 0, st>>>((float2*)amps, units, map, code);
+        } else if (prec == kC128 && fp64_exact) {
+            k_phase<double2, kUnroll, NZ><<<grid, kThreads, 0, st>>>((double2*)amps, units, map,
+                                                                    make_double2(ph_re, ph_im));
+        } else if (prec == kC128) {
+            k_phase_c128x<kUnroll, NZ><<<grid, kThreads, 0, st>>>((double2*)amps, units, map, host_split(ph_re),
+                                                                 host_split(ph_im), make_double2(ph_re, ph_im));
         } else {
-            k_phase<float2, kUnroll><<<grid_for(units, kThreads * kUnroll), kThreads, 0, st>>>(
-                (float2*)amps, units, map, make_float2((float)ph_re, (float)ph_im));
+            const bool pos0_free = map.nz == 0 || map.zpos[0] > 0;
+            if (pos0_free && (map.setmask & 1) == 0 && units >= 2) {
+                k_phase_vec2<kUnroll, NZ><<<grid_for(units / 2, kThreads * kUnroll), kThreads, 0, st>>>(
+                    (float2*)amps, units / 2, map, make_float2((float)ph_re, (float)ph_im));
+            } else {
+                k_phase<float2, kUnroll, NZ><<<grid, kThreads, 0, st>>>((float2*)amps, units, map,
+                                                                       make_float2((float)ph_re, (float)ph_im));
+            }
         }
-    }
+    });
     return cudaGetLastError();
 }
 
