@@ -36,15 +36,18 @@
 //            amplitudes from the stage, writes hi/lo to its group's A columns
 //            with tcgen05.st, one thread issues the MMAs, and after the commit
 //            each thread reads its row of D with tcgen05.ld and writes the
-//            new amplitudes back into the stage.  (Two warps per lane quarter,
-//            each with half a row, measured no faster: the TMEM stores of the
-//            split, not per-thread latency, bound this phase.)  While one group waits for
+//            new amplitudes back into the stage.  While one group waits for
 //            its MMAs the other converts or writes back, so the tensor pipe,
-//            the ALUs and the copy engine work at the same time.
-// TMEM (512 columns): group g uses 256g + [0,64) A_hi, [64,128) A_lo,
-// [128,192) D_main, [192,256) D_corr.  Every wait is bounded (in wall-clock
-// time, %globaltimer); on expiry the CTA records an error, lets its copies
-// land and releases its TMEM before returning.
+//            the ALUs and the copy engine work at the same time.  The split's
+//            TMEM stores (64 KB per tile and block) bound two-block passes;
+//            two warps per lane quarter, or one 64-column store instead of
+//            two 32-column stores, measured no faster.
+// TMEM (512 columns): group g uses 256g + [0,128) for A (K-step s: A_hi in
+// columns 16s..16s+7, A_lo in 16s+8..16s+15, so that a thread writes its
+// half row with one 64-column store), [128,192) D_main, [192,256) D_corr.
+// Every wait is bounded (in wall-clock time, %globaltimer); on expiry the CTA
+// records an error, lets its copies land and releases its TMEM before
+// returning.
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -188,6 +191,16 @@ __device__ __forceinline__ void tmem_st32(uint32_t taddr, const float* v)
         : "memory");
 }
 
+// 64 columns from 32 hi and 32 lo values of this thread's lane, interleaved
+// per K-step of 8: hi[8s..8s+7] then lo[8s..8s+7] for s = 0..3.
+__device__ __forceinline__ void tmem_st64_hilo(uint32_t taddr, const float* hi, const float* lo)
+{
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x64.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63,%64};" ::"r"(taddr),
+        "f"(hi[0]), "f"(hi[1]), "f"(hi[2]), "f"(hi[3]), "f"(hi[4]), "f"(hi[5]), "f"(hi[6]), "f"(hi[7]), "f"(lo[0]), "f"(lo[1]), "f"(lo[2]), "f"(lo[3]), "f"(lo[4]), "f"(lo[5]), "f"(lo[6]), "f"(lo[7]), "f"(hi[8]), "f"(hi[9]), "f"(hi[10]), "f"(hi[11]), "f"(hi[12]), "f"(hi[13]), "f"(hi[14]), "f"(hi[15]), "f"(lo[8]), "f"(lo[9]), "f"(lo[10]), "f"(lo[11]), "f"(lo[12]), "f"(lo[13]), "f"(lo[14]), "f"(lo[15]), "f"(hi[16]), "f"(hi[17]), "f"(hi[18]), "f"(hi[19]), "f"(hi[20]), "f"(hi[21]), "f"(hi[22]), "f"(hi[23]), "f"(lo[16]), "f"(lo[17]), "f"(lo[18]), "f"(lo[19]), "f"(lo[20]), "f"(lo[21]), "f"(lo[22]), "f"(lo[23]), "f"(hi[24]), "f"(hi[25]), "f"(hi[26]), "f"(hi[27]), "f"(hi[28]), "f"(hi[29]), "f"(hi[30]), "f"(hi[31]), "f"(lo[24]), "f"(lo[25]), "f"(lo[26]), "f"(lo[27]), "f"(lo[28]), "f"(lo[29]), "f"(lo[30]), "f"(lo[31])
+        : "memory");
+}
+
 __device__ __forceinline__ void mbar_arrive(uint32_t bar)
 {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
@@ -292,8 +305,8 @@ __device__ __forceinline__ void split_tf32(float x, float& hi, float& lo)
     lo = to_tf32((x - hi) * kLoScale);
 }
 
-// Gates 16*HH .. 16*HH+15 of row `rowb` -> hi/lo operands (columns
-// 32*HH.. of A_hi and 64+32*HH.. of A_lo at TMEM address tl).
+// Gates 16*HH .. 16*HH+15 of row `rowb` -> hi/lo operands: K-steps
+// 4*HH .. 4*HH+3, each 8 hi columns then 8 lo columns, at TMEM address tl.
 template <int HH>
 __device__ __forceinline__ void split_half(const uint8_t* raw, uint32_t rowb, const TcBlockGeom& G, uint32_t tl)
 {
@@ -315,8 +328,7 @@ __device__ __forceinline__ void split_half(const uint8_t* raw, uint32_t rowb, co
             split_tf32(v.y, hi[2 * j + 1], lo[2 * j + 1]);
         }
     }
-    tmem_st32(tl + 32u * HH, hi);
-    tmem_st32(tl + 64u + 32u * HH, lo);
+    tmem_st64_hilo(tl + 64u * HH, hi, lo);
 }
 
 // D = D_main + 2^-11 D_corr for gates 16*HH .. 16*HH+15 of row `rowb`, back
@@ -511,12 +523,12 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, const __grid_constant__ Inde
                     // [D_main | D_corr] = A_hi [B_hi; B_lo']^T, then D_corr += A_lo' B_hi^T
 #pragma unroll
                     for (int ks = 0; ks < 8; ++ks)
-                        mma_tf32_ts(tm + 128u, tm + 8u * ks,
+                        mma_tf32_ts(tm + 128u, tm + 16u * ks,
                                     desc_sw128(bb + (uint32_t)(ks >> 2) * kBAtom + (uint32_t)(ks & 3) * 32u),
                                     kIdescN128, ks > 0 ? 1u : 0u);
 #pragma unroll
                     for (int ks = 0; ks < 8; ++ks)
-                        mma_tf32_ts(tm + 192u, tm + 64u + 8u * ks,
+                        mma_tf32_ts(tm + 192u, tm + 16u * ks + 8u,
                                     desc_sw128(bb + (uint32_t)(ks >> 2) * kBAtom + (uint32_t)(ks & 3) * 32u),
                                     kIdescN64, 1u);
                     mma_commit(mbar);
