@@ -72,8 +72,10 @@ def test_other_errors_raise():
 
 @pytest.mark.gpu
 def test_binding_example_refparam_reexecute():
-    """python/test.py with a reassigned RefParam: the next execution uses
-    the new angle; a plain float bound at build time does not change."""
+    """python/test.py: reexecute() continues from the previous state
+    (python/q1tsim.py:483-490).  With the RefParam reassigned to -1.23 the
+    second RX undoes the first: every run reads 0.  A plain float bound at
+    build time does not change: RX(1.23) twice, P(1) = sin^2(1.23)."""
     shots = 20000
     ang = q1tsim.RefParam(1.23)
     with q1tsim.Circuit(1, 1) as c:
@@ -83,18 +85,17 @@ def test_binding_example_refparam_reexecute():
         h = c.histogram()
         assert set(h) <= {"0", "1"} and sum(h.values()) == shots
         assert measurement_ok(h.get("1", 0), shots, math.sin(1.23 / 2) ** 2, 1e-6)
-        ang.assign(2.9)
+        ang.assign(-1.23)
         c.reexecute()
-        h = c.histogram()
-        assert measurement_ok(h.get("1", 0), shots, math.sin(2.9 / 2) ** 2, 1e-6)
+        assert c.histogram() == {"0": shots}
     val = 1.23
     with q1tsim.Circuit(1, 1) as c:
         c.rx(val, 0)
         c.peek(0, 0)
         c.execute(shots)
-        val = 2.9     # rebinding the name changes nothing
+        val = -1.23     # rebinding the name changes nothing
         c.reexecute()
-        assert measurement_ok(c.histogram().get("1", 0), shots, math.sin(1.23 / 2) ** 2, 1e-6)
+        assert measurement_ok(c.histogram().get("1", 0), shots, math.sin(1.23) ** 2, 1e-6)
 
 
 @pytest.mark.gpu
