@@ -77,8 +77,15 @@ __device__ double block_scan_excl(double* data, uint64_t n, double* wsum)
     return carry;
 }
 
-// Smallest k with Binomial(n, p) CDF(k) > u; the host's binomial_inv.
-__device__ uint64_t binomial_inv_dev(uint64_t n, double p, double u)
+// Smallest k with Binomial(n, p) CDF(k) > u; the host's binomial_inv.  The
+// CTA evaluates the probability terms of up to kBinomChunk consecutive k in
+// parallel into `terms`; thread 0 then accumulates them in ascending k, the
+// same sums in the same order as the one-thread loop, so the same k.  Called
+// by every thread of the CTA with the same arguments.
+constexpr int kBinomChunk = 4096;
+static_assert(kBinomChunk <= kBatchWarps * (1 << kBatchTileBits), "the terms fit in the tile stage");
+
+__device__ uint64_t binomial_inv_block(uint64_t n, double p, double u, double* terms, uint64_t* s_k)
 {
     if (n == 0 || p <= 0.0) return 0;
     if (p >= 1.0) return n;
@@ -91,15 +98,80 @@ __device__ uint64_t binomial_inv_dev(uint64_t n, double p, double u)
     const uint64_t hi = hi_d > nn ? n : (uint64_t)hi_d;
     const double lp = log(p), lq = log1p(-p);
     const double lnf = lgamma(nn + 1.0);
-    double cdf = 0.0;
-    for (uint64_t k = lo; k <= hi; ++k) {
-        const double kk = (double)k;
-        cdf += exp(lnf - lgamma(kk + 1.0) - lgamma(nn - kk + 1.0) + kk * lp + (nn - kk) * lq);
-        if (u < cdf) return k;
+    double cdf = 0.0;   // thread 0's running sum
+    for (uint64_t k0 = lo; k0 <= hi; k0 += kBinomChunk) {
+        const uint64_t cnt = hi - k0 + 1 < (uint64_t)kBinomChunk ? hi - k0 + 1 : (uint64_t)kBinomChunk;
+        for (uint64_t j = threadIdx.x; j < cnt; j += kBatchThreads) {
+            const double kk = (double)(k0 + j);
+            terms[j] = exp(lnf - lgamma(kk + 1.0) - lgamma(nn - kk + 1.0) + kk * lp + (nn - kk) * lq);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint64_t found = ~uint64_t(0);
+            for (uint64_t j = 0; j < cnt; ++j) {
+                cdf += terms[j];
+                if (u < cdf) {
+                    found = k0 + j;
+                    break;
+                }
+            }
+            *s_k = found;
+        }
+        __syncthreads();
+        const uint64_t f = *s_k;
+        __syncthreads();
+        if (f != ~uint64_t(0)) return f;
     }
     return hi;
 }
 
+// 8- and 16-byte asynchronous copies global -> shared, committed in groups;
+// the issuing lane's copies of all but the newest N groups are complete
+// after cp_async_wait_group<N>
+__device__ __forceinline__ void cp_async8(float2* smem, const float2* gmem)
+{
+    const uint32_t sa = (uint32_t)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async16(float2* smem, const float2* gmem)
+{
+    const uint32_t sa = (uint32_t)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait_group() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// Shared-memory load of a 32-bit value that the compiler may not hoist out of
+// its loop.
+__device__ __forceinline__ uint32_t lds_u32(const uint32_t* p)
+{
+    uint32_t v;
+    asm volatile("ld.shared.u32 %0, [%1];\n" : "=r"(v) : "r"((uint32_t)__cvta_generic_to_shared(p)));
+    return v;
+}
+
+// Shared-memory load of one matrix entry (re, im), kept at its use: a plain
+// load of the (loop-invariant) matrix would be hoisted out of the tile loop
+// into as many registers as the matrix has entries.  All lanes read the same
+// entry, so the load is one broadcast wavefront.
+__device__ __forceinline__ float2 lds_entry(const float2* p)
+{
+    float2 v;
+    const uint32_t sa = (uint32_t)__cvta_generic_to_shared(p);
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];\n" : "=f"(v.x), "=f"(v.y) : "r"(sa));
+    return v;
+}
+
+// Complex products on packed FP32x2 FMAs with the matrix entry m = (re, im)
+// as one operand: with xa = (x.re, x.re) and xb = (x.im, x.im),
+//   a += xa * m = (x.re m.re, x.re m.im),  b += xb * m = (x.im m.re, x.im m.im),
+// and sum m x = (a.x - b.y, a.y + b.x).  An entry is read as 8 bytes and
+// serves every unit a lane holds; the inputs are duplicated once per unit.
+__device__ __forceinline__ float2 cdot_out(float2 a, float2 b) { return make_float2(a.x - b.y, a.y + b.x); }
+
+// States below kBatchTileBits qubits: one unit (the 2^TB amplitudes a
+// block mixes) per thread.  mat[r * D + s] is the block's entry (r, s).
 template <int TB>
 __device__ void dense_pass(float2* a, uint64_t n_amps, const BatchOp& op, const float2* mat)
 {
@@ -107,21 +179,182 @@ __device__ void dense_pass(float2* a, uint64_t n_amps, const BatchOp& op, const 
     const uint64_t units = n_amps >> op.map.nz;
     for (uint64_t u = threadIdx.x; u < units; u += kBatchThreads) {
         const uint64_t i = expand_index(u, op.map);
-        float2 x[D];
+        float2 xa[D], xb[D];
 #pragma unroll
-        for (int s = 0; s < D; ++s) x[s] = a[i | op.offs[s]];
+        for (int s = 0; s < D; ++s) {
+            const float2 v = a[i | op.offs[s]];
+            xa[s] = make_float2(v.x, v.x);
+            xb[s] = make_float2(v.y, v.y);
+        }
 #pragma unroll
         for (int r = 0; r < D; ++r) {
-            float2 acc = cmul(mat[r * D], x[0]);
+            float2 ac = make_float2(0.f, 0.f), bc = make_float2(0.f, 0.f);
 #pragma unroll
-            for (int s = 1; s < D; ++s) {
-                const float2 m = mat[r * D + s];
-                acc.x += m.x * x[s].x - m.y * x[s].y;
-                acc.y += m.x * x[s].y + m.y * x[s].x;
+            for (int s = 0; s < D; ++s) {
+                const float2 e = lds_entry(mat + r * D + s);
+                ac = __ffma2_rn(xa[s], e, ac);
+                bc = __ffma2_rn(xb[s], e, bc);
             }
-            a[i | op.offs[r]] = acc;
+            a[i | op.offs[r]] = cdot_out(ac, bc);
         }
     }
+}
+
+// States of kBatchTileBits qubits or more: each warp streams tiles of 1024
+// amplitudes (BatchOp::tiled).  Slot m of lane l is amplitude
+// tile_base + goff(m) + l, goff(m) = OR of gbit[b] over the set bits b of m,
+// so every copy and store instruction of the warp moves whole runs of 256
+// contiguous bytes whatever the gate positions.  A tile is copied
+// asynchronously into the warp's 8 KB stage at the swizzled offsets
+// soff(m) ^ soff(l) (soff is linear: XOR of sbit[b]); where the layout keeps
+// amplitude pairs (2i, 2i+1) adjacent (BatchOp::pairs16) a lane moves 16
+// bytes at a time, two slots per instruction.  Each lane then applies the
+// block to 32 / 2^TB units, KB units and RB output rows at a time, so that
+// one matrix entry read serves KB units and 2 * KB * RB FMA chains are in
+// flight.  Sixteen warps per SM overlap one another's copies, arithmetic and
+// stores.
+template <int TB>
+__device__ void tiled_pass(float2* a, uint64_t n_amps, const BatchOp& op, const float2* mat, float2* stage)
+{
+    constexpr int D = 1 << TB;
+    constexpr int U = 32 >> TB;
+    constexpr int KB = U < 2 ? U : 2;
+    constexpr int RB = TB >= 3 ? 2 : 1;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint64_t tiles = n_amps >> kBatchTileBits;
+    const uint32_t plane = (uint32_t)(lane & 15) ^ ((lane & 16) ? op.lane16 : 0u);
+    // 16-byte form: lane l moves amplitudes 2i, 2i+1 (i = l & 15) of slots 2mm + (l >> 4)
+    const uint32_t p16 = (uint32_t)((2 * lane) & 15) ^ ((lane & 8) ? op.lane16 : 0u);
+    uint32_t pl = 0;
+#pragma unroll
+    for (int b = 0; b < 5; ++b)
+        if ((lane >> b) & 1) pl ^= op.wbit[b];
+
+    for (uint64_t t = (uint64_t)warp; t < tiles; t += kBatchWarps) {
+        // slot offsets from the five basis values, read per tile (volatile)
+        // so that the 64 derived offsets are not kept in registers across tiles
+        uint32_t gb[5], sb[5];
+#pragma unroll
+        for (int b = 0; b < 5; ++b) {
+            gb[b] = lds_u32(&op.gbit[b]);
+            sb[b] = lds_u32(&op.sbit[b]);
+        }
+        float2* amps = a + expand_index(t, op.tile_map);
+        if (op.pairs16) {
+            const uint32_t gh = (lane & 16) ? gb[0] : 0u, sh = p16 ^ ((lane & 16) ? sb[0] : 0u);
+            const float2* src = amps + 2 * (lane & 15) + gh;
+#pragma unroll
+            for (int mm = 0; mm < 16; ++mm) {
+                uint32_t g = 0, so = sh;
+#pragma unroll
+                for (int b = 1; b < 5; ++b)
+                    if ((mm >> (b - 1)) & 1) {
+                        g |= gb[b];
+                        so ^= sb[b];
+                    }
+                cp_async16(stage + so, src + g);
+            }
+        } else {
+            const float2* src = amps + lane;
+#pragma unroll
+            for (int m = 0; m < 32; ++m) {
+                uint32_t g = 0, so = plane;
+#pragma unroll
+                for (int b = 0; b < 5; ++b)
+                    if ((m >> b) & 1) {
+                        g |= gb[b];
+                        so ^= sb[b];
+                    }
+                cp_async8(stage + so, src + g);
+            }
+        }
+        cp_async_commit();
+        cp_async_wait_group<0>();
+        __syncwarp();
+#pragma unroll 1
+        for (int k0 = 0; k0 < U; k0 += KB) {
+            uint32_t pw[KB];
+            float2 xa[KB][D], xb[KB][D];
+#pragma unroll
+            for (int k = 0; k < KB; ++k) {
+                uint32_t o = pl;
+#pragma unroll
+                for (int b = 0; b < 5 - TB; ++b)
+                    if (((k0 + k) >> b) & 1) o ^= op.wbit[5 + b];
+                pw[k] = o;
+#pragma unroll
+                for (int s = 0; s < D; ++s) {
+                    const float2 v = stage[o ^ op.gsoff[s]];
+                    xa[k][s] = make_float2(v.x, v.x);
+                    xb[k][s] = make_float2(v.y, v.y);
+                }
+            }
+#pragma unroll
+            for (int r = 0; r < D; r += RB) {
+                float2 ac[RB][KB], bc[RB][KB];
+#pragma unroll
+                for (int q = 0; q < RB; ++q)
+#pragma unroll
+                    for (int k = 0; k < KB; ++k) ac[q][k] = bc[q][k] = make_float2(0.f, 0.f);
+#pragma unroll
+                for (int s = 0; s < D; ++s) {
+#pragma unroll
+                    for (int q = 0; q < RB; ++q) {
+                        const float2 e = lds_entry(mat + (r + q) * D + s);
+#pragma unroll
+                        for (int k = 0; k < KB; ++k) {
+                            ac[q][k] = __ffma2_rn(xa[k][s], e, ac[q][k]);
+                            bc[q][k] = __ffma2_rn(xb[k][s], e, bc[q][k]);
+                        }
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < RB; ++q) {
+                    const uint32_t g = op.gsoff[r + q];
+#pragma unroll
+                    for (int k = 0; k < KB; ++k) stage[pw[k] ^ g] = cdot_out(ac[q][k], bc[q][k]);
+                }
+            }
+        }
+        __syncwarp();
+        if (op.pairs16) {
+            const uint32_t gh = (lane & 16) ? gb[0] : 0u, sh = p16 ^ ((lane & 16) ? sb[0] : 0u);
+            float2* dst = amps + 2 * (lane & 15) + gh;
+#pragma unroll
+            for (int mm = 0; mm < 16; ++mm) {
+                uint32_t g = 0, so = sh;
+#pragma unroll
+                for (int b = 1; b < 5; ++b)
+                    if ((mm >> (b - 1)) & 1) {
+                        g |= gb[b];
+                        so ^= sb[b];
+                    }
+                *reinterpret_cast<float4*>(dst + g) = *reinterpret_cast<const float4*>(stage + so);
+            }
+        } else {
+            float2* dst = amps + lane;
+#pragma unroll
+            for (int m = 0; m < 32; ++m) {
+                uint32_t g = 0, so = plane;
+#pragma unroll
+                for (int b = 0; b < 5; ++b)
+                    if ((m >> b) & 1) {
+                        g |= gb[b];
+                        so ^= sb[b];
+                    }
+                dst[g] = stage[so];
+            }
+        }
+        __syncwarp();
+    }
+}
+
+template <int TB>
+__device__ __forceinline__ void apply_dense(float2* a, uint64_t n_amps, const BatchOp& op, const float2* mat,
+                                            float2* stage)
+{
+    if (op.tiled) tiled_pass<TB>(a, n_amps, op, mat, stage);
+    else dense_pass<TB>(a, n_amps, op, mat);
 }
 
 __global__ void __launch_bounds__(kBatchThreads, 1)
@@ -129,6 +362,9 @@ k_batch(BatchArgs args)
 {
     __shared__ float2 smat[256];
     __shared__ BatchOp sop;
+    __shared__ uint64_t s_n0;
+    extern __shared__ float2 stage_all[];
+    float2* stage = stage_all + (threadIdx.x >> 5) * (1 << kBatchTileBits);
     __shared__ double red[kBatchWarps];
     __shared__ int s_circ;
     __shared__ int s_ncols, s_colbit[2];
@@ -147,7 +383,8 @@ k_batch(BatchArgs args)
         const uint64_t N = uint64_t(1) << C.nbits;
         float2* col[2] = {args.arena + C.state_off, args.arena + C.state_off + N};
         uint64_t* res = args.results + C.res_off;
-        for (uint64_t i = threadIdx.x; i < N; i += kBatchThreads) col[0][i] = make_float2(i == 0 ? 1.f : 0.f, 0.f);
+        for (uint64_t v = threadIdx.x; v < N / 2; v += kBatchThreads)
+            reinterpret_cast<float4*>(col[0])[v] = make_float4(v == 0 ? 1.f : 0.f, 0.f, 0.f, 0.f);
         if (threadIdx.x == 0) {
             s_ncols = 1;
             s_counts[0] = C.nshots;
@@ -157,7 +394,12 @@ k_batch(BatchArgs args)
         uint64_t ctr = 0;   // position in the circuit's uniform stream
         __syncthreads();
         for (uint32_t oi = C.op_begin; oi < C.op_end; ++oi) {
-            if (threadIdx.x == 0) sop = args.ops[oi];
+            {
+                static_assert(sizeof(BatchOp) % 4 == 0, "BatchOp copies as 32-bit words");
+                const uint32_t* src = reinterpret_cast<const uint32_t*>(args.ops + oi);
+                uint32_t* dst = reinterpret_cast<uint32_t*>(&sop);
+                for (int w = threadIdx.x; w < (int)(sizeof(BatchOp) / 4); w += kBatchThreads) dst[w] = src[w];
+            }
             __syncthreads();
             const int kind = sop.kind;
             if (kind == kBatchDense) {
@@ -167,10 +409,10 @@ k_batch(BatchArgs args)
                 for (int k = 0; k < s_ncols; ++k) {
                     if (sop.cond >= 0 && s_colbit[k] != sop.cond) continue;
                     switch (sop.t) {
-                        case 1: dense_pass<1>(col[k], N, sop, smat); break;
-                        case 2: dense_pass<2>(col[k], N, sop, smat); break;
-                        case 3: dense_pass<3>(col[k], N, sop, smat); break;
-                        default: dense_pass<4>(col[k], N, sop, smat); break;
+                        case 1: apply_dense<1>(col[k], N, sop, smat, stage); break;
+                        case 2: apply_dense<2>(col[k], N, sop, smat, stage); break;
+                        case 3: apply_dense<3>(col[k], N, sop, smat, stage); break;
+                        default: apply_dense<4>(col[k], N, sop, smat, stage); break;
                     }
                 }
                 __syncthreads();
@@ -178,14 +420,17 @@ k_batch(BatchArgs args)
                 // P(bit = 0) of the single column (src/vectorstate.rs:252-261)
                 const uint64_t bit = uint64_t(1) << sop.pos;
                 double acc = 0.0;
-                for (uint64_t i = threadIdx.x; i < N; i += kBatchThreads)
-                    if (!(i & bit)) acc += (double)psq(col[0][i]);
+                const float4* c4 = reinterpret_cast<const float4*>(col[0]);   // two amplitudes (N >= 2)
+#pragma unroll 4
+                for (uint64_t v = threadIdx.x; v < N / 2; v += kBatchThreads) {
+                    const float4 q = c4[v];
+                    if (!((2 * v) & bit)) acc += (double)psq(make_float2(q.x, q.y));
+                    if (!((2 * v + 1) & bit)) acc += (double)psq(make_float2(q.z, q.w));
+                }
                 const double w0 = block_reduce(acc, red);
+                const uint64_t n0 = binomial_inv_block(C.nshots, fmin(w0, 1.0), stream_uniform(C.seed, ctr),
+                                                       reinterpret_cast<double*>(stage_all), &s_n0);
                 if (threadIdx.x == 0) {
-                    const double u = stream_uniform(C.seed, ctr);
-                    const uint64_t n0 = binomial_inv_dev(C.nshots, fmin(w0, 1.0), u);
-                    const uint64_t one = uint64_t(1) << sop.cbit;
-                    for (uint64_t r = 0; r < C.nshots; ++r) res[r] = r < n0 ? (res[r] & ~one) : (res[r] | one);
                     if (n0 == C.nshots || n0 == 0) {
                         s_ncols = 1;
                         s_keep[0] = n0 == 0 ? 1 : 0;
@@ -206,19 +451,31 @@ k_batch(BatchArgs args)
                 }
                 ++ctr;
                 __syncthreads();
+                {
+                    const uint64_t one = uint64_t(1) << sop.cbit;
+                    for (uint64_t r = threadIdx.x; r < C.nshots; r += kBatchThreads)
+                        res[r] = r < n0 ? (res[r] & ~one) : (res[r] | one);
+                }
                 // collapse (src/vectorstate.rs:91-104), splitting into two columns
                 const float f0 = (float)s_scale[0];
                 const float f1 = s_ncols == 2 ? (float)s_scale[1] : 0.f;
                 const bool two = s_ncols == 2;
                 const uint64_t keep0 = s_keep[0] ? bit : 0;
-                for (uint64_t i = threadIdx.x; i < N; i += kBatchThreads) {
-                    const float2 v = col[0][i];
-                    const bool b = (i & bit) != 0;
+                float4* c0 = reinterpret_cast<float4*>(col[0]);
+                float4* c1 = reinterpret_cast<float4*>(col[1]);
+#pragma unroll 4
+                for (uint64_t v = threadIdx.x; v < N / 2; v += kBatchThreads) {
+                    const float4 q = c0[v];
+                    const bool b0 = ((2 * v) & bit) != 0, b1 = ((2 * v + 1) & bit) != 0;
                     if (two) {
-                        col[1][i] = b ? make_float2(v.x * f1, v.y * f1) : make_float2(0.f, 0.f);
-                        col[0][i] = b ? make_float2(0.f, 0.f) : make_float2(v.x * f0, v.y * f0);
+                        c1[v] = make_float4(b0 ? q.x * f1 : 0.f, b0 ? q.y * f1 : 0.f, b1 ? q.z * f1 : 0.f,
+                                            b1 ? q.w * f1 : 0.f);
+                        c0[v] = make_float4(b0 ? 0.f : q.x * f0, b0 ? 0.f : q.y * f0, b1 ? 0.f : q.z * f0,
+                                            b1 ? 0.f : q.w * f0);
                     } else {
-                        col[0][i] = ((i & bit) == keep0) ? make_float2(v.x * f0, v.y * f0) : make_float2(0.f, 0.f);
+                        const bool k0 = ((2 * v) & bit) == keep0, k1 = ((2 * v + 1) & bit) == keep0;
+                        c0[v] = make_float4(k0 ? q.x * f0 : 0.f, k0 ? q.y * f0 : 0.f, k1 ? q.z * f0 : 0.f,
+                                            k1 ? q.w * f0 : 0.f);
                     }
                 }
                 __syncthreads();
@@ -265,11 +522,18 @@ k_batch(BatchArgs args)
 
 }  // namespace
 
+constexpr size_t kBatchStageBytes = size_t(kBatchWarps) * (size_t(1) << kBatchTileBits) * sizeof(float2);
+
+cudaError_t setup_batch_kernel()
+{
+    return cudaFuncSetAttribute(k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBatchStageBytes);
+}
+
 cudaError_t launch_batch(const BatchArgs& a, int sm_count, cudaStream_t st)
 {
     const unsigned grid = (unsigned)std::min<uint64_t>((uint64_t)sm_count, (uint64_t)a.ncircuits);
     if (grid == 0) return cudaSuccess;
-    k_batch<<<grid, kBatchThreads, 0, st>>>(a);
+    k_batch<<<grid, kBatchThreads, kBatchStageBytes, st>>>(a);
     return cudaGetLastError();
 }
 

@@ -31,4 +31,6 @@ void batch_add_circuit(q1g_batch* b, size_t nr_bits, size_t nr_shots, uint64_t s
                        const size_t* nbits_per_op, const size_t* bits_flat, const double* mats_flat,
                        const size_t* args);
 void batch_run(q1g_batch* b, uint64_t* results, size_t len);
+// warp-tile layout of a dense op on nbits qubits, gate positions pos[0..tb)
+void batch_tile_layout(BatchOp& op, const int* pos, int tb, int nbits);
 }  // namespace q1g

@@ -174,7 +174,22 @@ struct BatchOp {
     uint64_t cmask;   // sample: classical bits the outcome overwrites
     IndexMap map;     // dense: the gate positions, zeroed
     uint64_t offs[16];
+    // dense on states of >= kBatchTileBits qubits: a warp streams tiles of
+    // 2^kBatchTileBits amplitudes over the lowest positions that hold the
+    // gate bits (positions 0..4 are the lane bits, five more are register
+    // slots), staged in shared memory under an XOR swizzle of the four
+    // low index bits.
+    int tiled;
+    int pairs16;              // position 0 is not a gate position: the swizzle keeps amplitude
+                              // pairs (2i, 2i+1) adjacent and 16-byte aligned in the stage
+    uint32_t lane16;          // staged offset of lane bit 4
+    IndexMap tile_map;        // the tile's positions, zeroed: tile number -> first amplitude
+    uint32_t gbit[5];         // amplitude offset of slot bit b (slot m: OR over its bits; the lane adds 0..31)
+    uint32_t sbit[5];         // staged offset of slot bit b (slot m: XOR over its bits, then XOR the lane's)
+    uint16_t gsoff[16];       // staged offset of gate state s (offs[s] inside the tile)
+    uint16_t wbit[10];        // staged offset of each bit of a unit's number in the tile
 };
+constexpr int kBatchTileBits = 10;
 struct BatchCircuit {
     uint64_t state_off;   // amplitude offset of column 0 (column 1 follows)
     uint64_t res_off;     // first classical word of this circuit's runs
@@ -196,6 +211,7 @@ struct BatchArgs {
     uint64_t scratch_per_cta;
     unsigned* queue;
 };
+cudaError_t setup_batch_kernel();   // opt the batch kernel in to its shared-memory stage
 cudaError_t launch_batch(const BatchArgs& a, int sm_count, cudaStream_t st);
 
 // Per-block partials (6 doubles per block) comparing two states; wa and wb

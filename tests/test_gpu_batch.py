@@ -69,3 +69,21 @@ def test_batch_rejects_unsupported_programs():
     b = Batch(4)
     with pytest.raises(Exception):
         b.add(c, 10, 1)
+
+
+def test_batch_warp_tiles_match_oracle():
+    """States of 10 to 16 qubits take the warp-tile path: blocks on low and
+    high positions, one or two columns after the mid-circuit measurement."""
+    circuits = workloads.batch_workload(10, seed=21, qmin=10, qmax=16, dmin=4, dmax=12)
+    seeds = [500 + i for i in range(len(circuits))]
+    shots = 256
+    b = Batch(4)
+    for c, s in zip(circuits, seeds):
+        b.add(c, shots, s)
+    res = b.run()
+    agree, total = 0, 0
+    for c, s, r in zip(circuits, seeds, res):
+        alone = run_alone(c, shots, s)
+        agree += int(np.sum(alone == r))
+        total += shots
+    assert agree / total >= 0.999, agree / total

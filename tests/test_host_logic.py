@@ -6,6 +6,8 @@
 - fused_tc.cu: the tile of a tensor-core pass as a tensor-map box, and the
   staged-tile padding and row order (tests/cpp/tile_check.cpp, linked
   against the built library).
+- batch_host.cpp: the batch executor's warp tiles, their staged (swizzled)
+  offsets and bank pairs (tests/cpp/batch_tile_check.cpp, same library).
 
 Both programs are compiled here with g++ and print one line of figures.
 """
@@ -51,19 +53,28 @@ def test_double_float_split_join_dot(gxx, tmp_path):
     assert out.startswith("bad 0"), out
 
 
-def test_tile_box_and_padding(gxx, tmp_path):
+def _link_against_library(gxx, tmp_path, name):
     cuda = _cuda_home()
     if cuda is None:
         pytest.skip("no CUDA headers")
     lib = build.build()
     libdir = os.path.dirname(lib)
-    exe = str(tmp_path / "tile_check")
+    exe = str(tmp_path / name)
     cudalib = [p for p in (os.path.join(cuda, "lib64"), os.path.join(cuda, "lib")) if os.path.isdir(p)]
     cmd = [gxx, "-O2", "-std=c++17", "-I", os.path.join(cuda, "include"), "-o", exe,
-           os.path.join(CPP, "tile_check.cpp"), "-L", libdir, "-lq1gpu", "-Wl,-rpath," + libdir]
+           os.path.join(CPP, name + ".cpp"), "-L", libdir, "-lq1gpu", "-Wl,-rpath," + libdir]
     for d in cudalib:
         cmd += ["-L", d, "-Wl,-rpath," + d]
     cmd += ["-lcudart"]
     subprocess.run(cmd, check=True)
-    out = _run(exe)
+    return exe
+
+
+def test_tile_box_and_padding(gxx, tmp_path):
+    out = _run(_link_against_library(gxx, tmp_path, "tile_check"))
     assert "bad 0" in out, out
+
+
+def test_batch_warp_tiles(gxx, tmp_path):
+    out = _run(_link_against_library(gxx, tmp_path, "batch_tile_check"))
+    assert out.startswith("bad 0"), out
