@@ -286,6 +286,10 @@ def batch_leg(args):
     ngates = sum(1 for c in circuits for op in c.ops if op[0] in ("gate", "cgate"))
     ms = statistics.median(dev_ms)
     info = b.info()
+    peak, peak_kind = peaks()
+    # algorithmic bytes counted by the kernel itself (amplitude passes and
+    # classical words) over the device time of the launch
+    achieved = info["traffic_bytes"] / (ms / 1e3) / 1e9
     # CPU: the oracle runs the first circuits one by one
     from oracle import oracle as orc
     from q1tsim_gb300.vectorstate import Rng
@@ -302,6 +306,9 @@ def batch_leg(args):
             "circuits_per_s": len(circuits) / (ms / 1e3), "gates_per_s": ngates / (ms / 1e3),
             "e2e_circuits_per_s": len(circuits) / (statistics.median(wall_ms) / 1e3),
             "arena_gib": info["arena_bytes"] / 2 ** 30, "lowered_ops": info["ops"],
+            "roofline": {"bound": "hbm", "kernel": "k_batch", "traffic_gb": info["traffic_bytes"] / 1e9,
+                         "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                         "frac": achieved / peak},
             "launches_per_run": 1, "setup_s": setup_s,
             "cpu_baseline": {"value": len(circuits) / cpu_total_s, "unit": "circuits/s", "cores": 1, "kind": "port",
                              "sample": f"oracle on the first {len(sample)} circuits in {cpu_s:.2f} s, scaled to "

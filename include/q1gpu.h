@@ -210,6 +210,10 @@ int q1g_batch_run(q1g_batch* b, uint64_t* results, size_t len);
  * last run in ms.  Any pointer may be NULL. */
 int q1g_batch_info(const q1g_batch* b, size_t* ncircuits, size_t* total_runs, size_t* arena_bytes,
                    size_t* nops, double* last_ms);
+/* Algorithmic device-memory bytes of the last run: every pass's amplitude
+ * reads and writes (gate blocks, measurement, collapse, sampling) and the
+ * classical words it updates, as counted by the kernel. */
+int q1g_batch_traffic(const q1g_batch* b, uint64_t* bytes);
 
 /* ---- profiling: per-kernel CUDA-event timing on the state's stream */
 int q1g_profile_enable(q1g_state* s, int enable);

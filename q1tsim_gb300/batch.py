@@ -35,6 +35,8 @@ def _protos(L):
     L.q1g_batch_run.restype = ctypes.c_int
     L.q1g_batch_info.argtypes = [ctypes.c_void_p, _szp, _szp, _szp, _szp, _dp]
     L.q1g_batch_info.restype = ctypes.c_int
+    L.q1g_batch_traffic.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]
+    L.q1g_batch_traffic.restype = ctypes.c_int
     L._batch_protos = True
 
 
@@ -143,5 +145,7 @@ class Batch:
         ms = ctypes.c_double()
         check(_lib.load().q1g_batch_info(self._h, ctypes.byref(nc), ctypes.byref(runs), ctypes.byref(arena),
                                          ctypes.byref(nops), ctypes.byref(ms)))
+        moved = ctypes.c_uint64()
+        check(_lib.load().q1g_batch_traffic(self._h, ctypes.byref(moved)))
         return {"circuits": nc.value, "runs": runs.value, "arena_bytes": arena.value, "ops": nops.value,
-                "last_ms": ms.value}
+                "last_ms": ms.value, "traffic_bytes": moved.value}

@@ -372,6 +372,12 @@ k_batch(BatchArgs args)
     __shared__ double s_scale[2];
     __shared__ int s_keep[2];
     double* scratch = args.scratch + (uint64_t)blockIdx.x * args.scratch_per_cta;
+    // algorithmic bytes (each pass's reads and writes of amplitudes and
+    // classical words), counted by thread 0 in shared memory (no register is
+    // held across the passes) and summed over the CTAs
+    __shared__ unsigned long long s_moved;
+    __shared__ unsigned s_cpass;   // dense column passes of the current circuit
+    if (threadIdx.x == 0) s_moved = 0;
 
     for (;;) {
         if (threadIdx.x == 0) s_circ = (int)atomicAdd(args.queue, 1u);
@@ -392,6 +398,10 @@ k_batch(BatchArgs args)
             s_colbit[0] = s_colbit[1] = -1;
         }
         uint64_t ctr = 0;   // position in the circuit's uniform stream
+        if (threadIdx.x == 0) {
+            s_moved += N * sizeof(float2);
+            s_cpass = 0;
+        }
         __syncthreads();
         for (uint32_t oi = C.op_begin; oi < C.op_end; ++oi) {
             {
@@ -408,6 +418,7 @@ k_batch(BatchArgs args)
                 __syncthreads();
                 for (int k = 0; k < s_ncols; ++k) {
                     if (sop.cond >= 0 && s_colbit[k] != sop.cond) continue;
+                    if (threadIdx.x == 0) ++s_cpass;
                     switch (sop.t) {
                         case 1: apply_dense<1>(col[k], N, sop, smat, stage); break;
                         case 2: apply_dense<2>(col[k], N, sop, smat, stage); break;
@@ -457,6 +468,7 @@ k_batch(BatchArgs args)
                         res[r] = r < n0 ? (res[r] & ~one) : (res[r] | one);
                 }
                 // collapse (src/vectorstate.rs:91-104), splitting into two columns
+                if (threadIdx.x == 0) s_moved += (2 + (uint64_t)s_ncols) * N * sizeof(float2) + 2 * C.nshots * sizeof(uint64_t);
                 const float f0 = (float)s_scale[0];
                 const float f1 = s_ncols == 2 ? (float)s_scale[1] : 0.f;
                 const bool two = s_ncols == 2;
@@ -512,12 +524,15 @@ k_batch(BatchArgs args)
                     }
                     ctr += m + 1;
                     r0 += m;
+                    if (threadIdx.x == 0) s_moved += N * sizeof(float2) + m * (chunk * sizeof(float2) + 2 * sizeof(uint64_t));
                     __syncthreads();
                 }
             }
         }
         __syncthreads();
+        if (threadIdx.x == 0) s_moved += (unsigned long long)s_cpass * 2 * N * sizeof(float2);
     }
+    if (threadIdx.x == 0) atomicAdd(args.traffic, s_moved);
 }
 
 }  // namespace

@@ -16,13 +16,14 @@ struct q1g_batch {
     uint64_t arena_amps = 0;
     uint64_t scratch_per_cta = 0;
     int sms = 0;
-    q1g::DevBuf arena, results, dcircuits, dops, dmats, dtables, scratch, queue;
-    q1g::HostBuf hresults;
+    q1g::DevBuf arena, results, dcircuits, dops, dmats, dtables, scratch, queue, traffic;
+    q1g::HostBuf hresults, htraffic;
     cudaStream_t stream = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     float last_ms = 0.f;
+    uint64_t last_traffic = 0;          // algorithmic device-memory bytes of the last run
     ~q1g_batch();
 };
 

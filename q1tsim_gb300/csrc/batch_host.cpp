@@ -252,6 +252,8 @@ static void batch_build(q1g_batch* b)
     const int grid = std::min<int>(b->sms, (int)std::max<size_t>(nc, 1));
     b->scratch.ensure((size_t)grid * b->scratch_per_cta * sizeof(double));
     b->queue.ensure(sizeof(unsigned));
+    b->traffic.ensure(sizeof(unsigned long long));
+    b->htraffic.ensure(sizeof(unsigned long long));
     check_cuda(cudaStreamSynchronize(b->stream), "batch upload");
 
     BatchArgs a{};
@@ -265,14 +267,19 @@ static void batch_build(q1g_batch* b)
     a.scratch = b->scratch.as<double>();
     a.scratch_per_cta = b->scratch_per_cta;
     a.queue = b->queue.as<unsigned>();
+    a.traffic = b->traffic.as<unsigned long long>();
     check_cuda(setup_batch_kernel(), "batch kernel attributes");
     // one execution = reset queue and results, the persistent launch, results out
     check_cuda(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
     cudaError_t e = cudaMemsetAsync(b->queue.p, 0, sizeof(unsigned), b->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->traffic.p, 0, sizeof(unsigned long long), b->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->results.p, 0, std::max<uint64_t>(res, 1) * sizeof(uint64_t), b->stream);
     if (e == cudaSuccess) e = launch_batch(a, b->sms, b->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(b->hresults.p, b->results.p, res * sizeof(uint64_t), cudaMemcpyDeviceToHost, b->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(b->htraffic.p, b->traffic.p, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                            b->stream);
     cudaGraph_t g = nullptr;
     const cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
     check_cuda(e, "batch capture");
@@ -296,6 +303,7 @@ void batch_run(q1g_batch* b, uint64_t* results, size_t len)
     float ms = 0.f;
     check_cuda(cudaEventElapsedTime(&ms, b->ev0, b->ev1), "event time");
     b->last_ms = ms;
+    b->last_traffic = *static_cast<const unsigned long long*>(b->htraffic.p);
     if (results) std::memcpy(results, b->hresults.p, b->total_runs * sizeof(uint64_t));
 }
 

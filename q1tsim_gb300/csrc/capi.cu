@@ -533,6 +533,15 @@ int q1g_batch_info(const q1g_batch* b, size_t* ncircuits, size_t* total_runs, si
     });
 }
 
+int q1g_batch_traffic(const q1g_batch* b, uint64_t* bytes)
+{
+    return guarded([&] {
+        need(b, "batch");
+        need(bytes, "bytes");
+        *bytes = b->last_traffic;
+    });
+}
+
 int q1g_sample_shots_noalloc(const void* d_amps, int precision, size_t nr_bits, const double* d_sorted_uniforms,
                              size_t nshots, uint64_t* d_outcomes, uint64_t* d_words, const size_t* cbits,
                              void* cuda_stream)

@@ -210,6 +210,7 @@ struct BatchArgs {
     double* scratch;
     uint64_t scratch_per_cta;
     unsigned* queue;
+    unsigned long long* traffic;    // algorithmic bytes the launch moves in device memory (summed)
 };
 cudaError_t setup_batch_kernel();   // opt the batch kernel in to its shared-memory stage
 cudaError_t launch_batch(const BatchArgs& a, int sm_count, cudaStream_t st);
