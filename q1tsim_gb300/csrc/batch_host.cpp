@@ -1,6 +1,7 @@
 // Host side of the batched executor: lowering of circuit programs, device
 // buffers, and the CUDA graph that replays the persistent launch.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <numeric>
 #include <string>
@@ -217,13 +218,33 @@ static void batch_build(q1g_batch* b)
     int dev = 0;
     check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
     check_cuda(cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev), "sm count");
-    // queue order: largest circuits first, so the long ones start early
+    // queue order: most work first (longest-processing-time order), so the
+    // long circuits start early and the short ones fill in at the end.  The
+    // work estimate counts amplitude reads and writes: every gate pass over
+    // every column (two after the measurement), the measurement, and the
+    // sampling's chunk sums and searched chunks.
     const size_t nc = b->circuits.size();
+    std::vector<double> work(nc, 0.0);
+    for (size_t i = 0; i < nc; ++i) {
+        const BatchCircuit& C = b->circuits[i];
+        const double N = std::ldexp(1.0, C.nbits);
+        double w = N, cols = 1.0;
+        for (uint32_t oi = C.op_begin; oi < C.op_end; ++oi) {
+            const BatchOp& op = b->ops[oi];
+            if (op.kind == kBatchDense) {
+                w += 2.0 * N * (op.cond >= 0 ? 1.0 : cols);
+            } else if (op.kind == kBatchMeasure) {
+                w += 4.0 * N;
+                cols = 2.0;
+            } else {
+                w += N * cols + (double)C.nshots * std::min(N, 256.0);
+            }
+        }
+        work[i] = w;
+    }
     std::vector<size_t> order(nc);
     std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) {
-        return b->circuits[x].nbits > b->circuits[y].nbits;
-    });
+    std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) { return work[x] > work[y]; });
     uint64_t res = 0;
     for (auto& C : b->circuits) {
         C.res_off = res;
