@@ -151,7 +151,12 @@ int q1g_reset_all(q1g_state* s);
  * (qubits per gate) and, for fusion_width > 0, their grouping into fused
  * blocks of at most fusion_width qubits (<= 5).  q1g_plan_run takes the
  * gate matrices for this execution, since parameters may change between
- * executions (src/gates/parameter.rs:23-75). */
+ * executions (src/gates/parameter.rs:23-75).  Fused blocks without controls
+ * run in warp tiles: complex64 blocks of up to 4 qubits (5-qubit blocks on
+ * the tensor cores), complex128 blocks of up to 3 qubits on double-float
+ * pairs; larger complex128 blocks, and every block of a state set to
+ * q1g_state_set_fp64_exact, use FP64 arithmetic, so complex128 plans are
+ * best made with fusion_width <= 3. */
 
 /* ks[g] = qubits of gate g; bits_flat = all gates' qubits concatenated. */
 int q1g_plan_create(size_t nr_bits, size_t ngates, const size_t* ks, const size_t* bits_flat,

@@ -235,15 +235,20 @@ class Circuit:
     def _run_seq(self, q_state, idx, seq):
         if hasattr(q_state, "apply_plan"):
             flat = self._frozen[idx] if self._frozen is not None else self._flat(seq)
-            plan = self._plans.get(idx)
+            key = (idx, q_state.precision)
+            plan = self._plans.get(key)
             if plan is None:
                 bits = [op[2] for op in seq]
                 width, tc = self.fusion_width, True
                 if width == "auto":
                     from . import autotune
                     width, tc = autotune.tune(self.nr_qbits, q_state.precision, bits, flat)
+                if q_state.precision == "c128" and width > 3:
+                    # complex128 blocks of up to 3 qubits run on double-float
+                    # pairs in warp tiles; larger ones would take the FP64 pipe
+                    width = 3
                 plan = Plan(self.nr_qbits, bits, width, tensor_cores=tc)
-                self._plans[idx] = plan
+                self._plans[key] = plan
             q_state.apply_plan(plan, flat)
         else:
             for op in seq:

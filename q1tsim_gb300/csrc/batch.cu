@@ -18,6 +18,7 @@
 
 #include "engine.h"
 #include "sampling.cuh"
+#include "warp_tile.cuh"
 
 namespace q1g {
 
@@ -83,7 +84,7 @@ __device__ double block_scan_excl(double* data, uint64_t n, double* wsum)
 // same sums in the same order as the one-thread loop, so the same k.  Called
 // by every thread of the CTA with the same arguments.
 constexpr int kBinomChunk = 4096;
-static_assert(kBinomChunk <= kBatchWarps * (1 << kBatchTileBits), "the terms fit in the tile stage");
+static_assert(kBinomChunk <= kBatchWarps * (1 << 10), "the terms fit in the tile stage");
 
 __device__ uint64_t binomial_inv_block(uint64_t n, double p, double u, double* terms, uint64_t* s_k)
 {
@@ -125,52 +126,7 @@ __device__ uint64_t binomial_inv_block(uint64_t n, double p, double u, double* t
     return hi;
 }
 
-// 8- and 16-byte asynchronous copies global -> shared, committed in groups;
-// the issuing lane's copies of all but the newest N groups are complete
-// after cp_async_wait_group<N>
-__device__ __forceinline__ void cp_async8(float2* smem, const float2* gmem)
-{
-    const uint32_t sa = (uint32_t)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async16(float2* smem, const float2* gmem)
-{
-    const uint32_t sa = (uint32_t)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait_group() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
-
-// Shared-memory load of a 32-bit value that the compiler may not hoist out of
-// its loop.
-__device__ __forceinline__ uint32_t lds_u32(const uint32_t* p)
-{
-    uint32_t v;
-    asm volatile("ld.shared.u32 %0, [%1];\n" : "=r"(v) : "r"((uint32_t)__cvta_generic_to_shared(p)));
-    return v;
-}
-
-// Shared-memory load of one matrix entry (re, im), kept at its use: a plain
-// load of the (loop-invariant) matrix would be hoisted out of the tile loop
-// into as many registers as the matrix has entries.  All lanes read the same
-// entry, so the load is one broadcast wavefront.
-__device__ __forceinline__ float2 lds_entry(const float2* p)
-{
-    float2 v;
-    const uint32_t sa = (uint32_t)__cvta_generic_to_shared(p);
-    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];\n" : "=f"(v.x), "=f"(v.y) : "r"(sa));
-    return v;
-}
-
-// Complex products on packed FP32x2 FMAs with the matrix entry m = (re, im)
-// as one operand: with xa = (x.re, x.re) and xb = (x.im, x.im),
-//   a += xa * m = (x.re m.re, x.re m.im),  b += xb * m = (x.im m.re, x.im m.im),
-// and sum m x = (a.x - b.y, a.y + b.x).  An entry is read as 8 bytes and
-// serves every unit a lane holds; the inputs are duplicated once per unit.
-__device__ __forceinline__ float2 cdot_out(float2 a, float2 b) { return make_float2(a.x - b.y, a.y + b.x); }
-
-// States below kBatchTileBits qubits: one unit (the 2^TB amplitudes a
+// States below 10 qubits (smaller than a warp tile): one unit (the 2^TB amplitudes a
 // block mixes) per thread.  mat[r * D + s] is the block's entry (r, s).
 template <int TB>
 __device__ void dense_pass(float2* a, uint64_t n_amps, const BatchOp& op, const float2* mat)
@@ -200,160 +156,11 @@ __device__ void dense_pass(float2* a, uint64_t n_amps, const BatchOp& op, const 
     }
 }
 
-// States of kBatchTileBits qubits or more: each warp streams tiles of 1024
-// amplitudes (BatchOp::tiled).  Slot m of lane l is amplitude
-// tile_base + goff(m) + l, goff(m) = OR of gbit[b] over the set bits b of m,
-// so every copy and store instruction of the warp moves whole runs of 256
-// contiguous bytes whatever the gate positions.  A tile is copied
-// asynchronously into the warp's 8 KB stage at the swizzled offsets
-// soff(m) ^ soff(l) (soff is linear: XOR of sbit[b]); where the layout keeps
-// amplitude pairs (2i, 2i+1) adjacent (BatchOp::pairs16) a lane moves 16
-// bytes at a time, two slots per instruction.  Each lane then applies the
-// block to 32 / 2^TB units, KB units and RB output rows at a time, so that
-// one matrix entry read serves KB units and 2 * KB * RB FMA chains are in
-// flight.  Sixteen warps per SM overlap one another's copies, arithmetic and
-// stores.
-template <int TB>
-__device__ void tiled_pass(float2* a, uint64_t n_amps, const BatchOp& op, const float2* mat, float2* stage)
-{
-    constexpr int D = 1 << TB;
-    constexpr int U = 32 >> TB;
-    constexpr int KB = U < 2 ? U : 2;
-    constexpr int RB = TB >= 3 ? 2 : 1;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint64_t tiles = n_amps >> kBatchTileBits;
-    const uint32_t plane = (uint32_t)(lane & 15) ^ ((lane & 16) ? op.lane16 : 0u);
-    // 16-byte form: lane l moves amplitudes 2i, 2i+1 (i = l & 15) of slots 2mm + (l >> 4)
-    const uint32_t p16 = (uint32_t)((2 * lane) & 15) ^ ((lane & 8) ? op.lane16 : 0u);
-    uint32_t pl = 0;
-#pragma unroll
-    for (int b = 0; b < 5; ++b)
-        if ((lane >> b) & 1) pl ^= op.wbit[b];
-
-    for (uint64_t t = (uint64_t)warp; t < tiles; t += kBatchWarps) {
-        // slot offsets from the five basis values, read per tile (volatile)
-        // so that the 64 derived offsets are not kept in registers across tiles
-        uint32_t gb[5], sb[5];
-#pragma unroll
-        for (int b = 0; b < 5; ++b) {
-            gb[b] = lds_u32(&op.gbit[b]);
-            sb[b] = lds_u32(&op.sbit[b]);
-        }
-        float2* amps = a + expand_index(t, op.tile_map);
-        if (op.pairs16) {
-            const uint32_t gh = (lane & 16) ? gb[0] : 0u, sh = p16 ^ ((lane & 16) ? sb[0] : 0u);
-            const float2* src = amps + 2 * (lane & 15) + gh;
-#pragma unroll
-            for (int mm = 0; mm < 16; ++mm) {
-                uint32_t g = 0, so = sh;
-#pragma unroll
-                for (int b = 1; b < 5; ++b)
-                    if ((mm >> (b - 1)) & 1) {
-                        g |= gb[b];
-                        so ^= sb[b];
-                    }
-                cp_async16(stage + so, src + g);
-            }
-        } else {
-            const float2* src = amps + lane;
-#pragma unroll
-            for (int m = 0; m < 32; ++m) {
-                uint32_t g = 0, so = plane;
-#pragma unroll
-                for (int b = 0; b < 5; ++b)
-                    if ((m >> b) & 1) {
-                        g |= gb[b];
-                        so ^= sb[b];
-                    }
-                cp_async8(stage + so, src + g);
-            }
-        }
-        cp_async_commit();
-        cp_async_wait_group<0>();
-        __syncwarp();
-#pragma unroll 1
-        for (int k0 = 0; k0 < U; k0 += KB) {
-            uint32_t pw[KB];
-            float2 xa[KB][D], xb[KB][D];
-#pragma unroll
-            for (int k = 0; k < KB; ++k) {
-                uint32_t o = pl;
-#pragma unroll
-                for (int b = 0; b < 5 - TB; ++b)
-                    if (((k0 + k) >> b) & 1) o ^= op.wbit[5 + b];
-                pw[k] = o;
-#pragma unroll
-                for (int s = 0; s < D; ++s) {
-                    const float2 v = stage[o ^ op.gsoff[s]];
-                    xa[k][s] = make_float2(v.x, v.x);
-                    xb[k][s] = make_float2(v.y, v.y);
-                }
-            }
-#pragma unroll
-            for (int r = 0; r < D; r += RB) {
-                float2 ac[RB][KB], bc[RB][KB];
-#pragma unroll
-                for (int q = 0; q < RB; ++q)
-#pragma unroll
-                    for (int k = 0; k < KB; ++k) ac[q][k] = bc[q][k] = make_float2(0.f, 0.f);
-#pragma unroll
-                for (int s = 0; s < D; ++s) {
-#pragma unroll
-                    for (int q = 0; q < RB; ++q) {
-                        const float2 e = lds_entry(mat + (r + q) * D + s);
-#pragma unroll
-                        for (int k = 0; k < KB; ++k) {
-                            ac[q][k] = __ffma2_rn(xa[k][s], e, ac[q][k]);
-                            bc[q][k] = __ffma2_rn(xb[k][s], e, bc[q][k]);
-                        }
-                    }
-                }
-#pragma unroll
-                for (int q = 0; q < RB; ++q) {
-                    const uint32_t g = op.gsoff[r + q];
-#pragma unroll
-                    for (int k = 0; k < KB; ++k) stage[pw[k] ^ g] = cdot_out(ac[q][k], bc[q][k]);
-                }
-            }
-        }
-        __syncwarp();
-        if (op.pairs16) {
-            const uint32_t gh = (lane & 16) ? gb[0] : 0u, sh = p16 ^ ((lane & 16) ? sb[0] : 0u);
-            float2* dst = amps + 2 * (lane & 15) + gh;
-#pragma unroll
-            for (int mm = 0; mm < 16; ++mm) {
-                uint32_t g = 0, so = sh;
-#pragma unroll
-                for (int b = 1; b < 5; ++b)
-                    if ((mm >> (b - 1)) & 1) {
-                        g |= gb[b];
-                        so ^= sb[b];
-                    }
-                *reinterpret_cast<float4*>(dst + g) = *reinterpret_cast<const float4*>(stage + so);
-            }
-        } else {
-            float2* dst = amps + lane;
-#pragma unroll
-            for (int m = 0; m < 32; ++m) {
-                uint32_t g = 0, so = plane;
-#pragma unroll
-                for (int b = 0; b < 5; ++b)
-                    if ((m >> b) & 1) {
-                        g |= gb[b];
-                        so ^= sb[b];
-                    }
-                dst[g] = stage[so];
-            }
-        }
-        __syncwarp();
-    }
-}
-
 template <int TB>
 __device__ __forceinline__ void apply_dense(float2* a, uint64_t n_amps, const BatchOp& op, const float2* mat,
                                             float2* stage)
 {
-    if (op.tiled) tiled_pass<TB>(a, n_amps, op, mat, stage);
+    if (op.tile.tiled) tiled_dense_c64<TB>(a, n_amps, op.tile, mat, stage, threadIdx.x >> 5, kBatchWarps);
     else dense_pass<TB>(a, n_amps, op, mat);
 }
 
@@ -364,7 +171,7 @@ k_batch(BatchArgs args)
     __shared__ BatchOp sop;
     __shared__ uint64_t s_n0;
     extern __shared__ float2 stage_all[];
-    float2* stage = stage_all + (threadIdx.x >> 5) * (1 << kBatchTileBits);
+    float2* stage = stage_all + (threadIdx.x >> 5) * (1 << 10);
     __shared__ double red[kBatchWarps];
     __shared__ int s_circ;
     __shared__ int s_ncols, s_colbit[2];
@@ -537,7 +344,7 @@ k_batch(BatchArgs args)
 
 }  // namespace
 
-constexpr size_t kBatchStageBytes = size_t(kBatchWarps) * (size_t(1) << kBatchTileBits) * sizeof(float2);
+constexpr size_t kBatchStageBytes = size_t(kBatchWarps) * (size_t(1) << 10) * sizeof(float2);
 
 cudaError_t setup_batch_kernel()
 {

@@ -24,67 +24,11 @@ q1g_batch::~q1g_batch()
 
 namespace q1g {
 
-// Warp-tile layout of a dense op on a state of nbits >= kBatchTileBits
-// qubits (BatchOp::tiled).  The tile's ten positions are the gate positions
-// and the lowest non-gate positions, so positions 0..4 always belong to it
-// (at most four of them are gate positions) and serve as the lane bits.  A
-// staged index keeps the tile's local bit order (local bit k = k-th tile
-// position); its local bits 4..9 select a row of 16 amplitudes (128 bytes)
-// and are XOR-ed into the four column bits so that, for each gate state, the
-// 16 units a half warp reads lie in 16 different 8-byte bank pairs: a unit's
-// four lowest number bits go to distinct column bits.
+// Warp-tile layout of a dense op (warp_tile.h): complex64 tiles of 1024
+// amplitudes, 16 per stage row.
 void batch_tile_layout(BatchOp& op, const int* pos, int tb, int nbits)
 {
-    op.tiled = 0;
-    if (nbits < kBatchTileBits || tb < 1 || tb > 4) return;
-    uint64_t gmask = 0;
-    for (int j = 0; j < tb; ++j) gmask |= uint64_t(1) << pos[j];
-    int L[kBatchTileBits], ng[kBatchTileBits];
-    int nl = 0, nng = 0;
-    for (int p = 0; nl < kBatchTileBits; ++p) {
-        if ((gmask >> p) & 1) {
-            L[nl++] = p;
-        } else if (nng < kBatchTileBits - tb) {
-            ng[nng++] = nl;
-            L[nl++] = p;
-        }
-    }
-    uint32_t M[kBatchTileBits - 4] = {};
-    uint32_t used = 0;
-    for (int b = 0; b < 4; ++b)
-        if (ng[b] < 4) used |= 1u << ng[b];
-    int free_col = 0;
-    for (int b = 0; b < 4; ++b) {
-        if (ng[b] < 4) continue;
-        while ((used >> free_col) & 1) ++free_col;
-        M[ng[b] - 4] = 1u << free_col;
-        used |= 1u << free_col;
-    }
-    auto phys = [&](uint32_t idx) {
-        uint32_t r = idx;
-        for (int q = 4; q < kBatchTileBits; ++q)
-            if ((idx >> q) & 1) r ^= M[q - 4];
-        return r;
-    };
-    auto local = [&](uint64_t amp_offset) {
-        uint32_t r = 0;
-        for (int k = 0; k < kBatchTileBits; ++k)
-            if ((amp_offset >> L[k]) & 1) r |= 1u << k;
-        return r;
-    };
-    op.tiled = 1;
-    op.pairs16 = (gmask & 1) ? 0 : 1;
-    op.lane16 = phys(16);
-    op.tile_map = IndexMap{};
-    op.tile_map.nz = kBatchTileBits;
-    for (int k = 0; k < kBatchTileBits; ++k) op.tile_map.zpos[k] = L[k];
-    op.tile_map.setmask = 0;
-    for (int b = 0; b < 5; ++b) {
-        op.gbit[b] = 1u << L[5 + b];
-        op.sbit[b] = phys(1u << (5 + b));
-    }
-    for (int s = 0; s < (1 << tb); ++s) op.gsoff[s] = (uint16_t)phys(local(op.offs[s]));
-    for (int b = 0; b < kBatchTileBits; ++b) op.wbit[b] = b < nng ? (uint16_t)phys(1u << ng[b]) : 0;
+    warp_tile_layout(op.tile, pos, tb, op.offs, nbits, 10, 4);
 }
 
 static BatchOp dense_op(const std::vector<cd>& m, const std::vector<int>& qubits, int nbits, int cond,

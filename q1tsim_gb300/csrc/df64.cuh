@@ -175,6 +175,20 @@ __host__ __device__ __forceinline__ uint64_t join_f64(DF v)
     return ((uint64_t)sign << 32) | mag;
 }
 
+// A matrix coefficient as a double-float pair on the host (split_f64; a
+// value outside the split's range becomes the nearest float pair).
+inline DF host_split(double v)
+{
+    uint64_t b;
+    std::memcpy(&b, &v, 8);
+    DF d{0.0f, 0.0f};
+    if (!split_f64(b, d)) {
+        d.h = (float)v;
+        d.l = (float)(v - (double)d.h);
+    }
+    return d;
+}
+
 // sum_k a[k] * b[k] over N double-float terms, normalised (|l| <= ulp(h)/2).
 template <int N>
 __host__ __device__ __forceinline__ DF dot(const DF* a, const DF* b)

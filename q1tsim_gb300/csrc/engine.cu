@@ -192,6 +192,19 @@ void q1g_state::apply_op(const GateOp& op, char* base, uint64_t total_amps)
                 hm[2 * e] = op.dense[e].real();
                 hm[2 * e + 1] = op.dense[e].imag();
             }
+            if (dense_tiled_applies(prec, nbits, op.t, op.map, fp64_exact)) {
+                std::vector<unsigned char> img(dense_tiled_matrix_bytes(prec, op.t));
+                dense_tiled_matrix(prec, op.t, hm.data(), img.data());
+                matbuf.ensure(img.size());
+                check_cuda(cudaMemcpyAsync(matbuf.p, img.data(), img.size(), cudaMemcpyHostToDevice, stream),
+                           "upload matrix");
+                sync();
+                launch(prec == kC128 ? "dense_tiled_c128" : "dense_tiled_c64", b2 * op.touched(total_amps), [&] {
+                    return launch_dense_tiled(base, prec, total_amps, nbits, op.map, op.offs, op.t, matbuf.p,
+                                              sm_count(), stream);
+                });
+                return;
+            }
             if (prec == kC64) {
                 std::vector<float> hf(hm.begin(), hm.end());
                 matbuf.ensure(hf.size() * sizeof(float));
@@ -810,6 +823,24 @@ void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n)
                                        s->errbuf.as<int>(), s->sm_count(), s->stream);
             });
             if (paired) ++i;   // the next block rode in this pass
+        } else if (op.kind == GateOp::Dense &&
+                   dense_tiled_applies(s->prec, s->nbits, op.t, op.map, s->fp64_exact)) {
+            begin();
+            const size_t d2 = op.dense.size();
+            std::vector<double> v(2 * d2);
+            for (size_t e = 0; e < d2; ++e) {
+                v[2 * e] = op.dense[e].real();
+                v[2 * e + 1] = op.dense[e].imag();
+            }
+            std::vector<unsigned char> img(dense_tiled_matrix_bytes(s->prec, op.t));
+            dense_tiled_matrix(s->prec, op.t, v.data(), img.data());
+            const void* dm = stage(img.data(), img.size());
+            const uint64_t total = s->total();
+            s->launch(s->prec == kC128 ? "dense_tiled_c128" : "dense_tiled_c64", 2.0 * s->bsz() * op.touched(total),
+                      [&] {
+                          return launch_dense_tiled(s->amps.p, s->prec, total, s->nbits, op.map, op.offs, op.t, dm,
+                                                    s->sm_count(), s->stream);
+                      });
         } else if (op.kind == GateOp::Dense) {
             begin();
             const size_t d2 = op.dense.size();

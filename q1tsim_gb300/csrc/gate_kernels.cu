@@ -177,18 +177,6 @@ struct Mat2DF {
     float2 h[2][4], l[2][4];
 };
 
-__host__ inline DF host_split(double v)
-{
-    uint64_t b;
-    std::memcpy(&b, &v, 8);
-    DF d{0.0f, 0.0f};
-    if (!split_f64(b, d)) {
-        // outside the split's range: nearest float pair
-        d.h = (float)v;
-        d.l = (float)(v - (double)d.h);
-    }
-    return d;
-}
 
 // out0 = m00 x0 + m01 x1, out1 = m10 x0 + m11 x1 on double-float pairs; a
 // unit with an amplitude outside the split's range is done in FP64 (md).

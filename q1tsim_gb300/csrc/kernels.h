@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include "common.cuh"
+#include "warp_tile.h"
 
 namespace q1g {
 
@@ -29,6 +30,18 @@ cudaError_t launch_phase(void* amps, int prec, uint64_t total, const IndexMap& m
 // dmat: device matrix 2^tb x 2^tb, complex in the state's precision.
 cudaError_t launch_dense(void* amps, int prec, uint64_t total, const IndexMap& map,
                          const DenseOffsets& offs, int tb, const void* dmat, cudaStream_t st);
+
+// ---- dense_tiled.cu: uncontrolled dense blocks in warp tiles (warp_tile.h)
+// True when the tiled kernel takes the block: no controls, t <= 4 (complex64,
+// >= 10 qubits) or t <= 3 on double-float pairs (complex128, >= 9 qubits).
+bool dense_tiled_applies(int prec, int nbits, int t, const IndexMap& map, bool fp64_exact);
+// The kernel's matrix image of a 2^t x 2^t complex matrix m (interleaved
+// doubles): complex64 entries, or complex128 double-float terms followed by
+// the FP64 matrix.
+size_t dense_tiled_matrix_bytes(int prec, int t);
+void dense_tiled_matrix(int prec, int t, const double* m, void* out);
+cudaError_t launch_dense_tiled(void* amps, int prec, uint64_t total, int nbits, const IndexMap& map,
+                               const DenseOffsets& offs, int t, const void* dmat, int sm_count, cudaStream_t st);
 
 // ---- fused_tc.cu: 5-qubit fused blocks on the tensor cores (complex64)
 // Geometry of one tensor-core pass over tiles of 2^12 amplitudes.  Tile
@@ -174,22 +187,11 @@ struct BatchOp {
     uint64_t cmask;   // sample: classical bits the outcome overwrites
     IndexMap map;     // dense: the gate positions, zeroed
     uint64_t offs[16];
-    // dense on states of >= kBatchTileBits qubits: a warp streams tiles of
-    // 2^kBatchTileBits amplitudes over the lowest positions that hold the
-    // gate bits (positions 0..4 are the lane bits, five more are register
-    // slots), staged in shared memory under an XOR swizzle of the four
-    // low index bits.
-    int tiled;
-    int pairs16;              // position 0 is not a gate position: the swizzle keeps amplitude
-                              // pairs (2i, 2i+1) adjacent and 16-byte aligned in the stage
-    uint32_t lane16;          // staged offset of lane bit 4
-    IndexMap tile_map;        // the tile's positions, zeroed: tile number -> first amplitude
-    uint32_t gbit[5];         // amplitude offset of slot bit b (slot m: OR over its bits; the lane adds 0..31)
-    uint32_t sbit[5];         // staged offset of slot bit b (slot m: XOR over its bits, then XOR the lane's)
-    uint16_t gsoff[16];       // staged offset of gate state s (offs[s] inside the tile)
-    uint16_t wbit[10];        // staged offset of each bit of a unit's number in the tile
+    // dense on states of >= 10 qubits: warp tiles of 1024 amplitudes
+    // (warp_tile.h); tile.tiled = 0 below that
+    WarpTile tile;
 };
-constexpr int kBatchTileBits = 10;
+
 struct BatchCircuit {
     uint64_t state_off;   // amplitude offset of column 0 (column 1 follows)
     uint64_t res_off;     // first classical word of this circuit's runs

@@ -276,6 +276,70 @@ def test_measure_all_identical_outcomes(prec, n):
         np.testing.assert_allclose(g.states(), o.states(), atol=1e-12 if prec == "c128" else 1e-6)
 
 
+def rand_unitary(d, rng):
+    z = rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))
+    q, r = np.linalg.qr(z)
+    return q * (np.diag(r) / np.abs(np.diag(r)))
+
+
+# qubit lists for 2-4 qubit blocks: the lowest and highest positions, runs and
+# scattered sets (qubit q is position n-1-q)
+TILE_QUBITS = [[-1, -2], [-4, -1], [0, -2], [3, 8], [-1, -2, -3], [2, 7, 0], [1, 5, -1], [-1, -2, -3, -4],
+               [0, 3, 7, -1], [1, 2, 6, 8]]
+
+
+@pytest.mark.parametrize("prec,tol", [("c128", TOL128), ("c64", TOL64)])
+@pytest.mark.parametrize("n", [9, 10, 13])
+def test_dense_blocks_in_warp_tiles_match_oracle(prec, tol, n):
+    """Uncontrolled dense blocks take the warp-tile kernels: complex64 blocks
+    of up to 4 qubits on states of 10+ qubits, complex128 blocks of up to 3
+    qubits on double-float pairs on states of 9+ qubits (4-qubit complex128
+    blocks keep the per-unit FP64 kernel).  Gate positions include 0 and the
+    state's top positions; a second round runs on two columns after a
+    measurement."""
+    rng = np.random.default_rng(300 + n)
+    shots = 64
+    o, g = pair(n, shots, rand_state(n, rng), prec)
+
+    def blocks():
+        for qs in TILE_QUBITS:
+            bits = [q % n for q in qs]
+            m = rand_unitary(1 << len(bits), rng)
+            o.apply_gate(m, bits)
+            g.apply_gate(m, bits)
+
+    blocks()
+    np.testing.assert_allclose(g.states(), o.states(), rtol=0, atol=tol)
+    u = np.array([0.5])
+    ro = np.zeros(shots, dtype=np.uint64)
+    rg = np.zeros(shots, dtype=np.uint64)
+    o.measure_into(n // 2, 3, ro, uniforms=u)
+    g.measure_into(n // 2, 3, rg, uniforms=u)
+    assert np.array_equal(ro, rg) and g.counts == o.counts
+    blocks()
+    assert g.counts == o.counts
+    np.testing.assert_allclose(g.states(), o.states(), rtol=0, atol=tol)
+
+
+def test_c128_dense_blocks_on_extreme_magnitudes():
+    """Tiled complex128 blocks: a unit with an amplitude of 2^126 or more is
+    done in FP64, amplitudes below 2^-126 are flushed; within 1e-12 of the
+    oracle relative to each amplitude's scale."""
+    rng = np.random.default_rng(79)
+    n = 11
+    amps = rand_state(n, rng)
+    amps[rng.random(1 << n) < 0.1] *= 1e-30
+    amps[rng.random(1 << n) < 0.03] *= 1e140
+    o, g = pair(n, 1, amps)
+    for qs in ([0, 1], [10, 3, 5], [9, 2]):
+        m = rand_unitary(1 << len(qs), rng)
+        o.apply_gate(m, qs)
+        g.apply_gate(m, qs)
+    so, sg = o.states()[:, 0], g.states()[:, 0]
+    err = np.abs(sg - so) / np.maximum(np.abs(so), 1.0)
+    assert float(np.max(err)) <= 1e-12, float(np.max(err))
+
+
 def test_rng_stream_matches_oracle():
     """The device-generated sorted uniforms agree with the oracle's host
     generation (same SplitMix64 stream); outcomes then agree except, with
