@@ -542,6 +542,25 @@ def main():
         accuracy = plain.compare(fused)
         plain_info = {"gates_per_s": ngates / (plain_ms / 1e3), "ms_per_circuit": plain_ms,
                       "fused_speedup": (ngates / (gate_ms_max / args.steps / 1e3)) / (ngates / (plain_ms / 1e3))}
+        # complex128 fused into 3-qubit blocks (double-float warp tiles)
+        f128 = VectorState(n, shots, "c128")
+        f128.set_stream(stream.cuda_stream)
+        fplan = Plan(n, bits, 3)
+        f128.apply_plan(fplan, mats)   # warm-up
+        f128.reset_all()
+        barrier()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        f128.apply_plan(fplan, mats)
+        f1.record(stream)
+        barrier()
+        f128_ms = f0.elapsed_time(f1)
+        acc128 = plain.compare(f128)
+        plain_info["fused_c128"] = {"fusion_width": 3, "blocks": fplan.nblocks, "ms_per_circuit": f128_ms,
+                                    "gates_per_s": ngates / (f128_ms / 1e3), "speedup_vs_plain": plain_ms / f128_ms,
+                                    "max_abs_diff_vs_plain": acc128["max_abs_diff"],
+                                    "infidelity_vs_plain": acc128["infidelity"]}
+        del f128
         del plain
 
     # ---- plain (unfused) gate kernels: the first layers, per-kernel profile
