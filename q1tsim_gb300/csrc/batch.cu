@@ -160,7 +160,7 @@ template <int TB>
 __device__ __forceinline__ void apply_dense(float2* a, uint64_t n_amps, const BatchOp& op, const float2* mat,
                                             float2* stage)
 {
-    if (op.tile.tiled) tiled_dense_c64<TB>(a, n_amps, op.tile, mat, stage, threadIdx.x >> 5, kBatchWarps);
+    if (op.tile.tiled) tiled_dense_c64<TB, true>(a, n_amps, op.tile, mat, stage, threadIdx.x >> 5, kBatchWarps);
     else dense_pass<TB>(a, n_amps, op, mat);
 }
 

@@ -45,7 +45,7 @@ k_dense_tiled_c64(float2* a, uint64_t total, const __grid_constant__ WarpTile ti
     for (int e = threadIdx.x; e < D * D; e += blockDim.x) mat[e] = gmat[e];
     __syncthreads();
     const int warp = threadIdx.x >> 5;
-    tiled_dense_c64<TB>(a, total, w, mat, stage_c64 + warp * 1024, (uint64_t)blockIdx.x * kTiledWarps + warp,
+    tiled_dense_c64<TB, false>(a, total, w, mat, stage_c64 + warp * 1024, (uint64_t)blockIdx.x * kTiledWarps + warp,
                         (uint64_t)gridDim.x * kTiledWarps);
 }
 
@@ -231,7 +231,9 @@ bool dense_tiled_applies(int prec, int nbits, int t, const IndexMap& map, bool f
 {
     if (map.nz != t || map.setmask != 0) return false;   // controls: the per-unit kernel
     if (prec == kC128) return !fp64_exact && t >= 1 && t <= 3 && nbits >= 9;
-    return t >= 1 && t <= 4 && nbits >= 10;
+    // complex64: the per-unit kernel is coalesced, and faster, for 1- and
+    // 2-qubit blocks whose gate positions are all >= 2
+    return t >= 1 && t <= 4 && nbits >= 10 && (t >= 3 || map.zpos[0] <= 1);
 }
 
 size_t dense_tiled_matrix_bytes(int prec, int t)

@@ -32,8 +32,10 @@ cudaError_t launch_dense(void* amps, int prec, uint64_t total, const IndexMap& m
                          const DenseOffsets& offs, int tb, const void* dmat, cudaStream_t st);
 
 // ---- dense_tiled.cu: uncontrolled dense blocks in warp tiles (warp_tile.h)
-// True when the tiled kernel takes the block: no controls, t <= 4 (complex64,
-// >= 10 qubits) or t <= 3 on double-float pairs (complex128, >= 9 qubits).
+// True when the tiled kernel takes the block: no controls; complex64 on
+// >= 10 qubits with t = 3 or 4, or t <= 2 with a gate at position 0 or 1
+// (higher 1-2 qubit blocks are coalesced, and faster, per unit); complex128
+// on >= 9 qubits with t <= 3 (double-float pairs).
 bool dense_tiled_applies(int prec, int nbits, int t, const IndexMap& map, bool fp64_exact);
 // The kernel's matrix image of a 2^t x 2^t complex matrix m (interleaved
 // doubles): complex64 entries, or complex128 double-float terms followed by

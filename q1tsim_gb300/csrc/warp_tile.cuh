@@ -69,12 +69,15 @@ __device__ __forceinline__ uint32_t lane_phys(const WarpTile& w, int lane)
 // Complex64 tile pass over tiles t0, t0 + tstride, ... of a state of
 // n_amps amplitudes (tile_bits 10: 1024 amplitudes, 8 KB of stage per warp).
 // w and mat (row-major 2^TB x 2^TB entries) are in shared memory.  A tile is
-// copied asynchronously into the warp's stage (8 bytes per lane and slot, or
-// 16 bytes covering two slots where w.pairs16), each lane applies the block
+// copied asynchronously into the warp's stage: 8 bytes per lane and slot, or,
+// where w.pairs16, 16 bytes covering two slots.  The 16-byte form saves
+// instructions where the arithmetic is heavy (4-qubit blocks); on one state,
+// lighter blocks measured faster with the 8-byte copies, so PAIRS_ANY_TB
+// false keeps it to 4-qubit blocks.  Each lane then applies the block
 // to 32 / 2^TB units, KB units and RB rows at a time so that one matrix entry
 // read serves KB units and 2 KB RB FMA chains are in flight, and the tile is
 // stored back.  Warps never synchronise with one another.
-template <int TB>
+template <int TB, bool PAIRS_ANY_TB>
 __device__ void tiled_dense_c64(float2* a, uint64_t n_amps, const WarpTile& w, const float2* mat, float2* stage,
                                 uint64_t t0, uint64_t tstride)
 {
@@ -105,7 +108,7 @@ __device__ void tiled_dense_c64(float2* a, uint64_t n_amps, const WarpTile& w, c
             sb[b] = lds_u32(&w.sbit[b]);
         }
         float2* amps = a + expand_index(t, w.tile_map);
-        if (w.pairs16) {
+        if ((PAIRS_ANY_TB || TB == 4) && w.pairs16) {
             const uint32_t gh = (lane & 16) ? gb[0] : 0u, sh = p16 ^ ((lane & 16) ? sb[0] : 0u);
             const float2* src = amps + 2 * (lane & 15) + gh;
 #pragma unroll
@@ -182,7 +185,7 @@ __device__ void tiled_dense_c64(float2* a, uint64_t n_amps, const WarpTile& w, c
             }
         }
         __syncwarp();
-        if (w.pairs16) {
+        if ((PAIRS_ANY_TB || TB == 4) && w.pairs16) {
             const uint32_t gh = (lane & 16) ? gb[0] : 0u, sh = p16 ^ ((lane & 16) ? sb[0] : 0u);
             float2* dst = amps + 2 * (lane & 15) + gh;
 #pragma unroll
