@@ -37,6 +37,7 @@ class Circuit:
         self._plans = {}
         self._frozen = None
         self._segs = None
+        self._flats = {}    # segment index -> (gates with reference parameters, their values, matrices)
 
     # ------------------------------------------------------------ building
     def _check_qbits(self, qbits):
@@ -54,6 +55,7 @@ class Circuit:
         self._plans.clear()
         self._frozen = None
         self._segs = None
+        self._flats = {}
 
     def freeze(self):
         """Evaluate every gate matrix now and reuse them on later executions
@@ -72,6 +74,21 @@ class Circuit:
     def _flat(seq):
         mats = [np.ascontiguousarray(op[1].matrix(), dtype=np.complex128).ravel() for op in seq]
         return np.concatenate(mats).view(np.float64) if mats else np.zeros(0)
+
+    def _flat_current(self, idx, seq):
+        """The segment's matrices for this execution.  They are evaluated
+        again only when a reference parameter of one of its gates has changed
+        (src/gates/parameter.rs:23-75); gates with plain values keep theirs."""
+        ent = self._flats.get(idx)
+        if ent is not None:
+            dyn, key, flat = ent
+            now = tuple(v for i in dyn for v in seq[i][1].param_key())
+            if now == key:
+                return flat
+        dyn = [i for i, op in enumerate(seq) if op[1].param_key()]
+        flat = self._flat(seq)
+        self._flats[idx] = (dyn, tuple(v for i in dyn for v in seq[i][1].param_key()), flat)
+        return flat
 
     @staticmethod
     def _gate(gate, params):
@@ -234,7 +251,7 @@ class Circuit:
 
     def _run_seq(self, q_state, idx, seq):
         if hasattr(q_state, "apply_plan"):
-            flat = self._frozen[idx] if self._frozen is not None else self._flat(seq)
+            flat = self._frozen[idx] if self._frozen is not None else self._flat_current(idx, seq)
             key = (idx, q_state.precision)
             plan = self._plans.get(key)
             if plan is None:

@@ -55,6 +55,11 @@ class Gate:
     def matrix(self):
         raise NotImplementedError
 
+    def param_key(self):
+        """Current values of the gate's reference parameters (Parameter
+        objects); () for a gate whose matrix cannot change."""
+        return ()
+
     def is_stabilizer(self):
         return False
 
@@ -146,6 +151,9 @@ class _Param(Gate):
     def matrix(self):
         return np.asarray(self._fn(*[_val(p) for p in self.params]), dtype=np.complex128)
 
+    def param_key(self):
+        return tuple(p.value for p in self.params if isinstance(p, Parameter))
+
 
 def _rx(theta):
     h = 0.5 * theta
@@ -225,6 +233,9 @@ class C(Gate):
         res[g:, g:] = gm
         return res
 
+    def param_key(self):
+        return self.gate.param_key()
+
     def is_stabilizer(self):
         return self.desc in ("CX", "CY", "CZ")
 
@@ -240,6 +251,9 @@ class Kron(Gate):
     def matrix(self):
         return np.kron(self.g0.matrix(), self.g1.matrix())
 
+    def param_key(self):
+        return self.g0.param_key() + self.g1.param_key()
+
 
 class Loop(Gate):
     """`gate` applied `count` times (src/gates/staticloop.rs:60-92)."""
@@ -251,6 +265,9 @@ class Loop(Gate):
 
     def matrix(self):
         return np.linalg.matrix_power(self.gate.matrix(), self.count)
+
+    def param_key(self):
+        return self.gate.param_key()
 
 
 class Composite(Gate):
@@ -271,6 +288,9 @@ class Composite(Gate):
         for g, bits in self.ops:
             m = embed(g.matrix(), bits, self.nbits) @ m
         return m
+
+    def param_key(self):
+        return tuple(v for g, _ in self.ops for v in g.param_key())
 
 
 def embed(mat, bits, nr_bits):

@@ -139,3 +139,25 @@ def test_binding_bases_and_conditional():
         assert np.all(cs & np.uint64(1) == 0)                        # peek of the reset qubit 2
         ones = int(((cs >> np.uint64(2)) & np.uint64(1)).sum())
         assert measurement_ok(ones, shots, 0.5, 1e-6)
+
+
+def test_segment_matrices_follow_reference_parameters():
+    """A circuit keeps each gate run's matrices between executions and
+    evaluates them again only when a reference parameter has changed
+    (src/gates/parameter.rs:23-75); plain values never change."""
+    from q1tsim_gb300 import Circuit as GpuCircuit
+    from q1tsim_gb300 import gates as G
+    p = q1tsim.RefParam(0.4)
+    c = GpuCircuit(2, 0, precision="c128", fusion_width=0)
+    c.add_gate(G.RX(p), [0])
+    c.add_gate(G.U3(0.1, 0.2, 0.3), [1])
+    c.add_gate(G.CRZ(p), [0, 1])
+    idx, seq = next((i, op[1]) for i, op in enumerate(c._segments()) if op[0] == "seq")
+    first = c._flat_current(idx, seq)
+    assert c._flat_current(idx, seq) is first
+    p.assign(-1.1)
+    second = c._flat_current(idx, seq)
+    assert second is not first
+    np.testing.assert_allclose(second, c._flat(seq), rtol=0, atol=0)
+    np.testing.assert_allclose(second[8:16], first[8:16], rtol=0, atol=0)   # the U3 block is unchanged
+    assert not np.array_equal(second[:8], first[:8])
