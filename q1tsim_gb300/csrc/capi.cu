@@ -411,6 +411,18 @@ int q1g_plan_info(const q1g_plan* p, size_t* ngates, size_t* nblocks)
     });
 }
 
+int q1g_plan_set_diagonal(q1g_plan* p, const unsigned char* diagonal, size_t ngates)
+{
+    return guarded([&] {
+        need(p, "plan");
+        if (ngates) need(diagonal, "diagonal");
+        if (ngates != p->gate_bits.size())
+            throw Error(Q1G_ERR_INVALID_ARGUMENT, "one diagonal flag per gate of the plan");
+        p->diagonal.assign(diagonal, diagonal + ngates);
+        if (p->width > 0) p->blocks = fuse_phase_runs(p->gate_bits, p->diagonal, p->nbits, p->width);
+    });
+}
+
 int q1g_plan_block(const q1g_plan* p, size_t i, size_t* qubits, size_t* nq, size_t* gates, size_t* ng)
 {
     return guarded([&] {
@@ -439,6 +451,8 @@ int q1g_plan_block_matrix(const q1g_plan* p, size_t i, const double* mats_flat, 
         if (n_doubles != p->mat_doubles)
             throw Error(Q1G_ERR_INVALID_ARGUMENT, "expected " + std::to_string(p->mat_doubles) + " matrix doubles");
         const auto& b = p->blocks[i];
+        if (b.phase_run || b.qubits.size() > 10)
+            throw Error(Q1G_ERR_INVALID_ARGUMENT, "a phase-run block has no dense matrix");
         const size_t dim = size_t(1) << b.qubits.size();
         if (*n_out < 2 * dim * dim) throw Error(Q1G_ERR_NOT_ENOUGH_SPACE, "output buffer too small");
         need(out, "out");

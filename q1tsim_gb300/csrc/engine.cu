@@ -724,6 +724,78 @@ static size_t union_size(const std::vector<int>& a, const std::vector<int>& b)
     return u.size();
 }
 
+// A phase-run block (fuse_phase_runs): on complex64 states of up to 32
+// qubits one pass of run_phase/phase_pair kernels with the block's phase
+// function (and its trailing 1-qubit gate); otherwise its gates one by one.
+// Each gate of the run must be diagonal with unit-modulus entries: its
+// log-phases theta_s over its (at most two) qubits contribute, by the Moebius
+// transform, a constant, one linear term per qubit and, for two qubits, the
+// product term, which contains the run's pivot.
+template <typename Stage>
+static void run_phase_block(q1g_plan* p, q1g_state* s, const FusedBlock& b, const std::vector<SeqGate>& gates,
+                            Stage&& stage)
+{
+    const int n = s->nbits;
+    const size_t ndiag = b.gates.size() - (b.trailing_pair ? 1 : 0);
+    if (s->prec != kC64 || n > 32) {
+        for (int g : b.gates) {
+            const GateOp op = classify(gates[g].mat.data(), (int)gates[g].bits.size(), gates[g].bits.data(), n);
+            if (op.kind != GateOp::Noop) s->apply_op(op, s->amps.as<char>(), s->total());
+        }
+        return;
+    }
+    const int pivot_q = phase_run_pivot(b, p->gate_bits);
+    const int pivot_pos = pivot_q >= 0 ? n - 1 - pivot_q : -1;
+    std::vector<double> lin0(n, 0.0), lin1(n, 0.0);
+    double c = 0.0;
+    for (size_t j = 0; j < ndiag; ++j) {
+        const SeqGate& g = gates[b.gates[j]];
+        const size_t k = g.bits.size(), dim = size_t(1) << k;
+        double th[4];
+        for (size_t r = 0; r < dim; ++r)
+            for (size_t col = 0; col < dim; ++col) {
+                const cd v = g.mat[r * dim + col];
+                if (r != col && v != cd(0.0, 0.0))
+                    throw Error(Q1G_ERR_INVALID_ARGUMENT, "a gate marked diagonal has an off-diagonal entry");
+                if (r == col) {
+                    if (std::abs(std::abs(v) - 1.0) > 1e-9)
+                        throw Error(Q1G_ERR_INVALID_ARGUMENT, "a gate marked diagonal is not a phase");
+                    th[r] = std::arg(v);
+                }
+            }
+        if (k == 1) {
+            c += th[0];
+            lin0[n - 1 - g.bits[0]] += th[1] - th[0];
+        } else {
+            // matrix index bit 1 = g.bits[0], bit 0 = g.bits[1]
+            c += th[0];
+            lin0[n - 1 - g.bits[0]] += th[2] - th[0];
+            lin0[n - 1 - g.bits[1]] += th[1] - th[0];
+            const double w = th[3] - th[2] - th[1] + th[0];
+            if (g.bits[0] == pivot_q) lin1[n - 1 - g.bits[1]] += w;
+            else if (g.bits[1] == pivot_q) lin1[n - 1 - g.bits[0]] += w;
+            else throw Error(Q1G_ERR_INVALID_ARGUMENT, "phase run without a common qubit");
+        }
+    }
+    std::vector<float2> tab(2048);
+    phase_run_tables(n, c, lin0.data(), lin1.data(), tab.data());
+    const void* dtab = stage(tab.data(), tab.size() * sizeof(float2));
+    int q_pos = -1;
+    double m2[8] = {1, 0, 0, 0, 0, 0, 1, 0};
+    if (b.trailing_pair) {
+        const SeqGate& t = gates[b.gates.back()];
+        q_pos = n - 1 - t.bits[0];
+        for (int e = 0; e < 4; ++e) {
+            m2[2 * e] = t.mat[e].real();
+            m2[2 * e + 1] = t.mat[e].imag();
+        }
+    }
+    const uint64_t total = s->total();
+    s->launch(b.trailing_pair ? "phase_pair_run_c64" : "phase_run_c64", 2.0 * total * s->bsz(), [&] {
+        return launch_phase_run(s->amps.as<float2>(), total, n, pivot_pos, dtab, q_pos, m2, s->sm_count(), s->stream);
+    });
+}
+
 void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n)
 {
     if (n != p->mat_doubles)
@@ -764,6 +836,7 @@ void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n)
     };
     // tensor-core eligible: dense blocks of >= 3 target qubits
     auto eligible = [&](size_t bi) {
+        if (p->blocks[bi].phase_run) return false;
         prepare(bi);
         return use_tc && ops[bi].kind == GateOp::Dense && ops[bi].t >= 3 && bbits[bi].size() <= 5;
     };
@@ -788,6 +861,11 @@ void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n)
         launched = true;
     };
     for (size_t i = 0; i < nb; ++i) {
+        if (p->blocks[i].phase_run) {
+            begin();
+            run_phase_block(p, s, p->blocks[i], gates, stage);
+            continue;
+        }
         prepare(i);
         const GateOp& op = ops[i];
         if (op.kind == GateOp::Noop) continue;

@@ -289,4 +289,80 @@ std::vector<FusedBlock> fuse(const std::vector<std::vector<int>>& gate_bits, int
     return res;
 }
 
+int phase_run_pivot(const FusedBlock& b, const std::vector<std::vector<int>>& gate_bits)
+{
+    std::vector<int> common;
+    bool any = false;
+    const size_t ndiag = b.gates.size() - (b.trailing_pair ? 1 : 0);
+    for (size_t j = 0; j < ndiag; ++j) {
+        const auto& q = gate_bits[b.gates[j]];
+        if (q.size() != 2) continue;
+        std::vector<int> s = q;
+        std::sort(s.begin(), s.end());
+        if (!any) {
+            common = s;
+            any = true;
+        } else {
+            std::vector<int> c;
+            std::set_intersection(common.begin(), common.end(), s.begin(), s.end(), std::back_inserter(c));
+            common.swap(c);
+        }
+    }
+    if (!any) return -1;
+    return common.empty() ? -2 : common[0];
+}
+
+std::vector<FusedBlock> fuse_phase_runs(const std::vector<std::vector<int>>& gate_bits,
+                                        const std::vector<unsigned char>& diagonal, int nbits, int width)
+{
+    const int ng = (int)gate_bits.size();
+    std::vector<FusedBlock> out;
+    std::vector<int> pending;   // regular gates since the last run
+    auto flush = [&] {
+        if (pending.empty()) return;
+        std::vector<std::vector<int>> sub;
+        for (int g : pending) sub.push_back(gate_bits[g]);
+        for (auto b : fuse(sub, nbits, width)) {
+            for (auto& gi : b.gates) gi = pending[gi];
+            out.push_back(b);
+        }
+        pending.clear();
+    };
+    int i = 0;
+    while (i < ng) {
+        if (!diagonal[i]) {
+            pending.push_back(i++);
+            continue;
+        }
+        int j = i;
+        bool small = true;
+        while (j < ng && diagonal[j]) {
+            small = small && gate_bits[j].size() <= 2;
+            ++j;
+        }
+        FusedBlock run;
+        run.phase_run = true;
+        for (int g = i; g < j; ++g) run.gates.push_back(g);
+        if (j - i < kMinPhaseRun || !small || phase_run_pivot(run, gate_bits) == -2) {
+            for (int g = i; g < j; ++g) pending.push_back(g);
+            i = j;
+            continue;
+        }
+        if (j < ng && gate_bits[j].size() == 1) {
+            run.gates.push_back(j);
+            run.trailing_pair = true;
+            ++j;
+        }
+        for (int g : run.gates)
+            for (int q : gate_bits[g])
+                if (std::find(run.qubits.begin(), run.qubits.end(), q) == run.qubits.end()) run.qubits.push_back(q);
+        std::sort(run.qubits.begin(), run.qubits.end());
+        flush();
+        out.push_back(run);
+        i = j;
+    }
+    flush();
+    return out;
+}
+
 }  // namespace q1g

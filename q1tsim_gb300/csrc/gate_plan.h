@@ -46,6 +46,10 @@ struct SeqGate {
 struct FusedBlock {
     std::vector<int> qubits;
     std::vector<int> gates;
+    // A run of diagonal gates applied as one phase function (fuse_phase_runs),
+    // its last gate a non-diagonal 1-qubit gate when trailing_pair is set.
+    bool phase_run = false;
+    bool trailing_pair = false;
 };
 
 // Greedy fusion over open blocks on disjoint qubit sets: a gate joins the
@@ -55,6 +59,22 @@ struct FusedBlock {
 // when every block in between is disjoint from it.  Only the qubit lists are
 // used, so the grouping can be computed once per circuit structure.
 std::vector<FusedBlock> fuse(const std::vector<std::vector<int>>& gate_bits, int nbits, int width);
+
+// Shortest run of consecutive diagonal gates taken as one phase pass.
+constexpr int kMinPhaseRun = 3;
+
+// fuse() with runs of diagonal gates (diagonal[g] != 0) taken out first: a
+// run of at least kMinPhaseRun consecutive diagonal gates, none on more than
+// two qubits and every two-qubit one sharing a common qubit (the pivot), is
+// one phase-run block; its phase is c + L0(x) + x_pivot L1(x) with L0, L1
+// linear in the basis bits.  A non-diagonal 1-qubit gate directly after the
+// run joins it (applied after the phases in the same pass).  The gates
+// between runs are fused by fuse(); blocks never cross a run.
+std::vector<FusedBlock> fuse_phase_runs(const std::vector<std::vector<int>>& gate_bits,
+                                        const std::vector<unsigned char>& diagonal, int nbits, int width);
+
+// Qubit shared by every two-qubit gate of a phase run (-1 when it has none).
+int phase_run_pivot(const FusedBlock& b, const std::vector<std::vector<int>>& gate_bits);
 
 // Matrix of a block: product of its gates' matrices embedded on its qubits.
 std::vector<cd> block_matrix(const FusedBlock& b, const std::vector<SeqGate>& gates);

@@ -31,6 +31,15 @@ cudaError_t launch_phase(void* amps, int prec, uint64_t total, const IndexMap& m
 cudaError_t launch_dense(void* amps, int prec, uint64_t total, const IndexMap& map,
                          const DenseOffsets& offs, int tb, const void* dmat, cudaStream_t st);
 
+// ---- phase_run.cu: a run of diagonal gates as one pass (complex64, <= 32 qubits)
+// out: the 2048 complex factors of phi = c + L0 + x_pivot L1, lin0/lin1 the
+// coefficients of L0/L1 per bit position (nbits each).
+void phase_run_tables(int nbits, double c, const double* lin0, const double* lin1, float2* out);
+// pivot_pos -1: no x_pivot term.  q_pos >= 0: then the 2x2 matrix m2 ((re, im)
+// row-major) on the pairs along position q_pos, in the same pass.
+cudaError_t launch_phase_run(float2* amps, uint64_t total, int nbits, int pivot_pos, const void* dtab, int q_pos,
+                             const double* m2, int sm_count, cudaStream_t st);
+
 // ---- dense_tiled.cu: uncontrolled dense blocks in warp tiles (warp_tile.h)
 // True when the tiled kernel takes the block: no controls; complex64 on
 // >= 10 qubits with t = 3 or 4, or t <= 2 with a gate at position 0 or 1

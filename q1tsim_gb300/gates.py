@@ -60,6 +60,10 @@ class Gate:
         objects); () for a gate whose matrix cannot change."""
         return ()
 
+    def is_diagonal(self):
+        """True when the matrix is diagonal for every parameter value."""
+        return False
+
     def is_stabilizer(self):
         return False
 
@@ -76,6 +80,9 @@ class _Fixed(Gate):
 
     def matrix(self):
         return self._m.copy()
+
+    def is_diagonal(self):
+        return bool(np.count_nonzero(self._m - np.diag(np.diag(self._m))) == 0)
 
     def is_stabilizer(self):
         return self._stab
@@ -142,17 +149,21 @@ def Swap():
 
 
 class _Param(Gate):
-    def __init__(self, desc, fn, params, nbits=1):
+    def __init__(self, desc, fn, params, nbits=1, diagonal=False):
         self.desc = desc
         self._fn = fn
         self.params = list(params)
         self.nbits = nbits
+        self._diagonal = diagonal
 
     def matrix(self):
         return np.asarray(self._fn(*[_val(p) for p in self.params]), dtype=np.complex128)
 
     def param_key(self):
         return tuple(p.value for p in self.params if isinstance(p, Parameter))
+
+    def is_diagonal(self):
+        return self._diagonal
 
 
 def _rx(theta):
@@ -199,12 +210,12 @@ def RY(theta):
 
 def RZ(lmb):
     """src/gates/rz.rs:65-70"""
-    return _Param("RZ", _rz, [lmb])
+    return _Param("RZ", _rz, [lmb], diagonal=True)
 
 
 def U1(lmb):
     """src/gates/u1.rs:69-75"""
-    return _Param("U1", _u1, [lmb])
+    return _Param("U1", _u1, [lmb], diagonal=True)
 
 
 def U2(phi, lmb):
@@ -236,6 +247,9 @@ class C(Gate):
     def param_key(self):
         return self.gate.param_key()
 
+    def is_diagonal(self):
+        return self.gate.is_diagonal()
+
     def is_stabilizer(self):
         return self.desc in ("CX", "CY", "CZ")
 
@@ -254,6 +268,9 @@ class Kron(Gate):
     def param_key(self):
         return self.g0.param_key() + self.g1.param_key()
 
+    def is_diagonal(self):
+        return self.g0.is_diagonal() and self.g1.is_diagonal()
+
 
 class Loop(Gate):
     """`gate` applied `count` times (src/gates/staticloop.rs:60-92)."""
@@ -268,6 +285,9 @@ class Loop(Gate):
 
     def param_key(self):
         return self.gate.param_key()
+
+    def is_diagonal(self):
+        return self.gate.is_diagonal()
 
 
 class Composite(Gate):
@@ -291,6 +311,9 @@ class Composite(Gate):
 
     def param_key(self):
         return tuple(v for g, _ in self.ops for v in g.param_key())
+
+    def is_diagonal(self):
+        return all(g.is_diagonal() for g, _ in self.ops)
 
 
 def embed(mat, bits, nr_bits):

@@ -142,3 +142,53 @@ def test_plain_plan_is_one_pass_per_gate(lib):
     p = Plan(8, gb, fusion_width=0)
     assert p.nblocks == len(gb)
     assert [gs for _, gs in p.blocks()] == [[i] for i in range(len(gb))]
+
+
+def _qft_structure(n):
+    from q1tsim_gb300 import workloads
+    q = workloads.qft(n, precision="c64", fusion_width=5, measure=False)
+    seq = [op for op in q.ops if op[0] == "gate"]
+    return [op[2] for op in seq], [op[1].is_diagonal() for op in seq]
+
+
+@pytest.mark.parametrize("n", [6, 12, 28])
+def test_phase_runs_group_the_qft_ladders(lib, n):
+    """With the diagonal gates marked, each QFT ladder of controlled phases
+    (all sharing the target qubit) becomes one phase-run pass together with
+    the next Hadamard; every gate appears once, in order."""
+    bits, diag = _qft_structure(n)
+    plan = Plan(n, bits, 5, diagonal=diag)
+    blocks = plan.blocks()
+    order = [g for _, gates in blocks for g in gates]
+    assert sorted(order) == list(range(len(bits)))
+    runs = [(qb, gates) for qb, gates in blocks if len(gates) >= 4 and len(qb) > 5]
+    assert len(runs) >= n - 6
+    for qb, gates in runs:
+        ladder = [g for g in gates if diag[g]]
+        assert len(ladder) >= 3
+        common = set(bits[ladder[0]])
+        for g in ladder:
+            common &= set(bits[g])
+        assert common   # one qubit shared by the whole ladder
+        # the absorbed gate is the non-diagonal 1-qubit gate right after the ladder
+        tail = [g for g in gates if not diag[g]]
+        assert tail == [] or (tail == [gates[-1]] and len(bits[tail[0]]) == 1 and tail[0] == ladder[-1] + 1)
+    assert plan.nblocks < Plan(n, bits, 5).nblocks or n < 8
+
+
+def test_phase_runs_need_a_common_qubit(lib):
+    """A run of diagonal two-qubit gates without a common qubit (a ring of
+    controlled phases) stays with the ordinary fusion."""
+    n = 8
+    bits = [[q, (q + 1) % n] for q in range(n)]
+    diag = [True] * n
+    plain = Plan(n, bits, 5).blocks()
+    marked = Plan(n, bits, 5, diagonal=diag).blocks()
+    assert marked == plain
+
+
+def test_plan_set_diagonal_checks_its_arguments(lib):
+    plan = Plan(4, [[0], [1, 2]], 3)
+    flags = (ctypes.c_ubyte * 1)(1)
+    assert lib.q1g_plan_set_diagonal(plan.handle, flags, 1) != 0    # one flag for two gates
+    assert lib.q1g_plan_set_diagonal(None, flags, 1) != 0

@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle as orc
-from q1tsim_gb300 import Circuit, Plan, Rng, VectorState
+from q1tsim_gb300 import Circuit, Plan, Rng, VectorState, workloads
 from q1tsim_gb300 import _lib
 from q1tsim_gb300 import gates as G
 from refcheck import dec, kats, measurement_ok
@@ -338,6 +338,82 @@ def test_c128_dense_blocks_on_extreme_magnitudes():
     so, sg = o.states()[:, 0], g.states()[:, 0]
     err = np.abs(sg - so) / np.maximum(np.abs(so), 1.0)
     assert float(np.max(err)) <= 1e-12, float(np.max(err))
+
+
+def _run_plan(n, gates, width, prec, amps, diagonal=True):
+    bits = [b for _, b in gates]
+    mats = np.concatenate([np.ascontiguousarray(g.matrix()).ravel() for g, _ in gates]).view(np.float64)
+    st = VectorState.from_amplitudes(amps, 1, prec)
+    flags = [g.is_diagonal() for g, _ in gates] if diagonal else None
+    st.apply_plan(Plan(n, bits, width, diagonal=flags), mats)
+    return st
+
+
+@pytest.mark.parametrize("n", [10, 13])
+def test_qft_phase_runs_match_oracle(n):
+    """The QFT with its controlled-phase ladders as phase-run passes (each
+    with the next Hadamard), complex64 fused: against the complex128 oracle
+    on a random state, as configs[1] runs it."""
+    rng = np.random.default_rng(400 + n)
+    amps = rand_state(n, rng)
+    q = workloads.qft(n, precision="c64", fusion_width=5, measure=False)
+    gates = [(op[1], op[2]) for op in q.ops if op[0] == "gate"]
+    o = orc.OracleState.from_amplitudes(amps, 1)
+    for g, b in gates:
+        o.apply_gate(g.matrix(), b)
+    g64 = _run_plan(n, gates, 5, "c64", amps)
+    so, sg = o.states()[:, 0], g64.states()[:, 0]
+    assert float(np.max(np.abs(sg - so))) <= TOL64
+    assert 1.0 - abs(np.vdot(so, sg)) ** 2 <= 1e-6
+
+
+def test_random_phase_runs_match_oracle():
+    """Runs of phases (RZ, T, S, Z, U1) and controlled phases (CU1, CZ, CRZ,
+    CS) around a common qubit, between U3 and CX layers; some runs end in a
+    1-qubit gate, one has no common qubit and stays fused as usual.
+    complex64 against the oracle; complex128 (runs applied gate by gate)
+    within 1e-12."""
+    n = 12
+    rng = np.random.default_rng(401)
+    amps = rand_state(n, rng)
+    gates = []
+    for layer in range(6):
+        for q in range(n):
+            gates.append((G.U3(*rng.uniform(0, 2 * np.pi, 3)), [q]))
+        pivot = int(rng.integers(n))
+        for _ in range(int(rng.integers(3, 9))):
+            kind = int(rng.integers(6))
+            other = int(rng.choice([q for q in range(n) if q != pivot]))
+            pair = [pivot, other] if rng.random() < 0.5 else [other, pivot]
+            g = [G.CU1(rng.uniform(0, 6.3)), G.CZ(), G.CRZ(rng.uniform(0, 6.3)), G.CS(),
+                 G.RZ(rng.uniform(0, 6.3)), G.T()][kind]
+            gates.append((g, pair if kind < 4 else [int(rng.integers(n))]))
+        if layer % 2:
+            gates.append((G.H(), [int(rng.integers(n))]))
+        for q in range(layer % 2, n - 1, 2):
+            gates.append((G.CX(), [q, q + 1]))
+    gates += [(G.CZ(), [q, (q + 1) % n]) for q in range(n)]   # no common qubit
+    o = orc.OracleState.from_amplitudes(amps, 1)
+    for g, b in gates:
+        o.apply_gate(g.matrix(), b)
+    so = o.states()[:, 0]
+    s64 = _run_plan(n, gates, 5, "c64", amps).states()[:, 0]
+    assert float(np.max(np.abs(s64 - so))) <= TOL64
+    s128 = _run_plan(n, gates, 3, "c128", amps).states()[:, 0]
+    assert float(np.max(np.abs(s128 - so))) <= TOL128
+
+
+def test_gate_wrongly_marked_diagonal_is_an_error():
+    """A plan whose diagonal flags mark a non-diagonal gate fails at run time
+    with an error, before any launch of that pass."""
+    n = 10
+    gates = [(G.CU1(0.3), [0, 1]), (G.CU1(0.4), [0, 2]), (G.H(), [0]), (G.CU1(0.5), [0, 3])]
+    bits = [b for _, b in gates]
+    mats = np.concatenate([np.ascontiguousarray(g.matrix()).ravel() for g, _ in gates]).view(np.float64)
+    st = VectorState(n, 1, "c64")
+    plan = Plan(n, bits, 5, diagonal=[True, True, True, True])
+    with pytest.raises(Exception):
+        st.apply_plan(plan, mats)
 
 
 def test_rng_stream_matches_oracle():
