@@ -464,8 +464,13 @@ void q1g_state::measure_all(const size_t* cbits, size_t ncbits, uint64_t* res, s
         return w;
     };
 
-    std::vector<uint64_t> outc(nshots);
+    // per-run outcome indices: the pinned download of the dense sampler, or
+    // the basis columns of a sparse state
+    std::vector<uint64_t> outc;
+    const uint64_t* h_outc = nullptr;
     if (sparse) {
+        outc.resize(nshots);
+        h_outc = outc.data();
         uint64_t off = 0;
         for (uint64_t c = 0; c < ncols; ++c) {
             for (uint64_t r = 0; r < counts[c]; ++r) outc[off + r] = basis[c];
@@ -544,29 +549,29 @@ void q1g_state::measure_all(const size_t* cbits, size_t ncbits, uint64_t* res, s
         check_cuda(cudaMemcpyAsync(hstage.p, d_out, 2 * nshots * sizeof(uint64_t), cudaMemcpyDeviceToHost, stream),
                    "download outcomes");
         sync();
-        const uint64_t* h_out = hstage.as<uint64_t>();
-        const uint64_t* h_word = h_out + nshots;
-        std::memcpy(outc.data(), h_out, nshots * sizeof(uint64_t));
+        h_outc = hstage.as<uint64_t>();
+        const uint64_t* h_word = h_outc + nshots;
         for (uint64_t r = 0; r < nshots; ++r) res[r] = (res[r] & mask) | h_word[r];
     }
     if (!collapse) return;
-    // one basis column per distinct (column, outcome), in order
-    std::vector<uint64_t> nb, nc;
+    // one basis column per distinct (column, outcome), in order, written into
+    // basis/counts themselves: their capacity carries over between runs
+    const std::vector<uint64_t> runs(counts.begin(), counts.end());
+    basis.clear();
+    counts.clear();
     uint64_t off = 0;
-    for (uint64_t c = 0; c < ncols; ++c) {
-        for (uint64_t r = 0; r < counts[c]; ++r) {
-            if (r == 0 || outc[off + r] != outc[off + r - 1]) {
-                nb.push_back(outc[off + r]);
-                nc.push_back(0);
+    for (uint64_t c = 0; c < runs.size(); ++c) {
+        for (uint64_t r = 0; r < runs[c]; ++r) {
+            if (r == 0 || h_outc[off + r] != h_outc[off + r - 1]) {
+                basis.push_back(h_outc[off + r]);
+                counts.push_back(0);
             }
-            nc.back() += 1;
+            counts.back() += 1;
         }
-        off += counts[c];
+        off += runs[c];
     }
     sparse = true;
-    basis = nb;
-    counts = nc;
-    ncols = nb.size();
+    ncols = basis.size();
     norms.assign(ncols, 1.0);
 }
 
