@@ -166,13 +166,13 @@ def qft_leg(args):
     amps /= np.linalg.norm(amps)
     qc = workloads.qft(n, measure=False)
     bits = [op[2] for op in qc.ops]
-    diagonal = [op[1].is_diagonal() for op in qc.ops]   # the controlled-phase ladders
+    kinds = [op[1].plan_kind() for op in qc.ops]   # controlled-phase ladders, final swaps
     mats = np.concatenate([np.ascontiguousarray(op[1].matrix()).ravel() for op in qc.ops]).view(np.float64)
     out = {"workload": f"QFT ({len(bits)} gates: H, CU1(pi/2^k), Swap) on a random N(0,1) {n}-qubit state",
            "gates": len(bits)}
     for prec, width in (("c128", 0), ("c64", args.fusion)):
         st = VectorState.from_amplitudes(amps, 1, prec)
-        plan = Plan(n, bits, width, diagonal=diagonal if width else None)
+        plan = Plan(n, bits, width, kinds=kinds if width else None)
         st.apply_plan(plan, mats)      # warm-up
         st2 = VectorState.from_amplitudes(amps, 1, prec)
         st2.synchronize()

@@ -163,15 +163,21 @@ int q1g_plan_create(size_t nr_bits, size_t ngates, const size_t* ks, const size_
                     int fusion_width, q1g_plan** out);
 void q1g_plan_free(q1g_plan* p);
 /* Number of passes (fused blocks or single gates) the plan launches. */
-/* Marks the gates whose matrices are always diagonal (diagonal[g] != 0 for
- * gate g), e.g. phases and controlled phases, and regroups a fused plan:
- * a run of at least 3 consecutive diagonal gates on at most two qubits each,
- * whose two-qubit gates share one qubit, becomes one pass that multiplies
- * every amplitude by the run's phase function, together with a following
- * 1-qubit gate (complex64 states of up to 32 qubits; other states apply the
- * run gate by gate).  q1g_plan_run then fails with Q1G_ERR_INVALID_ARGUMENT
- * if a marked gate's matrix is not a diagonal of unit-modulus entries. */
-int q1g_plan_set_diagonal(q1g_plan* p, const unsigned char* diagonal, size_t ngates);
+/* Tells a plan what some of its gates always are, and regroups a fused plan
+ * (fusion_width > 0) around them:
+ * - Q1G_GATE_DIAGONAL (phases, controlled phases): a run of at least 3
+ *   consecutive diagonal gates on at most two qubits each, whose two-qubit
+ *   gates share one qubit, becomes one pass that multiplies every amplitude
+ *   by the run's phase function, together with a following 1-qubit gate
+ *   (complex64 states of up to 32 qubits; other states apply the run gate by
+ *   gate);
+ * - Q1G_GATE_SWAP: a run of at least 2 consecutive swaps on disjoint qubit
+ *   pairs becomes one permutation pass (states of 10 qubits or more).
+ * q1g_plan_run fails with Q1G_ERR_INVALID_ARGUMENT if a marked gate's matrix
+ * is not what its kind says (a diagonal of unit-modulus entries, the swap
+ * permutation). */
+enum q1g_gate_kind { Q1G_GATE_GENERAL = 0, Q1G_GATE_DIAGONAL = 1, Q1G_GATE_SWAP = 2 };
+int q1g_plan_set_gate_kinds(q1g_plan* p, const unsigned char* kinds, size_t ngates);
 int q1g_plan_info(const q1g_plan* p, size_t* ngates, size_t* nblocks);
 /* Block i of the plan: its qubits (ascending; *nq in/out) and the indices of
  * the gates it absorbed, in application order (*ng in/out). */

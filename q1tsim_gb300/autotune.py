@@ -23,10 +23,10 @@ def structure_key(nr_bits, precision, gate_bits):
     return (nr_bits, precision, hash(tuple(tuple(b) for b in gate_bits)))
 
 
-def tune(nr_bits, precision, gate_bits, mats_flat, reps=2, candidates=None, diagonal=None):
+def tune(nr_bits, precision, gate_bits, mats_flat, reps=2, candidates=None, kinds=None):
     """Best (fusion_width, tensor_cores) for this structure, by device time.
-    diagonal: per gate, True for always-diagonal gates (phase runs)."""
-    key = structure_key(nr_bits, precision, gate_bits) + (tuple(bool(d) for d in diagonal or ()),)
+    kinds: per gate, Plan.KIND_* (phase and swap runs)."""
+    key = structure_key(nr_bits, precision, gate_bits) + (tuple(int(k) for k in kinds or ()),)
     if key in _cache:
         return _cache[key]
     if candidates is None:
@@ -34,7 +34,7 @@ def tune(nr_bits, precision, gate_bits, mats_flat, reps=2, candidates=None, diag
     scratch = VectorState(nr_bits, 1, precision)
     timings = []
     for width, tc in candidates:
-        plan = Plan(nr_bits, gate_bits, width, tensor_cores=tc, diagonal=diagonal)
+        plan = Plan(nr_bits, gate_bits, width, tensor_cores=tc, kinds=kinds)
         scratch.reset_all()
         scratch.apply_plan(plan, mats_flat)          # warm-up: first touch, caches
         scratch.synchronize()

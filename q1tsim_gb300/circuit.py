@@ -256,16 +256,16 @@ class Circuit:
             plan = self._plans.get(key)
             if plan is None:
                 bits = [op[2] for op in seq]
-                diagonal = [op[1].is_diagonal() for op in seq]
+                kinds = [op[1].plan_kind() for op in seq]
                 width, tc = self.fusion_width, True
                 if width == "auto":
                     from . import autotune
-                    width, tc = autotune.tune(self.nr_qbits, q_state.precision, bits, flat, diagonal=diagonal)
+                    width, tc = autotune.tune(self.nr_qbits, q_state.precision, bits, flat, kinds=kinds)
                 if q_state.precision == "c128" and width > 3:
                     # complex128 blocks of up to 3 qubits run on double-float
                     # pairs in warp tiles; larger ones would take the FP64 pipe
                     width = 3
-                plan = Plan(self.nr_qbits, bits, width, tensor_cores=tc, diagonal=diagonal)
+                plan = Plan(self.nr_qbits, bits, width, tensor_cores=tc, kinds=kinds)
                 self._plans[key] = plan
             q_state.apply_plan(plan, flat)
         else:

@@ -411,15 +411,20 @@ int q1g_plan_info(const q1g_plan* p, size_t* ngates, size_t* nblocks)
     });
 }
 
-int q1g_plan_set_diagonal(q1g_plan* p, const unsigned char* diagonal, size_t ngates)
+int q1g_plan_set_gate_kinds(q1g_plan* p, const unsigned char* kinds, size_t ngates)
 {
     return guarded([&] {
         need(p, "plan");
-        if (ngates) need(diagonal, "diagonal");
+        if (ngates) need(kinds, "kinds");
         if (ngates != p->gate_bits.size())
-            throw Error(Q1G_ERR_INVALID_ARGUMENT, "one diagonal flag per gate of the plan");
-        p->diagonal.assign(diagonal, diagonal + ngates);
-        if (p->width > 0) p->blocks = fuse_phase_runs(p->gate_bits, p->diagonal, p->nbits, p->width);
+            throw Error(Q1G_ERR_INVALID_ARGUMENT, "one kind per gate of the plan");
+        for (size_t g = 0; g < ngates; ++g) {
+            if (kinds[g] > Q1G_GATE_SWAP) throw Error(Q1G_ERR_INVALID_ARGUMENT, "unknown gate kind");
+            if (kinds[g] == Q1G_GATE_SWAP && p->gate_bits[g].size() != 2)
+                throw Error(Q1G_ERR_INVALID_ARGUMENT, "a swap acts on two qubits");
+        }
+        p->kinds.assign(kinds, kinds + ngates);
+        if (p->width > 0) p->blocks = fuse_runs(p->gate_bits, p->kinds, p->nbits, p->width);
     });
 }
 

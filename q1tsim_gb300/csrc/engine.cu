@@ -7,6 +7,7 @@
 #include "engine.h"
 
 #include <algorithm>
+#include <memory>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -729,7 +730,42 @@ static size_t union_size(const std::vector<int>& a, const std::vector<int>& b)
     return u.size();
 }
 
-// A phase-run block (fuse_phase_runs): on complex64 states of up to 32
+// A swap-run block (fuse_runs): every gate must be the swap permutation;
+// one permutation pass (swap_run.cu), or the swaps one by one when the
+// state has fewer than 10 qubits.
+template <typename Stage>
+static void run_swap_block(q1g_state* s, const FusedBlock& b, const std::vector<SeqGate>& gates, Stage&& stage)
+{
+    const int n = s->nbits;
+    std::vector<int> pa, pb;
+    for (int g : b.gates) {
+        const SeqGate& q = gates[g];
+        if (q.bits.size() != 2) throw Error(Q1G_ERR_INVALID_ARGUMENT, "a gate marked swap acts on two qubits");
+        for (int r = 0; r < 4; ++r)
+            for (int c = 0; c < 4; ++c) {
+                const bool one = (r == c && (r == 0 || r == 3)) || (r == 1 && c == 2) || (r == 2 && c == 1);
+                if (q.mat[4 * r + c] != cd(one ? 1.0 : 0.0, 0.0))
+                    throw Error(Q1G_ERR_INVALID_ARGUMENT, "a gate marked swap is not the swap");
+            }
+        pa.push_back(n - 1 - q.bits[0]);
+        pb.push_back(n - 1 - q.bits[1]);
+    }
+    auto t = std::make_unique<SwapTile>();
+    if (!swap_run_layout(*t, pa.data(), pb.data(), (int)pa.size(), n, (int)amp_bytes(s->prec))) {
+        for (int g : b.gates) {
+            const GateOp op = classify(gates[g].mat.data(), 2, gates[g].bits.data(), n);
+            if (op.kind != GateOp::Noop) s->apply_op(op, s->amps.as<char>(), s->total());
+        }
+        return;
+    }
+    const void* dt = stage(t.get(), sizeof(SwapTile));
+    const uint64_t total = s->total();
+    s->launch("swap_run", 2.0 * total * s->bsz(), [&] {
+        return launch_swap_run(s->amps.p, (int)amp_bytes(s->prec), total, dt, s->sm_count(), s->stream);
+    });
+}
+
+// A phase-run block (fuse_runs): on complex64 states of up to 32
 // qubits one pass of run_phase/phase_pair kernels with the block's phase
 // function (and its trailing 1-qubit gate); otherwise its gates one by one.
 // Each gate of the run must be diagonal with unit-modulus entries: its
@@ -841,7 +877,7 @@ void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n)
     };
     // tensor-core eligible: dense blocks of >= 3 target qubits
     auto eligible = [&](size_t bi) {
-        if (p->blocks[bi].phase_run) return false;
+        if (p->blocks[bi].phase_run || p->blocks[bi].swap_run) return false;
         prepare(bi);
         return use_tc && ops[bi].kind == GateOp::Dense && ops[bi].t >= 3 && bbits[bi].size() <= 5;
     };
@@ -869,6 +905,11 @@ void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n)
         if (p->blocks[i].phase_run) {
             begin();
             run_phase_block(p, s, p->blocks[i], gates, stage);
+            continue;
+        }
+        if (p->blocks[i].swap_run) {
+            begin();
+            run_swap_block(s, p->blocks[i], gates, stage);
             continue;
         }
         prepare(i);

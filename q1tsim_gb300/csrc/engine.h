@@ -163,7 +163,7 @@ struct q1g_plan {
     std::vector<size_t> mat_off;   // offset (doubles) of each gate's matrix
     size_t mat_doubles = 0;
     std::vector<q1g::FusedBlock> blocks;
-    std::vector<unsigned char> diagonal;   // per gate: its matrix is always diagonal (phase runs)
+    std::vector<unsigned char> kinds;      // per gate: q1g::GateKind (phase runs, swap runs)
     q1g::HostBuf hmats;            // pinned staging of dense matrices
     q1g::DevBuf dmats;
     cudaEvent_t staged = nullptr;  // last upload of hmats finished

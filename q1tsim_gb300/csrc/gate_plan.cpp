@@ -312,8 +312,8 @@ int phase_run_pivot(const FusedBlock& b, const std::vector<std::vector<int>>& ga
     return common.empty() ? -2 : common[0];
 }
 
-std::vector<FusedBlock> fuse_phase_runs(const std::vector<std::vector<int>>& gate_bits,
-                                        const std::vector<unsigned char>& diagonal, int nbits, int width)
+std::vector<FusedBlock> fuse_runs(const std::vector<std::vector<int>>& gate_bits,
+                                  const std::vector<unsigned char>& kinds, int nbits, int width)
 {
     const int ng = (int)gate_bits.size();
     std::vector<FusedBlock> out;
@@ -328,15 +328,46 @@ std::vector<FusedBlock> fuse_phase_runs(const std::vector<std::vector<int>>& gat
         }
         pending.clear();
     };
+    auto emit = [&](FusedBlock& run) {
+        for (int g : run.gates)
+            for (int q : gate_bits[g])
+                if (std::find(run.qubits.begin(), run.qubits.end(), q) == run.qubits.end()) run.qubits.push_back(q);
+        std::sort(run.qubits.begin(), run.qubits.end());
+        flush();
+        out.push_back(run);
+    };
     int i = 0;
     while (i < ng) {
-        if (!diagonal[i]) {
+        if (kinds[i] == kGateSwap && gate_bits[i].size() == 2) {
+            // consecutive swaps while their qubit pairs stay disjoint
+            std::vector<int> used;
+            int j = i;
+            while (j < ng && kinds[j] == kGateSwap && gate_bits[j].size() == 2 &&
+                   gate_bits[j][0] != gate_bits[j][1] &&
+                   std::find(used.begin(), used.end(), gate_bits[j][0]) == used.end() &&
+                   std::find(used.begin(), used.end(), gate_bits[j][1]) == used.end()) {
+                used.push_back(gate_bits[j][0]);
+                used.push_back(gate_bits[j][1]);
+                ++j;
+            }
+            if (j - i >= 2) {
+                FusedBlock run;
+                run.swap_run = true;
+                for (int g = i; g < j; ++g) run.gates.push_back(g);
+                emit(run);
+                i = j;
+            } else {
+                pending.push_back(i++);
+            }
+            continue;
+        }
+        if (kinds[i] != kGateDiagonal) {
             pending.push_back(i++);
             continue;
         }
         int j = i;
         bool small = true;
-        while (j < ng && diagonal[j]) {
+        while (j < ng && kinds[j] == kGateDiagonal) {
             small = small && gate_bits[j].size() <= 2;
             ++j;
         }
@@ -348,17 +379,12 @@ std::vector<FusedBlock> fuse_phase_runs(const std::vector<std::vector<int>>& gat
             i = j;
             continue;
         }
-        if (j < ng && gate_bits[j].size() == 1) {
+        if (j < ng && gate_bits[j].size() == 1 && kinds[j] == kGateGeneral) {
             run.gates.push_back(j);
             run.trailing_pair = true;
             ++j;
         }
-        for (int g : run.gates)
-            for (int q : gate_bits[g])
-                if (std::find(run.qubits.begin(), run.qubits.end(), q) == run.qubits.end()) run.qubits.push_back(q);
-        std::sort(run.qubits.begin(), run.qubits.end());
-        flush();
-        out.push_back(run);
+        emit(run);
         i = j;
     }
     flush();

@@ -46,11 +46,16 @@ struct SeqGate {
 struct FusedBlock {
     std::vector<int> qubits;
     std::vector<int> gates;
-    // A run of diagonal gates applied as one phase function (fuse_phase_runs),
-    // its last gate a non-diagonal 1-qubit gate when trailing_pair is set.
+    // A run of diagonal gates applied as one phase function (fuse_runs), its
+    // last gate a non-diagonal 1-qubit gate when trailing_pair is set.
     bool phase_run = false;
     bool trailing_pair = false;
+    // A run of swaps on pairwise disjoint qubit pairs, one permutation pass.
+    bool swap_run = false;
 };
+
+// Gate kinds a plan may be told about (q1g_plan_set_gate_kinds).
+enum GateKind : unsigned char { kGateGeneral = 0, kGateDiagonal = 1, kGateSwap = 2 };
 
 // Greedy fusion over open blocks on disjoint qubit sets: a gate joins the
 // open blocks it touches when their union fits in `width` qubits; otherwise
@@ -63,15 +68,18 @@ std::vector<FusedBlock> fuse(const std::vector<std::vector<int>>& gate_bits, int
 // Shortest run of consecutive diagonal gates taken as one phase pass.
 constexpr int kMinPhaseRun = 3;
 
-// fuse() with runs of diagonal gates (diagonal[g] != 0) taken out first: a
-// run of at least kMinPhaseRun consecutive diagonal gates, none on more than
-// two qubits and every two-qubit one sharing a common qubit (the pivot), is
-// one phase-run block; its phase is c + L0(x) + x_pivot L1(x) with L0, L1
-// linear in the basis bits.  A non-diagonal 1-qubit gate directly after the
-// run joins it (applied after the phases in the same pass).  The gates
-// between runs are fused by fuse(); blocks never cross a run.
-std::vector<FusedBlock> fuse_phase_runs(const std::vector<std::vector<int>>& gate_bits,
-                                        const std::vector<unsigned char>& diagonal, int nbits, int width);
+// fuse() with two kinds of runs taken out first (kinds[g] a GateKind):
+// - a run of at least kMinPhaseRun consecutive diagonal gates, none on more
+//   than two qubits and every two-qubit one sharing a common qubit (the
+//   pivot), is one phase-run block; its phase is c + L0(x) + x_pivot L1(x)
+//   with L0, L1 linear in the basis bits.  A non-diagonal 1-qubit gate
+//   directly after the run joins it (applied after the phases in the same
+//   pass);
+// - a run of at least 2 consecutive swaps on pairwise disjoint qubit pairs is
+//   one swap-run block (a permutation of the bit positions).
+// The gates between runs are fused by fuse(); blocks never cross a run.
+std::vector<FusedBlock> fuse_runs(const std::vector<std::vector<int>>& gate_bits,
+                                  const std::vector<unsigned char>& kinds, int nbits, int width);
 
 // Qubit shared by every two-qubit gate of a phase run (-1 when it has none).
 int phase_run_pivot(const FusedBlock& b, const std::vector<std::vector<int>>& gate_bits);

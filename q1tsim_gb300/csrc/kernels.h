@@ -40,6 +40,25 @@ void phase_run_tables(int nbits, double c, const double* lin0, const double* lin
 cudaError_t launch_phase_run(float2* amps, uint64_t total, int nbits, int pivot_pos, const void* dtab, int q_pos,
                              const double* m2, int sm_count, cudaStream_t st);
 
+// ---- swap_run.cu: a run of swaps on disjoint qubit pairs as one pass
+// Layout of the pass (host): tiles of 1024 amplitudes over 10 positions
+// closed under the swaps, the swaps outside them, and the stage offsets of
+// every local index (wphys) and of the source of every destination (rphys).
+struct SwapTile {
+    int nouter;                 // swapped pairs outside the tile
+    int pad_;
+    int pa[32], pb[32];         // their positions
+    uint64_t gbit[5];           // amplitude offset of slot bit b (positions 0..4 are the lane bits)
+    IndexMap tile_map;          // the tile's 10 positions, zeroed
+    uint16_t wphys[1024];
+    uint16_t rphys[1024];
+};
+// False when the pass does not apply (fewer than 10 qubits, pairs not disjoint).
+bool swap_run_layout(SwapTile& t, const int* pa, const int* pb, int npairs, int nbits, int amp_bytes);
+// dtile: the SwapTile in device memory; amp_bytes 8 (complex64) or 16.
+cudaError_t launch_swap_run(void* amps, int amp_bytes, uint64_t total, const void* dtile, int sm_count,
+                            cudaStream_t st);
+
 // ---- dense_tiled.cu: uncontrolled dense blocks in warp tiles (warp_tile.h)
 // True when the tiled kernel takes the block: no controls; complex64 on
 // >= 10 qubits with t = 3 or 4, or t <= 2 with a gate at position 0 or 1

@@ -1,4 +1,4 @@
-// Runs of diagonal gates as one pass (gate_plan.h, fuse_phase_runs).  Every
+// Runs of diagonal gates as one pass (gate_plan.h, fuse_runs).  Every
 // amplitude i is multiplied by e^{i phi(x)}, x = i mod 2^n its basis bits and
 //   phi(x) = c + L0(x) + x_p L1(x),   L0, L1 linear in the bits,
 // from per-byte tables of complex factors (computed in double on the host):

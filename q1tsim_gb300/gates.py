@@ -64,11 +64,25 @@ class Gate:
         """True when the matrix is diagonal for every parameter value."""
         return False
 
+    def is_swap(self):
+        """True for the swap of two qubits."""
+        return False
+
+    def plan_kind(self):
+        """What a gate plan may assume about this gate: 1 always diagonal, 2
+        a swap, 0 anything else (q1g_plan_set_gate_kinds)."""
+        if self.is_diagonal():
+            return 1
+        return 2 if self.is_swap() else 0
+
     def is_stabilizer(self):
         return False
 
     def __repr__(self):
         return f"{self.description()}"
+
+
+_SWAP = np.array([[1, 0, 0, 0], [0, 0, 1, 0], [0, 1, 0, 0], [0, 0, 0, 1]], dtype=np.complex128)
 
 
 class _Fixed(Gate):
@@ -83,6 +97,9 @@ class _Fixed(Gate):
 
     def is_diagonal(self):
         return bool(np.count_nonzero(self._m - np.diag(np.diag(self._m))) == 0)
+
+    def is_swap(self):
+        return self._m.shape == (4, 4) and bool(np.array_equal(self._m, _SWAP))
 
     def is_stabilizer(self):
         return self._stab

@@ -285,10 +285,14 @@ class VectorState:
 class Plan:
     """A gate sequence lowered once: structure, fusion grouping, passes."""
 
-    def __init__(self, nr_bits, gate_bits, fusion_width=0, tensor_cores=True, diagonal=None):
-        """diagonal: per gate, True when its matrix is always diagonal (phases,
-        controlled phases); runs of them then become single phase passes
-        (q1g_plan_set_diagonal)."""
+    KIND_GENERAL, KIND_DIAGONAL, KIND_SWAP = 0, 1, 2
+
+    def __init__(self, nr_bits, gate_bits, fusion_width=0, tensor_cores=True, diagonal=None, kinds=None):
+        """kinds: per gate, KIND_DIAGONAL for gates whose matrix is always
+        diagonal (phases, controlled phases) and KIND_SWAP for swaps; runs of
+        them then become single phase or permutation passes
+        (q1g_plan_set_gate_kinds).  diagonal: per gate, True for diagonal
+        gates (the same as kinds with only KIND_DIAGONAL)."""
         L = _lib.load()
         ks = np.asarray([len(b) for b in gate_bits], dtype=np.uint64)
         flat = np.asarray([q for b in gate_bits for q in b], dtype=np.uint64)
@@ -302,10 +306,12 @@ class Plan:
         self.ngates = len(ks)
         self.tensor_cores = bool(tensor_cores)
         check(L.q1g_plan_set_tensor_cores(h, 1 if tensor_cores else 0), "plan_set_tensor_cores")
-        if diagonal is not None and any(diagonal):
-            flags = np.asarray([1 if d else 0 for d in diagonal], dtype=np.uint8)
-            check(L.q1g_plan_set_diagonal(h, flags.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte)), len(flags)),
-                  "plan_set_diagonal")
+        if kinds is None and diagonal is not None:
+            kinds = [self.KIND_DIAGONAL if d else self.KIND_GENERAL for d in diagonal]
+        if kinds is not None and any(kinds):
+            flags = np.asarray(kinds, dtype=np.uint8)
+            check(L.q1g_plan_set_gate_kinds(h, flags.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte)), len(flags)),
+                  "plan_set_gate_kinds")
 
     @property
     def handle(self):

@@ -187,8 +187,34 @@ def test_phase_runs_need_a_common_qubit(lib):
     assert marked == plain
 
 
-def test_plan_set_diagonal_checks_its_arguments(lib):
+def test_plan_set_gate_kinds_checks_its_arguments(lib):
     plan = Plan(4, [[0], [1, 2]], 3)
     flags = (ctypes.c_ubyte * 1)(1)
-    assert lib.q1g_plan_set_diagonal(plan.handle, flags, 1) != 0    # one flag for two gates
-    assert lib.q1g_plan_set_diagonal(None, flags, 1) != 0
+    assert lib.q1g_plan_set_gate_kinds(plan.handle, flags, 1) != 0    # one kind for two gates
+    assert lib.q1g_plan_set_gate_kinds(None, flags, 1) != 0
+
+
+def test_swap_runs_group_the_qft_reversal(lib):
+    """The QFT's closing swaps (disjoint pairs) become one swap-run pass."""
+    from q1tsim_gb300 import workloads
+    n = 16
+    q = workloads.qft(n, precision="c64", fusion_width=5, measure=False)
+    seq = [op for op in q.ops if op[0] == "gate"]
+    bits = [op[2] for op in seq]
+    kinds = [op[1].plan_kind() for op in seq]
+    blocks = Plan(n, bits, 5, kinds=kinds).blocks()
+    last = blocks[-1]
+    assert [seq[g][1].description() for g in last[1]] == ["Swap"] * (n // 2)
+    assert sorted(last[0]) == list(range(n))
+    order = [g for _, gates in blocks for g in gates]
+    assert sorted(order) == list(range(len(bits)))
+
+
+def test_plan_gate_kinds_are_checked(lib):
+    plan = Plan(4, [[0], [1, 2]], 3)
+    kinds = (ctypes.c_ubyte * 2)(2, 0)   # a swap on one qubit
+    assert lib.q1g_plan_set_gate_kinds(plan.handle, kinds, 2) != 0
+    kinds = (ctypes.c_ubyte * 2)(0, 7)
+    assert lib.q1g_plan_set_gate_kinds(plan.handle, kinds, 2) != 0
+    kinds = (ctypes.c_ubyte * 2)(1, 2)
+    assert lib.q1g_plan_set_gate_kinds(plan.handle, kinds, 2) == 0

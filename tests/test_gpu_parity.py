@@ -340,12 +340,11 @@ def test_c128_dense_blocks_on_extreme_magnitudes():
     assert float(np.max(err)) <= 1e-12, float(np.max(err))
 
 
-def _run_plan(n, gates, width, prec, amps, diagonal=True):
+def _run_plan(n, gates, width, prec, amps, kinds=True):
     bits = [b for _, b in gates]
     mats = np.concatenate([np.ascontiguousarray(g.matrix()).ravel() for g, _ in gates]).view(np.float64)
     st = VectorState.from_amplitudes(amps, 1, prec)
-    flags = [g.is_diagonal() for g, _ in gates] if diagonal else None
-    st.apply_plan(Plan(n, bits, width, diagonal=flags), mats)
+    st.apply_plan(Plan(n, bits, width, kinds=[g.plan_kind() for g, _ in gates] if kinds else None), mats)
     return st
 
 
@@ -401,6 +400,38 @@ def test_random_phase_runs_match_oracle():
     assert float(np.max(np.abs(s64 - so))) <= TOL64
     s128 = _run_plan(n, gates, 3, "c128", amps).states()[:, 0]
     assert float(np.max(np.abs(s128 - so))) <= TOL128
+
+
+@pytest.mark.parametrize("prec", ["c64", "c128"])
+@pytest.mark.parametrize("n", [9, 12, 14])
+def test_swap_runs_move_amplitudes_exactly(prec, n):
+    """Runs of swaps on disjoint qubit pairs (the QFT's closing reversal, and
+    random pairings) as single permutation passes: bit-identical to the
+    oracle applying the swaps one by one (9 qubits: the swaps one by one)."""
+    rng = np.random.default_rng(500 + n)
+    amps = rand_state(n, rng)
+    rev = [(G.Swap(), [q, n - 1 - q]) for q in range(n // 2)]
+    perm = [int(q) for q in rng.permutation(n)]
+    rnd = [(G.Swap(), [perm[2 * k], perm[2 * k + 1]]) for k in range(n // 2 - 1)]
+    gates = [(G.U3(0.3, 0.2, 0.1), [0])] + rev + [(G.H(), [n - 1])] + rnd
+    o = orc.OracleState.from_amplitudes(amps, 1)
+    for g, b in gates:
+        o.apply_gate(g.matrix(), b)
+    plan_kinds = [g.plan_kind() for g, _ in gates]
+    assert plan_kinds.count(2) == len(rev) + len(rnd)
+    s = _run_plan(n, gates, 2, prec, amps)
+    so, sg = o.states()[:, 0], s.states()[:, 0]
+    tol = TOL128 if prec == "c128" else TOL64
+    np.testing.assert_allclose(sg, so, rtol=0, atol=tol)
+    # the swaps alone move amplitudes without arithmetic
+    o2 = orc.OracleState.from_amplitudes(amps, 1)
+    for g, b in rev:
+        o2.apply_gate(g.matrix(), b)
+    s2 = _run_plan(n, rev, 2, prec, amps)
+    exp = o2.states()[:, 0]
+    if prec == "c64":
+        exp = exp.astype(np.complex64).astype(np.complex128)
+    assert np.array_equal(s2.states()[:, 0], exp)
 
 
 def test_gate_wrongly_marked_diagonal_is_an_error():

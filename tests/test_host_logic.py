@@ -6,8 +6,11 @@
 - fused_tc.cu: the tile of a tensor-core pass as a tensor-map box, and the
   staged-tile padding and row order (tests/cpp/tile_check.cpp, linked
   against the built library).
-- batch_host.cpp: the batch executor's warp tiles, their staged (swizzled)
-  offsets and bank pairs (tests/cpp/batch_tile_check.cpp, same library).
+- warp_tile.cpp / batch_host.cpp: the warp tiles of the batch executor and
+  the single-state dense kernels, their staged (swizzled) offsets and bank
+  groups (tests/cpp/batch_tile_check.cpp, same library).
+- swap_run.cu: the swap-run pass replayed on the host against the direct
+  permutation (tests/cpp/swap_run_check.cpp, same library).
 
 Both programs are compiled here with g++ and print one line of figures.
 """
@@ -77,4 +80,9 @@ def test_tile_box_and_padding(gxx, tmp_path):
 
 def test_batch_warp_tiles(gxx, tmp_path):
     out = _run(_link_against_library(gxx, tmp_path, "batch_tile_check"))
+    assert out.startswith("bad 0"), out
+
+
+def test_swap_run_pass_replays_the_permutation(gxx, tmp_path):
+    out = _run(_link_against_library(gxx, tmp_path, "swap_run_check"))
     assert out.startswith("bad 0"), out
