@@ -53,6 +53,7 @@ struct SwapTile {
     uint16_t wphys[1024];
     uint16_t rphys[1024];
 };
+static_assert(sizeof(SwapTile) % 8 == 0, "SwapTile copies as 32-bit words");
 // False when the pass does not apply (fewer than 10 qubits, pairs not disjoint).
 bool swap_run_layout(SwapTile& t, const int* pa, const int* pb, int npairs, int nbits, int amp_bytes);
 // dtile: the SwapTile in device memory; amp_bytes 8 (complex64) or 16.
