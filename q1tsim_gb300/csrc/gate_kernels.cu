@@ -178,13 +178,24 @@ struct Mat2DF {
 };
 
 
+// Warps 0 and 2 of each 8-warp block do their pairs in FP64.  The
+// double-float path is issue-bound and leaves GB300's FP64 pipe idle; with a
+// quarter of the warps on it both pipes work (0.93 against 0.82 of measured
+// HBM at 28 qubits; more FP64 warps make that pipe the bottleneck).  Both
+// paths are within the complex128 contract, and which pairs take which is
+// fixed by the launch shape, so results are reproducible.
+constexpr unsigned kPairFp64Warps = 0x05;
+static_assert(kThreads == 256, "kPairFp64Warps assumes 8 warps per block");
+
 // out0 = m00 x0 + m01 x1, out1 = m10 x0 + m11 x1 on double-float pairs; a
-// unit with an amplitude outside the split's range is done in FP64 (md).
+// unit with an amplitude outside the split's range, and every unit of the
+// warps in kPairFp64Warps, is done in FP64 (md).
 template <int U, int NZ>
 __global__ void __launch_bounds__(kThreads)
 k_pair_c128x(double2* __restrict__ a, uint64_t units, IndexMap map, uint64_t o0, uint64_t o1, Mat2DF m,
              Mat2<double2> md)
 {
+    const bool fp64_warp = ((kPairFp64Warps >> (threadIdx.x >> 5)) & 1u) != 0;
     uint64_t base = (uint64_t(blockIdx.x) * U) * blockDim.x + threadIdx.x;
     ulonglong2 x0[U], x1[U];
     uint64_t idx[U];
@@ -203,7 +214,9 @@ k_pair_c128x(double2* __restrict__ a, uint64_t units, IndexMap map, uint64_t o0,
         if (idx[k] == ~uint64_t(0)) continue;
         DF v[4];   // x0.re, x0.im, x1.re, x1.im
         bool ok;
-        if (split_fast_ok(x0[k].x) & split_fast_ok(x0[k].y) & split_fast_ok(x1[k].x) & split_fast_ok(x1[k].y)) {
+        if (fp64_warp) {
+            ok = false;
+        } else if (split_fast_ok(x0[k].x) & split_fast_ok(x0[k].y) & split_fast_ok(x1[k].x) & split_fast_ok(x1[k].y)) {
             v[0] = split_fast(x0[k].x);
             v[1] = split_fast(x0[k].y);
             v[2] = split_fast(x1[k].x);
