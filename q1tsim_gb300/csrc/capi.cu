@@ -177,6 +177,7 @@ int q1g_state_set_stream(q1g_state* s, void* cuda_stream)
             check_cuda(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "cudaStreamCreate");
             s->own_stream = true;
         }
+        if (s->compact) s->compact->stream = s->stream;
     });
 }
 
@@ -425,6 +426,8 @@ int q1g_plan_set_gate_kinds(q1g_plan* p, const unsigned char* kinds, size_t ngat
         }
         p->kinds.assign(kinds, kinds + ngates);
         if (p->width > 0) p->blocks = fuse_runs(p->gate_bits, p->kinds, p->nbits, p->width);
+        p->prefix_known = false;
+        p->prefix_plan.reset();
     });
 }
 
@@ -483,6 +486,8 @@ int q1g_plan_set_tensor_cores(q1g_plan* p, int enable)
     return guarded([&] {
         need(p, "plan");
         p->tensor_cores = enable != 0;
+        p->prefix_known = false;
+        p->prefix_plan.reset();
     });
 }
 

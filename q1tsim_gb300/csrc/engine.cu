@@ -120,8 +120,15 @@ q1g_state::q1g_state(int nbits_, uint64_t nshots_, int prec_)
     own_stream = true;
 }
 
+q1g_state::q1g_state(int nbits_, uint64_t nshots_, int prec_, cudaStream_t shared)
+    : nbits(nbits_), nshots(nshots_), prec(prec_), N(uint64_t(1) << nbits_), ncols(1), counts{nshots_},
+      stream(shared), own_stream(false)
+{
+}
+
 q1g_state::~q1g_state()
 {
+    compact.reset();   // it runs on this state's stream: free it while the stream exists
     if (stream) cudaStreamSynchronize(stream);
     for (auto& p : pending) {
         cudaEventDestroy(p.a);
@@ -837,7 +844,98 @@ static void run_phase_block(q1g_plan* p, q1g_state* s, const FusedBlock& b, cons
     });
 }
 
-void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n)
+// Positions a plan may leave out of its start-of-run subspace: the compact
+// state is at most 1/8 of the full one.  Below kPrefixMinQubits the full
+// state is small enough as it is.
+constexpr int kPrefixSpare = 3;
+constexpr int kPrefixMinQubits = 16;
+
+// A basis state stays a basis state on every position no gate has touched.
+// So the plan's leading blocks, as long as together they touch at most
+// nbits - kPrefixSpare positions, run on a compact state of those positions
+// (the same blocks on renumbered qubits); the full state is then zeroed and
+// the compact one scattered into it, which replaces the fill of the basis
+// state.  Returns the number of blocks done.
+static size_t run_subspace_prefix(q1g_plan* p, q1g_state* s, const double* mats, size_t n)
+{
+    const int nb = s->nbits;
+    if (!p->prefix_known) {
+        p->prefix_known = true;
+        uint64_t mask = 0;
+        size_t len = 0;
+        for (const auto& b : p->blocks) {
+            if (b.phase_run || b.swap_run) break;
+            uint64_t m = mask;
+            for (int q : b.qubits) m |= uint64_t(1) << (nb - 1 - q);
+            if (__builtin_popcountll(m) > nb - kPrefixSpare) break;
+            mask = m;
+            ++len;
+        }
+        if (len >= 2 && nb >= kPrefixMinQubits) {
+            const int na = __builtin_popcountll(mask);
+            auto cq = [&](int q) {
+                const int pos = nb - 1 - q;
+                return na - 1 - __builtin_popcountll(mask & ((uint64_t(1) << pos) - 1));
+            };
+            auto tp = std::make_unique<q1g_plan>();
+            tp->nbits = na;
+            tp->width = p->width;
+            tp->tensor_cores = p->tensor_cores;
+            tp->gate_bits = p->gate_bits;
+            tp->mat_off = p->mat_off;
+            tp->mat_doubles = p->mat_doubles;
+            tp->kinds = p->kinds;
+            for (size_t i = 0; i < len; ++i) {
+                FusedBlock b = p->blocks[i];
+                for (auto& q : b.qubits) q = cq(q);
+                for (int g : b.gates)
+                    for (size_t j = 0; j < p->gate_bits[g].size(); ++j) tp->gate_bits[g][j] = cq(p->gate_bits[g][j]);
+                tp->blocks.push_back(b);
+            }
+            p->prefix_len = len;
+            p->prefix_mask = mask;
+            p->prefix_plan = std::move(tp);
+        }
+    }
+    if (!p->prefix_plan) return 0;
+    const uint64_t mask = p->prefix_mask;
+    const int na = __builtin_popcountll(mask);
+    if (!s->compact || s->compact->nbits != na || s->compact->prec != s->prec)
+        s->compact = std::make_unique<q1g_state>(na, s->nshots, s->prec, s->stream);
+    q1g_state* c = s->compact.get();
+    c->stream = s->stream;
+    c->fp64_exact = s->fp64_exact;
+    c->prof = s->prof;
+    c->nshots = s->nshots;
+    const uint64_t b = s->basis[0];
+    uint64_t cb = 0;
+    SubspacePositions sp{};
+    for (int pos = 0; pos < nb; ++pos)
+        if ((mask >> pos) & 1) {
+            if ((b >> pos) & 1) cb |= uint64_t(1) << sp.n;
+            sp.pos[sp.n++] = pos;
+        }
+    c->sparse = true;
+    c->basis.assign(1, cb);
+    c->counts.assign(1, s->counts[0]);
+    c->ncols = 1;
+    c->norms.assign(1, s->norms[0]);
+    plan_run(p->prefix_plan.get(), c, mats, n, false);
+    c->ensure_dense();
+    s->amps.ensure(s->N * s->bsz());
+    s->launch("subspace_scatter", double(s->N * s->bsz()), [&] {
+        cudaError_t e = cudaMemsetAsync(s->amps.p, 0, s->N * s->bsz(), s->stream);
+        if (e != cudaSuccess) return e;
+        return launch_scatter_subspace(s->amps.p, c->amps.p, s->prec, na, sp, b & ~mask, s->stream);
+    });
+    s->sparse = false;
+    s->basis.clear();
+    for (auto& pe : c->pending) s->pending.push_back(pe);
+    c->pending.clear();
+    return p->prefix_len;
+}
+
+void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n, bool subspace_prefix)
 {
     if (n != p->mat_doubles)
         throw Error(Q1G_ERR_INVALID_ARGUMENT, "expected " + std::to_string(p->mat_doubles) + " matrix doubles");
@@ -901,7 +999,10 @@ void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n)
         if (!launched) s->ensure_dense();
         launched = true;
     };
-    for (size_t i = 0; i < nb; ++i) {
+    const size_t first = (subspace_prefix && s->sparse && s->ncols == 1 && s->basis.size() == 1)
+                             ? run_subspace_prefix(p, s, mats, n)
+                             : 0;
+    for (size_t i = first; i < nb; ++i) {
         if (p->blocks[i].phase_run) {
             begin();
             run_phase_block(p, s, p->blocks[i], gates, stage);

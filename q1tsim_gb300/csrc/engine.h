@@ -7,6 +7,7 @@
 #include <exception>
 #include <utility>
 #include <map>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -105,7 +106,12 @@ struct q1g_state {
     std::vector<Pending> pending;
     std::map<std::string, q1g::ProfTotals> totals;
 
+    // A plan's leading blocks on a basis state run on this smaller state of
+    // the positions they touch (plan_run); its buffers are reused.
+    std::unique_ptr<q1g_state> compact;
+
     q1g_state(int nbits_, uint64_t nshots_, int prec_);
+    q1g_state(int nbits_, uint64_t nshots_, int prec_, cudaStream_t shared);   // runs on `shared`
     ~q1g_state();
 
     size_t bsz() const { return q1g::amp_bytes(prec); }
@@ -164,6 +170,14 @@ struct q1g_plan {
     size_t mat_doubles = 0;
     std::vector<q1g::FusedBlock> blocks;
     std::vector<unsigned char> kinds;      // per gate: q1g::GateKind (phase runs, swap runs)
+    // The leading blocks of the plan touch only the positions of prefix_mask
+    // (at most nbits - 3 of them): on a basis state they run on a compact
+    // state (prefix_plan, the same blocks on compact qubits).  Worked out on
+    // the first run; reset when the grouping changes.
+    bool prefix_known = false;
+    size_t prefix_len = 0;
+    uint64_t prefix_mask = 0;
+    std::unique_ptr<q1g_plan> prefix_plan;
     q1g::HostBuf hmats;            // pinned staging of dense matrices
     q1g::DevBuf dmats;
     cudaEvent_t staged = nullptr;  // last upload of hmats finished
@@ -172,7 +186,7 @@ struct q1g_plan {
 };
 
 namespace q1g {
-void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n);
+void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n, bool subspace_prefix = true);
 // noalloc.cu: the sampler whose scratch is a fixed device array.
 void sample_shots_noalloc(const void* d_amps, int precision, size_t nr_bits, const double* d_sorted_uniforms,
                           size_t nshots, uint64_t* d_outcomes, uint64_t* d_words, const size_t* cbits,

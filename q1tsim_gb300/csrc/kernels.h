@@ -143,6 +143,15 @@ void build_tc_image(const double* m, float* image);
 // ---- state_kernels.cu: construction, conversion, collapse
 cudaError_t launch_fill_basis(void* amps, int prec, uint64_t n_amps, const uint64_t* d_col_index,
                               uint64_t ncols, uint64_t col_len, cudaStream_t st);
+// Bit positions of a subspace: bit k of a compact index is position pos[k].
+struct SubspacePositions {
+    int n;
+    int pos[48];
+};
+// Writes the 2^nbits_compact amplitudes of `compact` into `full` at
+// deposit(c) | fixed (the caller zeroes `full` first).
+cudaError_t launch_scatter_subspace(void* full, const void* compact, int prec, int nbits_compact,
+                                   const SubspacePositions& sp, uint64_t fixed, cudaStream_t st);
 cudaError_t launch_product_state(void* amps, int prec, int nbits, const double* d_coefs,
                                  cudaStream_t st);
 cudaError_t launch_convert_c128_to_c64(float2* dst, const double2* src, uint64_t n, cudaStream_t st);

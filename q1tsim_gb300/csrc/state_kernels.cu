@@ -85,7 +85,34 @@ __global__ void k_collapse_copy(T* dst, const T* src, uint64_t col_len,
     }
 }
 
+// full[deposit(c) | fixed] = compact[c]: bit k of c goes to position pos[k]
+template <typename T>
+__global__ void k_scatter_subspace(T* full, const T* compact, uint64_t count, SubspacePositions sp, uint64_t fixed)
+{
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    for (uint64_t c = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; c < count; c += stride) {
+        uint64_t idx = fixed;
+#pragma unroll 8
+        for (int k = 0; k < sp.n; ++k)
+            if ((c >> k) & 1) idx |= uint64_t(1) << sp.pos[k];
+        full[idx] = compact[c];
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_scatter_subspace(void* full, const void* compact, int prec, int nbits_compact,
+                                   const SubspacePositions& sp, uint64_t fixed, cudaStream_t st)
+{
+    const uint64_t count = uint64_t(1) << nbits_compact;
+    const unsigned grid = blocks_for(count, kThreads) > 152 * 32 ? 152 * 32 : blocks_for(count, kThreads);
+    if (prec == kC128)
+        k_scatter_subspace<double2><<<grid, kThreads, 0, st>>>((double2*)full, (const double2*)compact, count, sp,
+                                                               fixed);
+    else
+        k_scatter_subspace<float2><<<grid, kThreads, 0, st>>>((float2*)full, (const float2*)compact, count, sp, fixed);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_fill_basis(void* amps, int prec, uint64_t n_amps, const uint64_t* d_col_index,
                               uint64_t ncols, uint64_t col_len, cudaStream_t st)

@@ -447,6 +447,62 @@ def test_gate_wrongly_marked_diagonal_is_an_error():
         st.apply_plan(plan, mats)
 
 
+def _brick(n, depth, seed):
+    rng = np.random.default_rng(seed)
+    out = []
+    for layer in range(depth):
+        for q in range(n):
+            out.append((G.U3(*rng.uniform(0, 2 * np.pi, 3)), [q]))
+        for q in range(layer % 2, n - 1, 2):
+            out.append((G.CX(), [q, q + 1]))
+    return out
+
+
+@pytest.mark.parametrize("prec,width,n", [("c64", 5, 18), ("c64", 4, 17), ("c128", 0, 17), ("c128", 3, 16)])
+def test_plan_from_basis_state_runs_its_prefix_compact(prec, width, n):
+    """From a basis state, a plan's leading blocks (touching at most n - 3
+    positions) run on a compact state of those positions, scattered into the
+    full one afterwards: same state as the oracle applying the gates."""
+    gates = _brick(n, 5, 600 + n)
+    o = orc.OracleState.new(n, 1)
+    for g, b in gates:
+        o.apply_gate(g.matrix(), b)
+    st = VectorState(n, 1, prec)
+    bits = [b for _, b in gates]
+    mats = np.concatenate([np.ascontiguousarray(g.matrix()).ravel() for g, _ in gates]).view(np.float64)
+    plan = Plan(n, bits, width)
+    st.apply_plan(plan, mats)
+    tol = TOL128 if prec == "c128" else TOL64
+    np.testing.assert_allclose(st.states()[:, 0], o.states()[:, 0], rtol=0, atol=tol)
+    # a second run on the same state object starts from the dense result
+    st.reset_all()
+    st.apply_plan(plan, mats)
+    np.testing.assert_allclose(st.states()[:, 0], o.states()[:, 0], rtol=0, atol=tol)
+
+
+def test_prefix_from_a_nonzero_basis_state():
+    """After measure_all collapses a 1-run state onto a basis state with ones
+    in it, the next plan's compact prefix keeps the untouched positions at
+    their measured values."""
+    n = 17
+    rng = np.random.default_rng(601)
+    amps = rand_state(n, rng)
+    o, g = pair(n, 1, amps, "c128")
+    u = np.array([0.37])
+    ro = np.zeros(1, dtype=np.uint64)
+    rg = np.zeros(1, dtype=np.uint64)
+    o.measure_all_into(list(range(n)), ro, uniforms=u)
+    g.measure_all_into(list(range(n)), rg, uniforms=u)
+    assert np.array_equal(ro, rg) and int(ro[0]) != 0
+    gates = [(G.U3(*rng.uniform(0, 6, 3)), [q]) for q in range(0, 8)] + [(G.CX(), [q, q + 1]) for q in range(0, 7)]
+    for gt, b in gates:
+        o.apply_gate(gt.matrix(), b)
+    bits = [b for _, b in gates]
+    mats = np.concatenate([np.ascontiguousarray(gt.matrix()).ravel() for gt, _ in gates]).view(np.float64)
+    g.apply_plan(Plan(n, bits, 3), mats)
+    np.testing.assert_allclose(g.states()[:, 0], o.states()[:, 0], rtol=0, atol=TOL128)
+
+
 def test_rng_stream_matches_oracle():
     """The device-generated sorted uniforms agree with the oracle's host
     generation (same SplitMix64 stream); outcomes then agree except, with
