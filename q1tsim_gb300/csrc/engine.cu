@@ -633,7 +633,7 @@ struct TcPass {
     IndexMap tilemap{};
     TcOffsets offs{};
     TcTileBox box{};             // the tile as a tensor-map box
-    std::vector<float> images;   // nblocks x 32 KB
+    std::vector<uint16_t> images;   // nblocks x 16 KB of f16
 };
 
 static std::vector<int> positions_of(const std::vector<int>& qubits, int nbits)
@@ -697,7 +697,7 @@ static TcPass lower_tc_pass(const std::vector<const std::vector<cd>*>& mats,
         t.offs.run_off[r] = o;
     }
     t.offs.nblocks = (uint32_t)mats.size();
-    t.images.assign(mats.size() * (32768 / 4), 0.0f);
+    t.images.assign(mats.size() * kTcImageHalves, 0);
     for (size_t bi = 0; bi < mats.size(); ++bi) {
         // gate qubits: the block's own, padded from the tile's highest positions
         std::vector<int> gpos = positions_of(*bits[bi], nbits);
@@ -712,7 +712,7 @@ static TcPass lower_tc_pass(const std::vector<const std::vector<cd>*>& mats,
             md[2 * e] = m32[e].real();
             md[2 * e + 1] = m32[e].imag();
         }
-        build_tc_image(md.data(), t.images.data() + bi * (32768 / 4));
+        build_tc_image(md.data(), t.images.data() + bi * kTcImageHalves);
         TcBlockGeom& G = t.offs.blk[bi];
         int r = 0;
         for (int j = 0; j < 12; ++j)
@@ -977,8 +977,11 @@ void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n, bool subs
     auto eligible = [&](size_t bi) {
         if (p->blocks[bi].phase_run || p->blocks[bi].swap_run) return false;
         prepare(bi);
-        return use_tc && ops[bi].kind == GateOp::Dense && ops[bi].t >= 3 && bbits[bi].size() <= 5;
+        return use_tc && ops[bi].kind == GateOp::Dense && ops[bi].t >= 3 && bbits[bi].size() <= 5 &&
+               tc_block_bounded(bmats[bi].data(), 1 << bbits[bi].size());
     };
+    double max_norm = 0.0;
+    for (double v : s->norms) max_norm = std::max(max_norm, v);
     // Staging: every pass uploads its matrix or tensor-core image from its own
     // slice of one pinned buffer (at most 32 KB per block).
     if (p->staged) check_cuda(cudaEventSynchronize(p->staged), "plan staging wait");
@@ -1041,7 +1044,8 @@ void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n, bool subs
                 check_cuda(cudaMemsetAsync(s->errbuf.p, 0, sizeof(int), s->stream), "clear error flag");
                 any_tc = true;
             }
-            const void* img = stage(t.images.data(), t.images.size() * sizeof(float));
+            tc_operand_scales(max_norm, t.offs);
+            const void* img = stage(t.images.data(), t.images.size() * sizeof(uint16_t));
             const uint64_t total = s->total();
             s->launch("fused_tc_c64", 2.0 * total * s->bsz(), [&] {
                 return launch_fused_tc(s->amps.as<float2>(), total >> 12, t.tilemap, t.offs, t.box, img,

@@ -9,16 +9,22 @@
 //     D[t][n] = sum_k A[t][k] * R[n][k],   A[t][2g+c] = component c of amp(t, g),
 // with R the 64x64 real embedding of M (R[2g'][2g] = Re M, R[2g'][2g+1] = -Im M,
 // R[2g'+1][2g] = Im M, R[2g'+1][2g+1] = Re M).  It runs on tcgen05.mma
-// kind::tf32 (M=128, K=8) with A and the accumulators in tensor memory and R
-// in shared memory.  FP32 accuracy comes from the 3xTF32 split (Ootomo &
-// Yokota 2022): x = hi + lo with hi = tf32(x), lo = tf32(x - hi), and
-// D = A_hi*B_hi + (A_lo*B_hi + A_hi*B_lo).  The correction products go to a
-// second accumulator with the lo halves pre-scaled by 2^11 (exact), and the
+// kind::f16 (M=128, K=16, FP32 accumulators) with A and the accumulators in
+// tensor memory and R in shared memory.  FP32 accuracy comes from splitting
+// both operands into two 11-bit halves (the 3-product scheme of Ootomo &
+// Yokota 2022): x = hi + lo with hi = x to 11 significant bits and
+// lo = x - hi, and D = A_hi*B_hi + (A_lo*B_hi + A_hi*B_lo).  Halves are f16,
+// so one 32-bit TMEM column holds one complex amplitude and a row's operands
+// take 64 columns.  f16 has a narrow exponent range, so the operands are
+// scaled by powers of two: amplitudes by 2^14 / 2^ceil(log2 sqrt(max column
+// norm)) (at most 2^14 in magnitude for blocks whose rows have 2-norm <= 1),
+// R by 2^14; the epilogue undoes both exactly.  The correction products go to
+// a second accumulator with the lo halves pre-scaled by 2^11 (exact), and the
 // epilogue adds D_corr * 2^-11: summed in one accumulator with the main
 // products, the correction terms were lost.  B is stored as [B_hi; B_lo]
-// (128 rows), so A_hi*[B_hi; B_lo] is one N=128 product into
+// (128 rows of 64 f16), so A_hi*[B_hi; B_lo] is one N=128 product into
 // [D_main | D_corr] and A_lo*B_hi one N=64 product added to D_corr:
-// 16 MMAs per block and tile.
+// 8 MMAs per block and tile.
 //
 // One CTA per SM, persistent over tiles, with 11 warps:
 //   warp 8   loader: copies a tile into a ring of shared-memory stages,
@@ -38,13 +44,10 @@
 //            each thread reads its row of D with tcgen05.ld and writes the
 //            new amplitudes back into the stage.  While one group waits for
 //            its MMAs the other converts or writes back, so the tensor pipe,
-//            the ALUs and the copy engine work at the same time.  The split's
-//            TMEM stores (64 KB per tile and block) bound two-block passes;
-//            two warps per lane quarter, or one 64-column store instead of
-//            two 32-column stores, measured no faster.
-// TMEM (512 columns): group g uses 256g + [0,128) for A (K-step s: A_hi in
-// columns 16s..16s+7, A_lo in 16s+8..16s+15, so that a thread writes its
-// half row with one 64-column store), [128,192) D_main, [192,256) D_corr.
+//            the ALUs and the copy engine work at the same time.
+// TMEM (512 columns): group g uses 256g + [0,64) for A (K-step s: A_hi pairs
+// in columns 16s..16s+7, A_lo pairs in 16s+8..16s+15, so that a thread writes
+// half a row with one 32-column store), [128,192) D_main, [192,256) D_corr.
 // Every wait is bounded (in wall-clock time, %globaltimer); on expiry the CTA
 // records an error, lets its copies land and releases its TMEM before
 // returning.
@@ -61,6 +64,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "f16_host.h"
 #include "kernels.h"
 
 namespace q1g {
@@ -75,9 +79,8 @@ constexpr int kTcThreads = kConsumers + 96;
 constexpr uint32_t kTileBytes = 4096 * 8;        // one tile (complex64), without padding
 constexpr uint32_t kTmemCols = 512;
 constexpr float kLoScale = 2048.0f;     // 2^11: lo halves are stored scaled up
-constexpr float kLoUnscale = 1.0f / 2048.0f;
-constexpr uint32_t kBAtom = 16384;      // one K-atom of [B_hi; B_lo]: 128 rows x 128 B
-constexpr uint32_t kBImage = 2 * kBAtom;   // one block's image (K = 64)
+constexpr uint32_t kBImage = 16384;     // one block's [B_hi; B_lo']: 128 rows x 64 f16 (128 B)
+constexpr int kBScaleLog2 = 14;         // B entries (|R| <= 1) are stored times 2^14
 constexpr uint32_t kMaxStages = 8;
 // shared memory: [0, 1024) barriers, TMEM slot, abort flag, run offsets;
 // then nblocks B images; then the stages.
@@ -114,16 +117,18 @@ __device__ __forceinline__ uint64_t desc_sw128(uint32_t saddr)
     return d;
 }
 
-// Instruction descriptor, kind::tf32: D f32, A/B tf32, both K-major, M=128.
-constexpr uint32_t idesc_tf32(uint32_t n)
+// Instruction descriptor, kind::f16: D f32 (bits 4-5 = 1), A and B f16
+// (bits 7-9 and 10-12 = 0), both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+constexpr uint32_t idesc_f16(uint32_t n)
 {
-    return (1u << 4) | (2u << 7) | (2u << 10) | ((n >> 3) << 17) | ((128u >> 4) << 24);
+    return (1u << 4) | (0u << 7) | (0u << 10) | ((n >> 3) << 17) | ((128u >> 4) << 24);
 }
-constexpr uint32_t kIdescN128 = idesc_tf32(128);
-constexpr uint32_t kIdescN64 = idesc_tf32(64);
+constexpr uint32_t kIdescN128 = idesc_f16(128);
+constexpr uint32_t kIdescN64 = idesc_f16(64);
 
-// Nearest TF32 value (ties away from zero) as an FP32 with the 13 low
-// mantissa bits cleared, so that x - to_tf32(x) is the exact remainder.
+// x rounded to 11 significant bits (nearest, ties away from zero) as an
+// FP32 with the 13 low mantissa bits cleared, so that x - to_tf32(x) is the
+// exact remainder.  In the normal range of f16 the result is an f16 value.
 __device__ __forceinline__ float to_tf32(float x)
 {
     return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
@@ -148,13 +153,13 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
 }
 
 // D (TMEM) (+)= A (TMEM) * B (SMEM descriptor)^T
-__device__ __forceinline__ void mma_tf32_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t b, uint32_t idesc,
+__device__ __forceinline__ void mma_f16_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t b, uint32_t idesc,
                                             uint32_t acc)
 {
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
         "setp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
         "r"(a_tmem), "l"(b), "r"(idesc), "r"(acc));
 }
 
@@ -178,26 +183,16 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t* v)
         : "r"(taddr));
 }
 
-__device__ __forceinline__ void tmem_st32(uint32_t taddr, const float* v)
+__device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t* v)
 {
     asm volatile(
         "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], "
         "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,"
         "%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(taddr),
-        "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7]), "f"(v[8]),
-        "f"(v[9]), "f"(v[10]), "f"(v[11]), "f"(v[12]), "f"(v[13]), "f"(v[14]), "f"(v[15]), "f"(v[16]),
-        "f"(v[17]), "f"(v[18]), "f"(v[19]), "f"(v[20]), "f"(v[21]), "f"(v[22]), "f"(v[23]), "f"(v[24]),
-        "f"(v[25]), "f"(v[26]), "f"(v[27]), "f"(v[28]), "f"(v[29]), "f"(v[30]), "f"(v[31])
-        : "memory");
-}
-
-// 64 columns from 32 hi and 32 lo values of this thread's lane, interleaved
-// per K-step of 8: hi[8s..8s+7] then lo[8s..8s+7] for s = 0..3.
-__device__ __forceinline__ void tmem_st64_hilo(uint32_t taddr, const float* hi, const float* lo)
-{
-    asm volatile(
-        "tcgen05.st.sync.aligned.32x32b.x64.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63,%64};" ::"r"(taddr),
-        "f"(hi[0]), "f"(hi[1]), "f"(hi[2]), "f"(hi[3]), "f"(hi[4]), "f"(hi[5]), "f"(hi[6]), "f"(hi[7]), "f"(lo[0]), "f"(lo[1]), "f"(lo[2]), "f"(lo[3]), "f"(lo[4]), "f"(lo[5]), "f"(lo[6]), "f"(lo[7]), "f"(hi[8]), "f"(hi[9]), "f"(hi[10]), "f"(hi[11]), "f"(hi[12]), "f"(hi[13]), "f"(hi[14]), "f"(hi[15]), "f"(lo[8]), "f"(lo[9]), "f"(lo[10]), "f"(lo[11]), "f"(lo[12]), "f"(lo[13]), "f"(lo[14]), "f"(lo[15]), "f"(hi[16]), "f"(hi[17]), "f"(hi[18]), "f"(hi[19]), "f"(hi[20]), "f"(hi[21]), "f"(hi[22]), "f"(hi[23]), "f"(lo[16]), "f"(lo[17]), "f"(lo[18]), "f"(lo[19]), "f"(lo[20]), "f"(lo[21]), "f"(lo[22]), "f"(lo[23]), "f"(hi[24]), "f"(hi[25]), "f"(hi[26]), "f"(hi[27]), "f"(hi[28]), "f"(hi[29]), "f"(hi[30]), "f"(hi[31]), "f"(lo[24]), "f"(lo[25]), "f"(lo[26]), "f"(lo[27]), "f"(lo[28]), "f"(lo[29]), "f"(lo[30]), "f"(lo[31])
+        "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]), "r"(v[8]),
+        "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15]), "r"(v[16]),
+        "r"(v[17]), "r"(v[18]), "r"(v[19]), "r"(v[20]), "r"(v[21]), "r"(v[22]), "r"(v[23]), "r"(v[24]),
+        "r"(v[25]), "r"(v[26]), "r"(v[27]), "r"(v[28]), "r"(v[29]), "r"(v[30]), "r"(v[31])
         : "memory");
 }
 
@@ -299,49 +294,65 @@ __device__ __forceinline__ bool group_any(bool fail, uint32_t id)
     return any != 0;
 }
 
-__device__ __forceinline__ void split_tf32(float x, float& hi, float& lo)
+// Two f32 values as an f16 pair: `first` in the low half (the lower K index).
+__device__ __forceinline__ uint32_t pack_f16x2(float first, float second)
 {
-    hi = to_tf32(x);
-    lo = to_tf32((x - hi) * kLoScale);
+    uint32_t d;
+    asm("cvt.rn.f16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(second), "f"(first));
+    return d;
 }
 
-// Gates 16*HH .. 16*HH+15 of row `rowb` -> hi/lo operands: K-steps
-// 4*HH .. 4*HH+3, each 8 hi columns then 8 lo columns, at TMEM address tl.
-template <int HH>
-__device__ __forceinline__ void split_half(const uint8_t* raw, uint32_t rowb, const TcBlockGeom& G, uint32_t tl)
+// Amplitude v scaled by sc -> hi = (re, im) to 11 bits and lo = 2^11 (v sc - hi),
+// each an f16 pair with the real part in the low half.
+__device__ __forceinline__ void split_amp(float2 v, float sc, uint32_t& hi, uint32_t& lo)
 {
-    float hi[32], lo[32];
+    const float re = v.x * sc, im = v.y * sc;
+    const float hr = to_tf32(re), hm = to_tf32(im);
+    hi = pack_f16x2(hr, hm);
+    lo = pack_f16x2((re - hr) * kLoScale, (im - hm) * kLoScale);
+}
+
+// Gates 16*HH .. 16*HH+15 of row `rowb` -> f16 operands in TMEM columns
+// 32*HH .. 32*HH+31: per K-step of 8 gates (16 f16), 8 columns of hi pairs
+// then 8 of lo pairs.
+template <int HH>
+__device__ __forceinline__ void split_half(const uint8_t* raw, uint32_t rowb, const TcBlockGeom& G, uint32_t tl,
+                                           float sc)
+{
+    uint32_t v[32];
     if (G.vec2) {
 #pragma unroll
         for (int m = 0; m < 8; ++m) {
-            const float4 v = *(const float4*)(raw + rowb + G.gateoff[16 * HH + 2 * m]);
-            split_tf32(v.x, hi[4 * m], lo[4 * m]);
-            split_tf32(v.y, hi[4 * m + 1], lo[4 * m + 1]);
-            split_tf32(v.z, hi[4 * m + 2], lo[4 * m + 2]);
-            split_tf32(v.w, hi[4 * m + 3], lo[4 * m + 3]);
+            const float4 p = *(const float4*)(raw + rowb + G.gateoff[16 * HH + 2 * m]);
+            const int j = 2 * m, c = (j >> 3) * 16 + (j & 7);
+            split_amp(make_float2(p.x, p.y), sc, v[c], v[c + 8]);
+            split_amp(make_float2(p.z, p.w), sc, v[c + 1], v[c + 9]);
         }
     } else {
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
-            const float2 v = *(const float2*)(raw + rowb + G.gateoff[16 * HH + j]);
-            split_tf32(v.x, hi[2 * j], lo[2 * j]);
-            split_tf32(v.y, hi[2 * j + 1], lo[2 * j + 1]);
+            const float2 p = *(const float2*)(raw + rowb + G.gateoff[16 * HH + j]);
+            const int c = (j >> 3) * 16 + (j & 7);
+            split_amp(p, sc, v[c], v[c + 8]);
         }
     }
-    tmem_st64_hilo(tl + 64u * HH, hi, lo);
+    tmem_st32(tl + 32u * HH, v);
 }
 
-// D = D_main + 2^-11 D_corr for gates 16*HH .. 16*HH+15 of row `rowb`, back
-// into the stage.
+// D_main * dm + D_corr * dc for gates 16*HH .. 16*HH+15 of row `rowb` (the
+// scales undo the operands' and the lo halves' powers of two), back into the
+// stage.
 template <int HH>
-__device__ __forceinline__ void writeback_half(uint8_t* raw, uint32_t rowb, const TcBlockGeom& G, uint32_t tl)
+__device__ __forceinline__ void writeback_half(uint8_t* raw, uint32_t rowb, const TcBlockGeom& G, uint32_t tl,
+                                               float dm_scale, float dc_scale)
 {
     uint32_t dm[32], dc[32];
     tmem_ld32(tl + 128u + 32u * HH, dm);
     tmem_ld32(tl + 192u + 32u * HH, dc);
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-    for (int j = 0; j < 32; ++j) dm[j] = __float_as_uint(__fmaf_rn(__uint_as_float(dc[j]), kLoUnscale, __uint_as_float(dm[j])));
+    for (int j = 0; j < 32; ++j)
+        dm[j] = __float_as_uint(__fmaf_rn(__uint_as_float(dc[j]), dc_scale, __uint_as_float(dm[j]) * dm_scale));
     if (G.vec2) {
 #pragma unroll
         for (int m = 0; m < 8; ++m)
@@ -512,25 +523,23 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, const __grid_constant__ Inde
                 const uint32_t rowb = b ? rowb1 : rowb0;
                 if (b > 0) group_sync(gbar);    // the previous block's results are all staged
                 // row t -> hi/lo operands, columns 2g+c, in TMEM
-                split_half<0>(raw, rowb, G, tl);
-                split_half<1>(raw, rowb, G, tl);
+                split_half<0>(raw, rowb, G, tl, offs.ascale);
+                split_half<1>(raw, rowb, G, tl, offs.ascale);
                 asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
                 asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
                 group_sync(gbar);
                 if (issuer) {
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                     const uint32_t bb = sbase + kOffB + (uint32_t)b * kBImage;
-                    // [D_main | D_corr] = A_hi [B_hi; B_lo']^T, then D_corr += A_lo' B_hi^T
+                    // [D_main | D_corr] = A_hi [B_hi; B_lo']^T, then D_corr += A_lo' B_hi^T;
+                    // K-step ks (16 f16) starts 32 B into each 128 B row
 #pragma unroll
-                    for (int ks = 0; ks < 8; ++ks)
-                        mma_tf32_ts(tm + 128u, tm + 16u * ks,
-                                    desc_sw128(bb + (uint32_t)(ks >> 2) * kBAtom + (uint32_t)(ks & 3) * 32u),
-                                    kIdescN128, ks > 0 ? 1u : 0u);
+                    for (int ks = 0; ks < 4; ++ks)
+                        mma_f16_ts(tm + 128u, tm + 16u * ks, desc_sw128(bb + (uint32_t)ks * 32u), kIdescN128,
+                                   ks > 0 ? 1u : 0u);
 #pragma unroll
-                    for (int ks = 0; ks < 8; ++ks)
-                        mma_tf32_ts(tm + 192u, tm + 16u * ks + 8u,
-                                    desc_sw128(bb + (uint32_t)(ks >> 2) * kBAtom + (uint32_t)(ks & 3) * 32u),
-                                    kIdescN64, 1u);
+                    for (int ks = 0; ks < 4; ++ks)
+                        mma_f16_ts(tm + 192u, tm + 16u * ks + 8u, desc_sw128(bb + (uint32_t)ks * 32u), kIdescN64, 1u);
                     mma_commit(mbar);
                 }
                 if (group_any(!wait_phase(mbar, mph & 1u, abort_flag), gbar)) {
@@ -539,8 +548,8 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, const __grid_constant__ Inde
                 }
                 ++mph;
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                writeback_half<0>(raw, rowb, G, tl);
-                writeback_half<1>(raw, rowb, G, tl);
+                writeback_half<0>(raw, rowb, G, tl, offs.dmain, offs.dcorr);
+                writeback_half<1>(raw, rowb, G, tl, offs.dmain, offs.dcorr);
                 asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             }
             if (stop) break;
@@ -558,17 +567,6 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, const __grid_constant__ Inde
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (warp == 0)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
-}
-
-// Round to TF32 the way to_tf32 does: nearest, ties away from zero.
-float host_tf32(float x)
-{
-    uint32_t u;
-    std::memcpy(&u, &x, 4);
-    u = (u + 0x1000u) & 0xFFFFE000u;
-    float r;
-    std::memcpy(&r, &u, 4);
-    return r;
 }
 
 uint32_t staged_offset(uint32_t x, uint32_t pad)
@@ -701,11 +699,13 @@ void tc_choose_padding(TcOffsets& o, bool tma_ok)
     }
 }
 
-void build_tc_image(const double* m, float* image)
+void build_tc_image(const double* m, uint16_t* image)
 {
-    // R[n][k]: n = 2g'+c' output component, k = 2g+c input component.  Rows
-    // n of B_hi and 64+n of B_lo' (= 2^11 lo), K-major, SWIZZLE_128B, one
-    // 16 KB atom per 32 values of k.
+    // R[n][k]: n = 2g'+c' output component, k = 2g+c input component, times
+    // 2^14.  Rows n of B_hi and 64+n of B_lo' (= 2^11 lo) as f16, K-major,
+    // SWIZZLE_128B: 8-row groups of 1024 B, 16-byte chunk j of row r at
+    // chunk position j ^ (r & 7).
+    const double bs = std::ldexp(1.0, kBScaleLog2);
     for (int gp = 0; gp < 32; ++gp)
         for (int g = 0; g < 32; ++g) {
             const double re = m[2 * (gp * 32 + g)], im = m[2 * (gp * 32 + g) + 1];
@@ -713,18 +713,43 @@ void build_tc_image(const double* m, float* image)
             for (int cp = 0; cp < 2; ++cp)
                 for (int c = 0; c < 2; ++c) {
                     const int n = 2 * gp + cp, k = 2 * g + c;
-                    const float v = (float)rv[cp][c];
-                    const float hi = host_tf32(v);
-                    const float lo = host_tf32((v - hi) * 2048.0f);
-                    const int atom = k >> 5, kc = (k & 31) >> 2, e = k & 3;
+                    const double v = rv[cp][c] * bs;
+                    double hi = 0.0, lo = 0.0;
+                    const uint16_t hb = host_f16_bits(v, &hi);
+                    const uint16_t lb = host_f16_bits((v - hi) * 2048.0, &lo);
                     for (int half = 0; half < 2; ++half) {
                         const int row = n + 64 * half;
-                        const size_t off = (size_t)atom * kBAtom + (size_t)(row >> 3) * 1024 +
-                                           (size_t)(row & 7) * 128 + (size_t)((kc ^ (row & 7)) << 4) + (size_t)e * 4;
-                        image[off / 4] = half ? lo : hi;
+                        const size_t off = (size_t)(row >> 3) * 1024 + (size_t)(row & 7) * 128 +
+                                           (size_t)(((k >> 3) ^ (row & 7)) << 4) + (size_t)(k & 7) * 2;
+                        image[off / 2] = half ? lb : hb;
                     }
                 }
         }
+}
+
+void tc_operand_scales(double max_norm, TcOffsets& offs)
+{
+    // |amplitude| <= sqrt(column norm) <= 2^e: amplitudes enter the tensor
+    // cores times 2^(14-e), at most 2^14 (f16 holds up to 65504), so that
+    // those above 2^(-28+e) are normal f16 numbers
+    int e = 0;
+    if (max_norm > 0.0 && std::isfinite(max_norm)) e = (int)std::ceil(0.5 * std::log2(max_norm));
+    e = std::max(-60, std::min(60, e));
+    offs.ascale = std::ldexp(1.0f, 14 - e);
+    offs.dmain = std::ldexp(1.0f, -(14 - e) - kBScaleLog2);
+    offs.dcorr = std::ldexp(offs.dmain, -11);
+}
+
+bool tc_block_bounded(const std::complex<double>* m, int dim)
+{
+    // every output amplitude is a row of m times the input: with row
+    // 2-norms <= 1 it stays within the column norm (true of unitary blocks)
+    for (int r = 0; r < dim; ++r) {
+        double s = 0.0;
+        for (int c = 0; c < dim; ++c) s += std::norm(m[(size_t)r * dim + c]);
+        if (!(s <= 1.0 + 1e-6)) return false;
+    }
+    return true;
 }
 
 TcTileBox tc_tile_box(const int* tile_pos, int nbits, uint64_t ncols)

@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <complex>
+
 #include "common.cuh"
 #include "warp_tile.h"
 
@@ -107,6 +109,11 @@ struct TcOffsets {
     uint32_t use_tma;        // 1: one tensor-map copy per tile (set by launch_fused_tc)
     uint32_t tshift[5];      // tensor-map coordinate d = (tile >> tshift[d]) & tmask[d]
     uint32_t tmask[5];
+    // operand scales (tc_operand_scales): amplitudes enter as f16 times
+    // ascale; D_main * dmain + D_corr * dcorr is the result
+    float ascale;
+    float dmain;
+    float dcorr;
     uint32_t pad1_;
     uint64_t run_off[32];
     TcBlockGeom blk[2];
@@ -130,15 +137,23 @@ TcTileBox tc_tile_box(const int* tile_pos /* 12, ascending */, int nbits, uint64
 // its conflicts stay within twice the minimum: one tensor copy per tile beats
 // padded piece copies.
 void tc_choose_padding(TcOffsets& offs, bool tma_ok);
-// d_bimage: nblocks consecutive 32 KB hi/lo images of the blocks' real 64x64
-// embeddings in the kernel's swizzled layout; d_err: set to 1 if a bounded
-// wait expired.
+// d_bimage: nblocks consecutive 16 KB f16 hi/lo images of the blocks' real
+// 64x64 embeddings in the kernel's swizzled layout; d_err: set to 1 if a
+// bounded wait expired.
 // box: the tile as a tensor-map box (used for unpadded passes when usable).
 cudaError_t launch_fused_tc(float2* amps, uint64_t ntiles, const IndexMap& tilemap, const TcOffsets& offs,
                             const TcTileBox& box, const void* d_bimage, int* d_err, int sm_count,
                             cudaStream_t st);
-// Host: the 32 KB image for the 32x32 complex matrix m (row-major (re, im)).
-void build_tc_image(const double* m, float* image);
+// Host: the 16 KB image (8192 f16) for the 32x32 complex matrix m
+// (row-major (re, im)), entries times 2^14.
+constexpr size_t kTcImageHalves = 8192;
+void build_tc_image(const double* m, uint16_t* image);
+// Host: offs.ascale / dmain / dcorr for states whose columns have squared
+// norms at most max_norm.
+void tc_operand_scales(double max_norm, TcOffsets& offs);
+// Host: whether every row of the dim x dim block has 2-norm <= 1 (so that no
+// amplitude outgrows its column norm, as the operand scale assumes).
+bool tc_block_bounded(const std::complex<double>* m, int dim);
 
 // ---- state_kernels.cu: construction, conversion, collapse
 cudaError_t launch_fill_basis(void* amps, int prec, uint64_t n_amps, const uint64_t* d_col_index,

@@ -11,6 +11,9 @@
   groups (tests/cpp/batch_tile_check.cpp, same library).
 - swap_run.cu: the swap-run pass replayed on the host against the direct
   permutation (tests/cpp/swap_run_check.cpp, same library).
+- f16_host.h / fused_tc.cu: binary16 rounding against numpy's float16, the
+  f16 image of a block read back through its swizzle, the operand scales and
+  the row-norm bound of tensor-core blocks (tests/cpp/tc_image_check.cpp).
 
 Both programs are compiled here with g++ and print one line of figures.
 """
@@ -86,3 +89,28 @@ def test_batch_warp_tiles(gxx, tmp_path):
 def test_swap_run_pass_replays_the_permutation(gxx, tmp_path):
     out = _run(_link_against_library(gxx, tmp_path, "swap_run_check"))
     assert out.startswith("bad 0"), out
+
+
+def test_f16_rounding_and_tensor_core_images(gxx, tmp_path):
+    """Binary16 rounding of the operand images equals numpy's float16
+    conversion (round to nearest even) on normals, subnormals, halfway cases
+    and zeros; the image reads back to 2^14 R within 2^-22."""
+    import numpy as np
+    rng = np.random.default_rng(5)
+    vals = np.concatenate([
+        rng.uniform(-2.0 ** 15, 2.0 ** 15, 20000),
+        rng.standard_normal(20000) * 2.0 ** rng.integers(-30, 14, 20000),
+        (rng.integers(0, 2048, 4000) + 0.5) * 2.0 ** rng.integers(-34, 4, 4000),   # ties
+        (rng.integers(0, 1024, 2000) + 0.5) * 2.0 ** -24,                           # subnormal ties
+        np.array([0.0, -0.0, 2.0 ** -14, 2.0 ** -25, 2.0 ** -26, 65504.0, 2047.5 * 2.0 ** -11]),
+    ])
+    path = tmp_path / "vals.bin"
+    vals.astype(np.float64).tofile(path)
+    exe = _link_against_library(gxx, tmp_path, "tc_image_check")
+    r = subprocess.run([exe, str(path)], capture_output=True, text=True, timeout=600)
+    lines = r.stdout.split()
+    assert r.returncode == 0 and lines[:2] == ["bad", "0"], r.stdout[:200] + r.stderr
+    got = np.array([int(x, 16) for x in lines[4:]], dtype=np.uint16)
+    want = vals.astype(np.float16).view(np.uint16)
+    assert got.shape == want.shape
+    assert np.array_equal(got, want), np.flatnonzero(got != want)[:10]
