@@ -192,7 +192,7 @@ def qft_leg(args):
 
 def cfg2_leg(args):
     """configs[2]: 32-qubit U3/CX brick, depth 24, complex64 with fused
-    5-qubit 3xTF32 tensor-core blocks, then 10^6 Z-basis shots; 1 - F and
+    5-qubit tensor-core blocks (f16 hi/lo halves), then 10^6 Z-basis shots; 1 - F and
     outcome TV against a complex128 run of the same circuit on the GPU
     (32 GiB + 64 GiB of HBM).  Opt-in (--cfg2): the complex128 run alone
     takes tens of seconds."""

@@ -194,7 +194,8 @@ int q1g_plan_block_matrix(const q1g_plan* p, size_t i, const double* mats_flat, 
 /* mats_flat = all gates' matrices concatenated ((re, im) doubles). */
 int q1g_plan_run(q1g_plan* p, q1g_state* s, const double* mats_flat, size_t n_doubles);
 /* Kernel for dense complex64 blocks of >= 3 qubits on states of >= 12 qubits:
- * 1 (default) = tcgen05 tensor cores (3xTF32), 0 = CUDA cores (FP32). */
+ * 1 (default) = tcgen05 tensor cores (FP32-accurate: three f16 products of
+ * 11-bit operand halves), 0 = CUDA cores (FP32). */
 int q1g_plan_set_tensor_cores(q1g_plan* p, int enable);
 
 /* ---- batches of independent circuits: one persistent launch, replayed from a

@@ -1,4 +1,5 @@
-// Fused 5-qubit blocks as tensor-core contractions (complex64 state, 3xTF32).
+// Fused 5-qubit blocks as tensor-core contractions (complex64 state, f16
+// operand halves, FP32 accuracy).
 //
 // A fused block is a dense 32x32 complex matrix M on five qubits (gate
 // positions p_0 > ... > p_4).  The state is cut into tiles of 2^12

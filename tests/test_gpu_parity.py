@@ -585,7 +585,7 @@ def test_fused_plans_match_plain(width):
 def test_tensor_core_block_is_exact_on_split_values():
     """A 3-qubit cyclic permutation (entries 0/1) on amplitudes with 20
     fraction bits goes through the tensor-core block kernel; hi + lo recovers
-    every amplitude, so the result is exact, not TF32-rounded."""
+    every amplitude, so the result is exact, not rounded to 11 bits."""
     n = 12
     k = np.arange(1 << n) % 4096
     amps = ((1.0 + k * 2.0 ** -20) / 64.0).astype(np.complex128)
