@@ -712,7 +712,8 @@ static TcPass lower_tc_pass(const std::vector<const std::vector<cd>*>& mats,
             md[2 * e] = m32[e].real();
             md[2 * e + 1] = m32[e].imag();
         }
-        build_tc_image(md.data(), t.images.data() + bi * kTcImageHalves);
+        build_tc_image(md.data(), t.images.data() + bi * kTcImageHalves,
+                       bi + 1 == mats.size() ? kTcLastBScaleLog2 : 0);
         TcBlockGeom& G = t.offs.blk[bi];
         int r = 0;
         for (int j = 0; j < 12; ++j)

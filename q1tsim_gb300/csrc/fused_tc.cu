@@ -18,8 +18,10 @@
 // so one 32-bit TMEM column holds one complex amplitude and a row's operands
 // take 64 columns.  f16 has a narrow exponent range, so the operands are
 // scaled by powers of two: amplitudes by 2^14 / 2^ceil(log2 sqrt(max column
-// norm)) (at most 2^14 in magnitude for blocks whose rows have 2-norm <= 1),
-// R by 2^14; the epilogue undoes both exactly.  The correction products go to
+// norm)) (at most 2^14 in magnitude for blocks whose rows have 2-norm <= 1)
+// as the first block of a pass reads them; they stay scaled into the second
+// block (whose R is not scaled), and the last block's R is scaled by 2^14
+// and its epilogue undoes both exactly.  The correction products go to
 // a second accumulator with the lo halves pre-scaled by 2^11 (exact), and the
 // epilogue adds D_corr * 2^-11: summed in one accumulator with the main
 // products, the correction terms were lost.  B is stored as [B_hi; B_lo]
@@ -80,8 +82,8 @@ constexpr int kTcThreads = kConsumers + 96;
 constexpr uint32_t kTileBytes = 4096 * 8;        // one tile (complex64), without padding
 constexpr uint32_t kTmemCols = 512;
 constexpr float kLoScale = 2048.0f;     // 2^11: lo halves are stored scaled up
+constexpr float kLoUnscale = 1.0f / 2048.0f;
 constexpr uint32_t kBImage = 16384;     // one block's [B_hi; B_lo']: 128 rows x 64 f16 (128 B)
-constexpr int kBScaleLog2 = 14;         // B entries (|R| <= 1) are stored times 2^14
 constexpr uint32_t kMaxStages = 8;
 // shared memory: [0, 1024) barriers, TMEM slot, abort flag, run offsets;
 // then nblocks B images; then the stages.
@@ -303,11 +305,12 @@ __device__ __forceinline__ uint32_t pack_f16x2(float first, float second)
     return d;
 }
 
-// Amplitude v scaled by sc -> hi = (re, im) to 11 bits and lo = 2^11 (v sc - hi),
-// each an f16 pair with the real part in the low half.
+// Amplitude v (times sc when SCALE) -> hi = (re, im) to 11 bits and
+// lo = 2^11 (v - hi), each an f16 pair with the real part in the low half.
+template <bool SCALE>
 __device__ __forceinline__ void split_amp(float2 v, float sc, uint32_t& hi, uint32_t& lo)
 {
-    const float re = v.x * sc, im = v.y * sc;
+    const float re = SCALE ? v.x * sc : v.x, im = SCALE ? v.y * sc : v.y;
     const float hr = to_tf32(re), hm = to_tf32(im);
     hi = pack_f16x2(hr, hm);
     lo = pack_f16x2((re - hr) * kLoScale, (im - hm) * kLoScale);
@@ -315,8 +318,9 @@ __device__ __forceinline__ void split_amp(float2 v, float sc, uint32_t& hi, uint
 
 // Gates 16*HH .. 16*HH+15 of row `rowb` -> f16 operands in TMEM columns
 // 32*HH .. 32*HH+31: per K-step of 8 gates (16 f16), 8 columns of hi pairs
-// then 8 of lo pairs.
-template <int HH>
+// then 8 of lo pairs.  SCALE: the stage holds plain amplitudes (first block
+// of a pass), which enter times sc; later blocks find them scaled already.
+template <int HH, bool SCALE>
 __device__ __forceinline__ void split_half(const uint8_t* raw, uint32_t rowb, const TcBlockGeom& G, uint32_t tl,
                                            float sc)
 {
@@ -326,34 +330,37 @@ __device__ __forceinline__ void split_half(const uint8_t* raw, uint32_t rowb, co
         for (int m = 0; m < 8; ++m) {
             const float4 p = *(const float4*)(raw + rowb + G.gateoff[16 * HH + 2 * m]);
             const int j = 2 * m, c = (j >> 3) * 16 + (j & 7);
-            split_amp(make_float2(p.x, p.y), sc, v[c], v[c + 8]);
-            split_amp(make_float2(p.z, p.w), sc, v[c + 1], v[c + 9]);
+            split_amp<SCALE>(make_float2(p.x, p.y), sc, v[c], v[c + 8]);
+            split_amp<SCALE>(make_float2(p.z, p.w), sc, v[c + 1], v[c + 9]);
         }
     } else {
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
             const float2 p = *(const float2*)(raw + rowb + G.gateoff[16 * HH + j]);
             const int c = (j >> 3) * 16 + (j & 7);
-            split_amp(p, sc, v[c], v[c + 8]);
+            split_amp<SCALE>(p, sc, v[c], v[c + 8]);
         }
     }
     tmem_st32(tl + 32u * HH, v);
 }
 
-// D_main * dm + D_corr * dc for gates 16*HH .. 16*HH+15 of row `rowb` (the
-// scales undo the operands' and the lo halves' powers of two), back into the
-// stage.
-template <int HH>
+// D_main + 2^-11 D_corr for gates 16*HH .. 16*HH+15 of row `rowb`, back
+// into the stage.  UNSCALE (last block of a pass): times `unscale`, which
+// undoes the operands' powers of two; otherwise the amplitudes stay scaled
+// for the next block (whose B is not scaled).
+template <int HH, bool UNSCALE>
 __device__ __forceinline__ void writeback_half(uint8_t* raw, uint32_t rowb, const TcBlockGeom& G, uint32_t tl,
-                                               float dm_scale, float dc_scale)
+                                               float unscale)
 {
     uint32_t dm[32], dc[32];
     tmem_ld32(tl + 128u + 32u * HH, dm);
     tmem_ld32(tl + 192u + 32u * HH, dc);
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-    for (int j = 0; j < 32; ++j)
-        dm[j] = __float_as_uint(__fmaf_rn(__uint_as_float(dc[j]), dc_scale, __uint_as_float(dm[j]) * dm_scale));
+    for (int j = 0; j < 32; ++j) {
+        const float d = __fmaf_rn(__uint_as_float(dc[j]), kLoUnscale, __uint_as_float(dm[j]));
+        dm[j] = __float_as_uint(UNSCALE ? d * unscale : d);
+    }
     if (G.vec2) {
 #pragma unroll
         for (int m = 0; m < 8; ++m)
@@ -524,8 +531,13 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, const __grid_constant__ Inde
                 const uint32_t rowb = b ? rowb1 : rowb0;
                 if (b > 0) group_sync(gbar);    // the previous block's results are all staged
                 // row t -> hi/lo operands, columns 2g+c, in TMEM
-                split_half<0>(raw, rowb, G, tl, offs.ascale);
-                split_half<1>(raw, rowb, G, tl, offs.ascale);
+                if (b == 0) {
+                    split_half<0, true>(raw, rowb, G, tl, offs.ascale);
+                    split_half<1, true>(raw, rowb, G, tl, offs.ascale);
+                } else {
+                    split_half<0, false>(raw, rowb, G, tl, offs.ascale);
+                    split_half<1, false>(raw, rowb, G, tl, offs.ascale);
+                }
                 asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
                 asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
                 group_sync(gbar);
@@ -549,8 +561,13 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, const __grid_constant__ Inde
                 }
                 ++mph;
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                writeback_half<0>(raw, rowb, G, tl, offs.dmain, offs.dcorr);
-                writeback_half<1>(raw, rowb, G, tl, offs.dmain, offs.dcorr);
+                if ((uint32_t)b + 1 == nblocks) {
+                    writeback_half<0, true>(raw, rowb, G, tl, offs.unscale);
+                    writeback_half<1, true>(raw, rowb, G, tl, offs.unscale);
+                } else {
+                    writeback_half<0, false>(raw, rowb, G, tl, offs.unscale);
+                    writeback_half<1, false>(raw, rowb, G, tl, offs.unscale);
+                }
                 asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             }
             if (stop) break;
@@ -700,13 +717,14 @@ void tc_choose_padding(TcOffsets& o, bool tma_ok)
     }
 }
 
-void build_tc_image(const double* m, uint16_t* image)
+void build_tc_image(const double* m, uint16_t* image, int scale_log2)
 {
     // R[n][k]: n = 2g'+c' output component, k = 2g+c input component, times
-    // 2^14.  Rows n of B_hi and 64+n of B_lo' (= 2^11 lo) as f16, K-major,
-    // SWIZZLE_128B: 8-row groups of 1024 B, 16-byte chunk j of row r at
-    // chunk position j ^ (r & 7).
-    const double bs = std::ldexp(1.0, kBScaleLog2);
+    // 2^scale_log2.  Rows n of B_hi and 64+n of B_lo' (= 2^11 lo) as f16,
+    // K-major, SWIZZLE_128B: 8-row groups of 1024 B, 16-byte chunk j of row r
+    // at chunk position j ^ (r & 7).  Entries below f16's normal range keep
+    // their remainder in B_lo' (scaled by 2^11), to 2^-35 absolute.
+    const double bs = std::ldexp(1.0, scale_log2);
     for (int gp = 0; gp < 32; ++gp)
         for (int g = 0; g < 32; ++g) {
             const double re = m[2 * (gp * 32 + g)], im = m[2 * (gp * 32 + g) + 1];
@@ -732,13 +750,14 @@ void tc_operand_scales(double max_norm, TcOffsets& offs)
 {
     // |amplitude| <= sqrt(column norm) <= 2^e: amplitudes enter the tensor
     // cores times 2^(14-e), at most 2^14 (f16 holds up to 65504), so that
-    // those above 2^(-28+e) are normal f16 numbers
+    // those above 2^(-28+e) are normal f16 numbers.  They stay scaled from
+    // block to block; the last block's B carries 2^kTcLastBScaleLog2 and its
+    // epilogue multiplies by `unscale`.
     int e = 0;
     if (max_norm > 0.0 && std::isfinite(max_norm)) e = (int)std::ceil(0.5 * std::log2(max_norm));
     e = std::max(-60, std::min(60, e));
     offs.ascale = std::ldexp(1.0f, 14 - e);
-    offs.dmain = std::ldexp(1.0f, -(14 - e) - kBScaleLog2);
-    offs.dcorr = std::ldexp(offs.dmain, -11);
+    offs.unscale = std::ldexp(1.0f, -(14 - e) - kTcLastBScaleLog2);
 }
 
 bool tc_block_bounded(const std::complex<double>* m, int dim)

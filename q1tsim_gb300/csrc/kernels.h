@@ -109,11 +109,10 @@ struct TcOffsets {
     uint32_t use_tma;        // 1: one tensor-map copy per tile (set by launch_fused_tc)
     uint32_t tshift[5];      // tensor-map coordinate d = (tile >> tshift[d]) & tmask[d]
     uint32_t tmask[5];
-    // operand scales (tc_operand_scales): amplitudes enter as f16 times
-    // ascale; D_main * dmain + D_corr * dcorr is the result
+    // operand scales (tc_operand_scales): amplitudes enter the first block
+    // as f16 times ascale; (D_main + 2^-11 D_corr) * unscale after the last
     float ascale;
-    float dmain;
-    float dcorr;
+    float unscale;
     uint32_t pad1_;
     uint64_t run_off[32];
     TcBlockGeom blk[2];
@@ -145,9 +144,11 @@ cudaError_t launch_fused_tc(float2* amps, uint64_t ntiles, const IndexMap& tilem
                             const TcTileBox& box, const void* d_bimage, int* d_err, int sm_count,
                             cudaStream_t st);
 // Host: the 16 KB image (8192 f16) for the 32x32 complex matrix m
-// (row-major (re, im)), entries times 2^14.
+// (row-major (re, im)), entries times 2^scale_log2: kTcLastBScaleLog2 for
+// the last block of a pass, 0 for the one before (whose output stays scaled).
 constexpr size_t kTcImageHalves = 8192;
-void build_tc_image(const double* m, uint16_t* image);
+constexpr int kTcLastBScaleLog2 = 14;
+void build_tc_image(const double* m, uint16_t* image, int scale_log2);
 // Host: offs.ascale / dmain / dcorr for states whose columns have squared
 // norms at most max_norm.
 void tc_operand_scales(double max_norm, TcOffsets& offs);
