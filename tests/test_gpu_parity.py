@@ -894,6 +894,32 @@ def test_autotuned_circuit_matches_oracle():
     assert autotune.tune.last_timings[0]["seconds"] <= autotune.tune.last_timings[-1]["seconds"]
 
 
+def test_tensor_core_plan_with_many_tiles_per_sm_matches_oracle():
+    """21 qubits: 512 tiles of 4096 amplitudes, so every SM's CTA takes
+    several tiles and both consumer groups of the tensor-core kernel work
+    (at 12-16 qubits a CTA has one tile at most).  A brick of U3/CX fused
+    into 5-qubit blocks, one- and two-block passes, against the oracle."""
+    n = 21
+    rng = np.random.default_rng(2101)
+    gates = []
+    for layer in range(6):
+        for q in range(n):
+            gates.append((G.U3(*rng.uniform(0, 2 * np.pi, 3)), [q]))
+        for q in range(layer % 2, n - 1, 2):
+            gates.append((G.CX(), [q, q + 1]))
+    amps = rand_state(n, rng)
+    o = orc.OracleState.from_amplitudes(amps, 1)
+    for gt, b in gates:
+        o.apply_gate(gt.matrix(), b)
+    ref = o.states()[:, 0]
+    mats = np.concatenate([np.ascontiguousarray(gt.matrix()).ravel() for gt, _ in gates]).view(np.float64)
+    g = VectorState.from_amplitudes(amps, 1, "c64")
+    g.apply_plan(Plan(n, [b for _, b in gates], 5), mats)
+    out = g.states()[:, 0]
+    assert np.max(np.abs(out - ref)) <= TOL64, float(np.max(np.abs(out - ref)))
+    assert 1 - abs(np.vdot(ref, out)) ** 2 / np.linalg.norm(out) ** 2 <= 1e-9
+
+
 def test_fused_plan_renormalises_to_the_input_norm():
     """After a tensor-core plan the column norms equal the input norms (an
     unnormalised input keeps its norm)."""
