@@ -625,16 +625,6 @@ q1g_plan::~q1g_plan()
 
 namespace q1g {
 
-// Tensor-core lowering of a pass: one or two fused blocks (each <= 5
-// qubits) whose positions fit in one 12-position tile.  Each block is padded
-// with untouched tile positions to five gate positions; its other seven tile
-// positions are its rows.
-struct TcPass {
-    IndexMap tilemap{};
-    TcOffsets offs{};
-    TcTileBox box{};             // the tile as a tensor-map box
-    std::vector<uint16_t> images;   // nblocks x 16 KB of f16
-};
 
 static std::vector<int> positions_of(const std::vector<int>& qubits, int nbits)
 {
@@ -846,10 +836,12 @@ static void run_phase_block(q1g_plan* p, q1g_state* s, const FusedBlock& b, cons
 }
 
 // Positions a plan may leave out of its start-of-run subspace: the compact
-// state is at most 1/8 of the full one.  Below kPrefixMinQubits the full
-// state is small enough as it is.
+// state is at most 1/8 of the full one.  Below kPrefixMinQubits a full pass
+// costs microseconds, less than the compact plan's own launches and norm
+// check (a 16-qubit brick of 20 layers with 8192 runs took 6.4 ms with the
+// prefix against 4.3 ms without).
 constexpr int kPrefixSpare = 3;
-constexpr int kPrefixMinQubits = 16;
+constexpr int kPrefixMinQubits = 24;
 
 // A basis state stays a basis state on every position no gate has touched.
 // So the plan's leading blocks, as long as together they touch at most
@@ -974,6 +966,31 @@ void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n, bool subs
         ops[bi] = classify(bmats[bi].data(), (int)bbits[bi].size(), bbits[bi].data(), s->nbits);
         ready[bi] = 1;
     };
+    // The lowering of a tensor-core pass (tile geometry, padding and the f16
+    // images) is kept with the plan, keyed by its first block and block count
+    // and checked against the blocks' matrices and qubits and the state's
+    // shape: a circuit run again builds no images (about 50 us per block on
+    // the host, which small states do not hide behind their passes).
+    auto lower_tc_cached = [&](size_t i, int nblk) -> TcPass {
+        if (p->tc_memo.size() != 2 * nb) p->tc_memo.assign(2 * nb, TcPassMemo{});
+        TcPassMemo& e = p->tc_memo[2 * i + (size_t)(nblk - 1)];
+        bool hit = e.nblocks == nblk && e.nbits == s->nbits && e.ncols == s->ncols;
+        for (int j = 0; hit && j < nblk; ++j) hit = e.bits[j] == bbits[i + j] && e.mats[j] == bmats[i + j];
+        if (!hit) {
+            if (nblk == 2)
+                e.pass = lower_tc_pass({&bmats[i], &bmats[i + 1]}, {&bbits[i], &bbits[i + 1]}, s->nbits, s->ncols);
+            else
+                e.pass = lower_tc_pass({&bmats[i]}, {&bbits[i]}, s->nbits, s->ncols);
+            e.nblocks = nblk;
+            e.nbits = s->nbits;
+            e.ncols = s->ncols;
+            for (int j = 0; j < nblk; ++j) {
+                e.bits[j] = bbits[i + j];
+                e.mats[j] = bmats[i + j];
+            }
+        }
+        return e.pass;
+    };
     // tensor-core eligible: dense blocks of >= 3 target qubits
     auto eligible = [&](size_t bi) {
         if (p->blocks[bi].phase_run || p->blocks[bi].swap_run) return false;
@@ -1033,12 +1050,12 @@ void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n, bool subs
                 const int L2 = tile_run_bits(T2);
                 if (high <= kMaxTcHighPositions &&
                     (L2 >= kMinTcRunBits || tc_tile_box(T2.data(), s->nbits, s->ncols).usable)) {
-                    t = lower_tc_pass({&bmats[i], &bmats[i + 1]}, {&bbits[i], &bbits[i + 1]}, s->nbits, s->ncols);
+                    t = lower_tc_cached(i, 2);
                     // short runs only as one unpadded tensor-map copy
                     paired = L2 >= kMinTcRunBits || t.offs.pad_shift >= 31;
                 }
             }
-            if (!paired) t = lower_tc_pass({&bmats[i]}, {&bbits[i]}, s->nbits, s->ncols);
+            if (!paired) t = lower_tc_cached(i, 1);
             begin();
             if (!any_tc) {
                 s->errbuf.ensure(sizeof(int));

@@ -161,6 +161,28 @@ struct q1g_state {
     void sync();
 };
 
+namespace q1g {
+// Tensor-core lowering of a pass: one or two fused blocks (each <= 5
+// qubits) whose positions fit in one 12-position tile.  Each block is padded
+// with untouched tile positions to five gate positions; its other seven tile
+// positions are its rows.
+struct TcPass {
+    IndexMap tilemap{};
+    TcOffsets offs{};
+    TcTileBox box{};                // the tile as a tensor-map box
+    std::vector<uint16_t> images;   // nblocks x kTcImageHalves f16
+};
+// A pass's lowering kept by its plan, with what it was made from.
+struct TcPassMemo {
+    int nblocks = 0;
+    int nbits = -1;
+    uint64_t ncols = 0;
+    std::vector<int> bits[2];
+    std::vector<std::complex<double>> mats[2];
+    TcPass pass;
+};
+}  // namespace q1g
+
 struct q1g_plan {
     int nbits = 0;
     int width = 0;
@@ -178,6 +200,7 @@ struct q1g_plan {
     size_t prefix_len = 0;
     uint64_t prefix_mask = 0;
     std::unique_ptr<q1g_plan> prefix_plan;
+    std::vector<q1g::TcPassMemo> tc_memo;   // by 2 * first block + block count - 1 (plan_run)
     q1g::HostBuf hmats;            // pinned staging of dense matrices
     q1g::DevBuf dmats;
     cudaEvent_t staged = nullptr;  // last upload of hmats finished
