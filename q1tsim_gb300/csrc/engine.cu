@@ -558,28 +558,52 @@ void q1g_state::measure_all(const size_t* cbits, size_t ncbits, uint64_t* res, s
                    "download outcomes");
         sync();
         h_outc = hstage.as<uint64_t>();
-        const uint64_t* h_word = h_outc + nshots;
-        for (uint64_t r = 0; r < nshots; ++r) res[r] = (res[r] & mask) | h_word[r];
+        if (!collapse) {
+            const uint64_t* h_word = h_outc + nshots;
+            for (uint64_t r = 0; r < nshots; ++r) res[r] = (res[r] & mask) | h_word[r];
+            return;
+        }
     }
     if (!collapse) return;
-    // one basis column per distinct (column, outcome), in order, written into
-    // basis/counts themselves: their capacity carries over between runs
+    // one basis column per distinct (column, outcome), in order: outcomes are
+    // sorted within a column, so a column's distinct outcomes are its runs of
+    // equal ones.  A first pass writes the words and counts the runs (about
+    // 10^6 at 30 qubits and 10^6 shots, two for a GHZ state), a second fills
+    // basis/counts sized to that count; their capacity carries over between
+    // runs.
+    const uint64_t* h_word = sparse ? nullptr : h_outc + nshots;
     const std::vector<uint64_t> runs(counts.begin(), counts.end());
+    uint64_t m = 0, off = 0;
+    for (uint64_t c = 0; c < runs.size(); ++c) {
+        const uint64_t end = off + runs[c];
+        for (uint64_t r = off; r < end; ++r) {
+            if (h_word) res[r] = (res[r] & mask) | h_word[r];
+            m += (r == off || h_outc[r] != h_outc[r - 1]) ? 1 : 0;
+        }
+        off = end;
+    }
     basis.clear();
     counts.clear();
-    uint64_t off = 0;
+    basis.resize(m);
+    counts.resize(m);
+    uint64_t* bp = basis.data();
+    uint64_t* cp = counts.data();
+    uint64_t k = 0;
+    off = 0;
     for (uint64_t c = 0; c < runs.size(); ++c) {
-        for (uint64_t r = 0; r < runs[c]; ++r) {
-            if (r == 0 || h_outc[off + r] != h_outc[off + r - 1]) {
-                basis.push_back(h_outc[off + r]);
-                counts.push_back(0);
+        const uint64_t end = off + runs[c];
+        for (uint64_t r = off; r < end; ++r) {
+            if (r == off || h_outc[r] != h_outc[r - 1]) {
+                bp[k] = h_outc[r];
+                cp[k] = 0;
+                ++k;
             }
-            counts.back() += 1;
+            ++cp[k - 1];
         }
-        off += runs[c];
+        off = end;
     }
     sparse = true;
-    ncols = basis.size();
+    ncols = m;
     norms.assign(ncols, 1.0);
 }
 
