@@ -72,8 +72,57 @@ class Circuit:
 
     @staticmethod
     def _flat(seq):
-        mats = [np.ascontiguousarray(op[1].matrix(), dtype=np.complex128).ravel() for op in seq]
-        return np.concatenate(mats).view(np.float64) if mats else np.zeros(0)
+        """The segment's gate matrices, concatenated row-major as (re, im)
+        doubles.  Fixed gates contribute their stored matrices; U3 gates (most
+        of a random circuit) are evaluated together with numpy, with the
+        formulas of gates._u3 (src/gates/u3.rs:74-84).  A server builds these
+        for every request, under the interpreter lock."""
+        n = len(seq)
+        if n == 0:
+            return np.zeros(0)
+        sizes = np.empty(n, dtype=np.int64)
+        parts = [None] * n
+        u3_rows, u3_par, cu1_rows, cu1_par = [], [], [], []
+        for i, op in enumerate(seq):
+            g = op[1]
+            sizes[i] = 1 << (2 * g.nr_affected_bits())
+            tg = type(g)
+            if tg is G._Param and g._fn is G._u3:
+                u3_rows.append(i)
+                u3_par.append([float(p) for p in g.params])
+                continue
+            if tg is G.C and type(g.gate) is G._Param and g.gate._fn is G._u1:
+                cu1_rows.append(i)
+                cu1_par.append(float(g.gate.params[0]))
+                continue
+            shared = getattr(g, "_shared_matrix", None)
+            m = shared() if shared is not None else None
+            parts[i] = m if m is not None else np.asarray(g.matrix(), dtype=np.complex128)
+        offs = np.zeros(n + 1, dtype=np.int64)
+        np.cumsum(sizes, out=offs[1:])
+        out = np.empty(int(offs[-1]), dtype=np.complex128)
+        for i, m in enumerate(parts):
+            if m is not None:
+                out[offs[i]:offs[i + 1]] = m.ravel()
+        if u3_rows:
+            p = np.asarray(u3_par)
+            theta, phi, lmb = p[:, 0], p[:, 1], p[:, 2]
+            c, s = np.cos(0.5 * theta), np.sin(0.5 * theta)
+            pl = phi + lmb
+            m = np.empty((len(u3_rows), 4), dtype=np.complex128)
+            m.real[:, 0], m.imag[:, 0] = c, 0.0
+            m.real[:, 1], m.imag[:, 1] = -(s * np.cos(lmb)), -(s * np.sin(lmb))
+            m.real[:, 2], m.imag[:, 2] = s * np.cos(phi), s * np.sin(phi)
+            m.real[:, 3], m.imag[:, 3] = c * np.cos(pl), c * np.sin(pl)
+            out[offs[np.asarray(u3_rows)][:, None] + np.arange(4)] = m
+        if cu1_rows:
+            # C(U1(lmb)) = diag(1, 1, 1, e^(i lmb)) (src/gates/u1.rs:69-84)
+            lmb = np.asarray(cu1_par)
+            m = np.zeros((len(cu1_rows), 16), dtype=np.complex128)
+            m[:, 0] = m[:, 5] = m[:, 10] = 1.0
+            m.real[:, 15], m.imag[:, 15] = np.cos(lmb), np.sin(lmb)
+            out[offs[np.asarray(cu1_rows)][:, None] + np.arange(16)] = m
+        return out.view(np.float64)
 
     def _flat_current(self, idx, seq):
         """The segment's matrices for this execution.  They are evaluated

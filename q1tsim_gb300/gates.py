@@ -95,6 +95,10 @@ class _Fixed(Gate):
     def matrix(self):
         return self._m.copy()
 
+    def _shared_matrix(self):
+        """The matrix itself, not a copy (read by Circuit._flat only)."""
+        return self._m
+
     def is_diagonal(self):
         return bool(np.count_nonzero(self._m - np.diag(np.diag(self._m))) == 0)
 
@@ -172,12 +176,13 @@ class _Param(Gate):
         self.params = list(params)
         self.nbits = nbits
         self._diagonal = diagonal
+        self._refs = [p for p in self.params if isinstance(p, Parameter)]
 
     def matrix(self):
         return np.asarray(self._fn(*[_val(p) for p in self.params]), dtype=np.complex128)
 
     def param_key(self):
-        return tuple(p.value for p in self.params if isinstance(p, Parameter))
+        return tuple(p.value for p in self._refs) if self._refs else ()
 
     def is_diagonal(self):
         return self._diagonal
@@ -245,6 +250,9 @@ def U3(theta, phi, lmb):
     return _Param("U3", _u3, [theta, phi, lmb])
 
 
+_CONTROLLED_FIXED = {}
+
+
 class C(Gate):
     """Controlled gate: identity, with `gate` in the bottom-right block
     (src/gates/controlled.rs:62-71); the control is the first bit."""
@@ -260,6 +268,20 @@ class C(Gate):
         res = np.eye(2 * g, dtype=np.complex128)
         res[g:, g:] = gm
         return res
+
+    def _shared_matrix(self):
+        """For a fixed inner gate, one matrix shared by every instance with
+        that inner matrix (a CX per gate of a circuit would otherwise build
+        its 4x4 each time); None otherwise.  Read by Circuit._flat only."""
+        if not isinstance(self.gate, _Fixed):
+            return None
+        key = (self.gate._m.shape[0], self.gate._m.tobytes())
+        m = _CONTROLLED_FIXED.get(key)
+        if m is None:
+            m = self.matrix()
+            m.setflags(write=False)
+            _CONTROLLED_FIXED[key] = m
+        return m
 
     def param_key(self):
         return self.gate.param_key()

@@ -161,3 +161,25 @@ def test_segment_matrices_follow_reference_parameters():
     np.testing.assert_allclose(second, c._flat(seq), rtol=0, atol=0)
     np.testing.assert_allclose(second[8:16], first[8:16], rtol=0, atol=0)   # the U3 block is unchanged
     assert not np.array_equal(second[:8], first[:8])
+
+
+def test_segment_matrices_equal_each_gates_matrix():
+    """Circuit._flat evaluates U3 and controlled-U1 gates together and shares
+    fixed controlled matrices: the result equals each gate's own matrix(),
+    bit for bit, over a mix of gate kinds and reference parameters."""
+    from q1tsim_gb300 import Circuit as GpuCircuit
+    from q1tsim_gb300 import gates as G
+    rng = np.random.default_rng(3)
+    p, q = q1tsim.RefParam(0.3), q1tsim.RefParam(1.3)
+    make = [lambda: G.U3(*rng.uniform(-7, 7, 3)), G.CX, G.H, lambda: G.RX(rng.uniform(0, 7)),
+            lambda: G.CRZ(p), G.Swap, lambda: G.U3(p, 0.2, q), lambda: G.CU1(rng.uniform(-7, 7)),
+            lambda: G.CU1(q), G.CZ, lambda: G.U1(rng.uniform(0, 7)), G.T]
+    seq = [("gate", make[int(rng.integers(0, len(make)))](), [0]) for _ in range(500)]
+    want = np.concatenate([np.ascontiguousarray(op[1].matrix(), dtype=np.complex128).ravel()
+                           for op in seq]).view(np.float64)
+    got = GpuCircuit._flat(seq)
+    assert got.dtype == np.float64 and np.array_equal(got, want)
+    p.assign(-2.5)
+    want2 = np.concatenate([np.ascontiguousarray(op[1].matrix(), dtype=np.complex128).ravel()
+                            for op in seq]).view(np.float64)
+    assert np.array_equal(GpuCircuit._flat(seq), want2) and not np.array_equal(want2, want)
