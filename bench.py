@@ -322,13 +322,13 @@ def serving_leg(args):
     admitted by HBM budget into concurrent slots."""
     from q1tsim_gb300.serving import latency_stats, mixed_requests, serve
     reqs = mixed_requests(args.serve_requests, args.seed + 23)
-    done, wall, srv = serve(reqs, rate_hz=2000.0, hbm_budget_bytes=64 << 30, slots=8, seed=args.seed)
+    done, wall, srv = serve(reqs, rate_hz=2000.0, hbm_budget_bytes=64 << 30, slots=16, seed=args.seed)
     st = latency_stats(done)
     first = min(r.arrival for r in done)
     last = max(r.done for r in done)
     st.update({"requests": len(reqs), "offered_rate_hz": 2000.0,
                "circuits_per_s": len(done) / (last - first), "peak_inflight": srv.peak_inflight,
-               "peak_budget_gib": srv.peak_used / 2 ** 30, "slots": 8, "hbm_budget_gib": 64,
+               "peak_budget_gib": srv.peak_used / 2 ** 30, "slots": 16, "hbm_budget_gib": 64,
                "workload": "Poisson 2000/s mix of GHZ, QFT (on a random product state) and U3/CX brick "
                            "circuits, 10-26 qubits, depth 5-50, 4096 shots, complex64 fused"})
     return st

@@ -56,7 +56,11 @@ def run_alone(req):
 class Server:
     """Admits requests by HBM budget into `slots` concurrent device workers."""
 
-    def __init__(self, hbm_budget_bytes, slots=8):
+    # 16 slots by default: a slot's thread spends much of each request on the
+    # host (plan lowering, waits on its own stream), so more slots keep the
+    # device busier; on the serving mix 8 / 12 / 16 slots gave 970 / 1069 /
+    # 1126 circuits/s
+    def __init__(self, hbm_budget_bytes, slots=16):
         self.budget = int(hbm_budget_bytes)
         self.slots = int(slots)
         self.used = 0
@@ -137,7 +141,7 @@ class Server:
                 self.cv.notify_all()
 
 
-def serve(requests, rate_hz, hbm_budget_bytes, slots=8, seed=0):
+def serve(requests, rate_hz, hbm_budget_bytes, slots=16, seed=0):
     """Replay `requests` as a Poisson stream of mean rate `rate_hz` and serve
     them.  Returns (requests in completion order, wall seconds, server)."""
     rng = np.random.default_rng(seed)
