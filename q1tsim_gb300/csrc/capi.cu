@@ -229,6 +229,8 @@ int q1g_state_compare(q1g_state* a, q1g_state* b, double* out5)
             throw Error(Q1G_ERR_INVALID_ARGUMENT, "states differ in shape");
         a->ensure_dense();
         b->ensure_dense();
+        a->settle_norms();
+        b->settle_norms();
         b->sync();
         const uint64_t n = a->ncols * a->N;
         const uint64_t want = (n + 255) / 256;

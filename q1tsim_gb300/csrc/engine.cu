@@ -298,6 +298,7 @@ static std::vector<CondRange> conditional_ranges(const std::vector<uint64_t>& co
 void q1g_state::apply_conditional(const uint8_t* control, size_t ncontrol, const double* mat,
                                   size_t k, const size_t* bits, size_t nbits_given)
 {
+    settle_norms();
     if (ncontrol != nshots)
         throw Error(Q1G_ERR_INVALID_NR_CONTROL_BITS, "Expected " + std::to_string(nshots) +
                                                          " control bits, got " + std::to_string(ncontrol));
@@ -370,6 +371,7 @@ void q1g_state::measure(size_t qbit, size_t cbit, uint64_t* res, size_t res_len,
                         const double* uniforms, size_t nu, q1g_rng* rng, bool collapse)
 {
     if (qbit >= (size_t)nbits) throw Error(Q1G_ERR_INVALID_QBIT, "Invalid qubit index " + std::to_string(qbit));
+    settle_norms();     // P(0) is the half's weight against the column's norm
     if (res_len < nshots)
         throw Error(Q1G_ERR_NOT_ENOUGH_SPACE, "Unable to store " + std::to_string(nshots) +
                                                   " measurements in array of size " + std::to_string(res_len));
@@ -603,12 +605,14 @@ void q1g_state::measure_all(const size_t* cbits, size_t ncbits, uint64_t* res, s
         off = end;
     }
     sparse = true;
+    norm_pending = false;
     ncols = m;
     norms.assign(ncols, 1.0);
 }
 
 void q1g_state::reset_all()
 {
+    norm_pending = false;
     sparse = true;
     basis.assign(1, 0);
     counts.assign(1, nshots);
@@ -620,6 +624,7 @@ void q1g_state::download(double* out, size_t len)
 {
     if (len < 2 * ncols * N)
         throw Error(Q1G_ERR_NOT_ENOUGH_SPACE, "download buffer too small");
+    settle_norms();
     if (sparse) {
         std::memset(out, 0, 2 * ncols * N * sizeof(double));
         for (uint64_t c = 0; c < ncols; ++c) out[2 * (c * N + basis[c])] = 1.0;
@@ -947,6 +952,8 @@ static size_t run_subspace_prefix(q1g_plan* p, q1g_state* s, const double* mats,
     });
     s->sparse = false;
     s->basis.clear();
+    s->norm_pending = c->norm_pending;    // the compact plan's norm correction, if any, is still to come
+    c->norm_pending = false;
     for (auto& pe : c->pending) s->pending.push_back(pe);
     c->pending.clear();
     return p->prefix_len;
@@ -1144,8 +1151,30 @@ void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n, bool subs
     p->last_h2d_bytes = staged;
     if (!launched) return;
     if (any_tc) {
-        // per-column squared norms after the plan, then rescale each column to
-        // the norm it had before (the plan is unitary)
+        // the tensor-core passes' bounded waits: report an expiry now
+        s->hstage.ensure(sizeof(int));
+        int* h_flag = s->hstage.as<int>();
+        check_cuda(cudaMemcpyAsync(h_flag, s->errbuf.p, sizeof(int), cudaMemcpyDeviceToHost, s->stream),
+                   "read error flag");
+        s->sync();
+        if (*h_flag) throw Error(Q1G_ERR_TIMEOUT, "a tensor-core block kernel gave up waiting on its MMAs");
+        s->norm_pending = true;
+    }
+}
+
+}  // namespace q1g
+
+void q1g_state::settle_norms()
+{
+    using namespace q1g;
+    if (!norm_pending || sparse) {
+        norm_pending = false;
+        return;
+    }
+    q1g_state* s = this;
+    {
+        // per-column squared norms now, then rescale each column to the norm
+        // it should have (the plans since the last settle were unitary)
         const uint64_t total = s->total();
         const uint64_t chunk = std::min<uint64_t>(s->N, 256);
         const uint64_t nch = s->N / chunk;
@@ -1158,15 +1187,11 @@ void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n, bool subs
         });
         check_cuda(launch_segment_sums(d_sums, s->ncols, nch, d_norm, d_norm + 2 * s->ncols, s->stream),
                    "segment_sums");
-        s->hstage.ensure(s->ncols * sizeof(double) + sizeof(int));
+        s->hstage.ensure(s->ncols * sizeof(double));
         double* h_norm = s->hstage.as<double>();
-        int* h_flag = reinterpret_cast<int*>(h_norm + s->ncols);
         check_cuda(cudaMemcpyAsync(h_norm, d_norm, s->ncols * sizeof(double), cudaMemcpyDeviceToHost, s->stream),
                    "read norms");
-        check_cuda(cudaMemcpyAsync(h_flag, s->errbuf.p, sizeof(int), cudaMemcpyDeviceToHost, s->stream),
-                   "read error flag");
         s->sync();
-        if (*h_flag) throw Error(Q1G_ERR_TIMEOUT, "a tensor-core block kernel gave up waiting on its MMAs");
         std::vector<double> scale(s->ncols, 1.0);
         bool any_scale = false;
         for (uint64_t c = 0; c < s->ncols; ++c) {
@@ -1184,6 +1209,5 @@ void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n, bool subs
             s->sync();
         }
     }
+    norm_pending = false;
 }
-
-}  // namespace q1g

@@ -86,6 +86,14 @@ struct q1g_state {
     // cores rescale their result to it (their FP32 accumulation rounds toward
     // zero and shrinks the norm by ~1e-7 per block).
     std::vector<double> norms{1.0};
+    // After tensor-core passes the columns' actual norms may be off from
+    // `norms` by ~1e-7 per block (FP32 accumulation rounds toward zero).
+    // The rescale is left pending: sampling in measure_all divides by each
+    // column's total and a collapse leaves exact basis columns, unitary gates
+    // commute with it, and a later plan's passes keep the same bound.
+    // settle_norms() applies it where absolute amplitudes matter (download,
+    // compare, single-qubit measurement, conditional gates).
+    bool norm_pending = false;
 
     q1g::DevBuf amps, spare;
     q1g::DevBuf dscratch;   // doubles
@@ -147,6 +155,7 @@ struct q1g_state {
     void collect_profile();
 
     void ensure_dense();
+    void settle_norms();
     void apply_op(const q1g::GateOp& op, char* base, uint64_t total_amps);
     void apply_gate(const double* mat, size_t k, const size_t* bits, size_t nbits_given);
     void apply_conditional(const uint8_t* control, size_t ncontrol, const double* mat, size_t k,

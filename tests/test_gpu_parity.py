@@ -925,6 +925,41 @@ def test_tensor_core_plan_with_many_tiles_per_sm_matches_oracle():
     assert 1 - abs(np.vdot(ref, out)) ** 2 / np.linalg.norm(out) ** 2 <= 1e-9
 
 
+def test_norm_correction_left_pending_until_needed():
+    """A tensor-core plan leaves its norm correction pending: peek_all on the
+    unsettled state samples the same outcomes as on a settled copy (sampling
+    divides by the column totals), and a single-qubit measurement settles
+    first, so both copies end in the same state with the input norm."""
+    rng = np.random.default_rng(31)
+    n = 14
+    amps = rand_state(n, rng)
+    gl = [random_gate(n, rng) for _ in range(60)]
+    mats = np.concatenate([np.ascontiguousarray(gt.matrix()).ravel() for gt, _ in gl]).view(np.float64)
+    plan = Plan(n, [b for _, b in gl], 5)
+    shots = 64
+    a = VectorState.from_amplitudes(amps, shots, "c64")
+    b = VectorState.from_amplitudes(amps, shots, "c64")
+    a.apply_plan(plan, mats)
+    b.apply_plan(plan, mats)
+    b.states()                                   # settles b
+    u = np.sort(rng.random(shots))
+    ra = np.zeros(shots, dtype=np.uint64)
+    rb = np.zeros(shots, dtype=np.uint64)
+    a.peek_all_into(list(range(n)), ra, uniforms=u)
+    b.peek_all_into(list(range(n)), rb, uniforms=u)
+    assert np.array_equal(ra, rb)
+    u1 = rng.random(shots)
+    ma = np.zeros(shots, dtype=np.uint64)
+    mb = np.zeros(shots, dtype=np.uint64)
+    a.measure_into(3, 0, ma, uniforms=u1)
+    b.measure_into(3, 0, mb, uniforms=u1)
+    assert np.array_equal(ma, mb)
+    acc = b.compare(a)
+    # after the measurement each column (one per outcome) has norm 1
+    assert acc["max_abs_diff"] <= 1e-7 and abs(acc["norm_b"] - acc["norm_a"]) <= 1e-6, acc
+    assert abs(acc["norm_b"] - round(acc["norm_b"])) <= 1e-6, acc
+
+
 def test_fused_plan_renormalises_to_the_input_norm():
     """After a tensor-core plan the column norms equal the input norms (an
     unnormalised input keeps its norm)."""
