@@ -102,10 +102,18 @@ __device__ bool sample_one(const T* a, uint64_t chunk, const double* excl, uint6
     // u < 1, but keep the target strictly inside the mass if rounding pushed
     // it onto the total: the shot then lands on the last nonzero amplitude.
     if (!(target < total)) target = nextafter(total, 0.0);
-    uint64_t lo = 0, hi = nchunks - 1;   // largest chunk c with excl[c] <= target
-    while (lo < hi) {
-        const uint64_t mid = (lo + hi + 1) >> 1;
-        if (excl[mid] <= target) lo = mid; else hi = mid - 1;
+    // Largest chunk c with excl[c] <= target (excl is non-decreasing and
+    // excl[0] = 0).  The warp searches 32-ary: lane j probes lo + j * step,
+    // and the last lane whose prefix is <= target narrows [lo, hi) to one
+    // step: 5 dependent rounds over 2^22 chunks instead of 22 for a binary
+    // search.
+    uint64_t lo = 0, hi = nchunks;
+    while (hi - lo > 1) {
+        const uint64_t step = (hi - lo + 31) >> 5;
+        const uint64_t pj = lo + (uint64_t)lane * step;
+        const unsigned ok = __ballot_sync(0xffffffffu, pj < hi && excl[pj] <= target);
+        lo += (uint64_t)(31 - __clz(ok)) * step;    // lane 0 always qualifies
+        hi = min(hi, lo + step);
     }
     const uint64_t i0 = lo * chunk;
     const double tl = target - excl[lo];
