@@ -945,10 +945,8 @@ static size_t run_subspace_prefix(q1g_plan* p, q1g_state* s, const double* mats,
     plan_run(p->prefix_plan.get(), c, mats, n, false);
     c->ensure_dense();
     s->amps.ensure(s->N * s->bsz());
-    s->launch("subspace_scatter", double(s->N * s->bsz()), [&] {
-        cudaError_t e = cudaMemsetAsync(s->amps.p, 0, s->N * s->bsz(), s->stream);
-        if (e != cudaSuccess) return e;
-        return launch_scatter_subspace(s->amps.p, c->amps.p, s->prec, na, sp, b & ~mask, s->stream);
+    s->launch("subspace_fill", double(s->N * s->bsz()), [&] {
+        return launch_scatter_subspace(s->amps.p, c->amps.p, s->prec, nb, na, sp, b & ~mask, s->stream);
     });
     s->sparse = false;
     s->basis.clear();

@@ -164,9 +164,12 @@ struct SubspacePositions {
     int n;
     int pos[48];
 };
-// Writes the 2^nbits_compact amplitudes of `compact` into `full` at
-// deposit(c) | fixed (the caller zeroes `full` first).
-cudaError_t launch_scatter_subspace(void* full, const void* compact, int prec, int nbits_compact,
+// Writes the full state of 2^nbits_full amplitudes: the amplitudes of
+// `compact` at deposit(c) | fixed, zero elsewhere.  With at most
+// kFillMaxExcluded positions outside the subspace one pass writes every
+// amplitude; otherwise a memset and a scatter.
+constexpr int kFillMaxExcluded = 8;
+cudaError_t launch_scatter_subspace(void* full, const void* compact, int prec, int nbits_full, int nbits_compact,
                                    const SubspacePositions& sp, uint64_t fixed, cudaStream_t st);
 cudaError_t launch_product_state(void* amps, int prec, int nbits, const double* d_coefs,
                                  cudaStream_t st);

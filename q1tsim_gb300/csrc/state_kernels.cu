@@ -99,11 +99,80 @@ __global__ void k_scatter_subspace(T* full, const T* compact, uint64_t count, Su
     }
 }
 
+// Every amplitude of the full state in one coalesced pass: full[i] is
+// compact[i with the excluded positions removed] where i's excluded bits
+// equal `fixed`, zero elsewhere.  ex holds the excluded positions, highest
+// first, so that removing one leaves the lower ones in place.
+struct Excluded {
+    int n;
+    int pos[kFillMaxExcluded];
+};
+
+template <typename T>
+__device__ __forceinline__ T fill_value(const T* compact, uint64_t i, uint64_t exmask, uint64_t fixed,
+                                        const Excluded& ex)
+{
+    T v{};
+    if ((i & exmask) == fixed) {
+        uint64_t c = i;
+#pragma unroll
+        for (int k = 0; k < kFillMaxExcluded; ++k)
+            if (k < ex.n) {
+                const int p = ex.pos[k];
+                c = ((c >> (p + 1)) << p) | (c & ((uint64_t(1) << p) - 1));
+            }
+        v = compact[c];
+    }
+    return v;
+}
+
+// Four amplitudes per thread and iteration (n a multiple of 4): 32-byte
+// (complex64) or 64-byte (complex128) stores per thread.
+template <typename T>
+__global__ void k_fill_subspace(T* full, const T* compact, uint64_t n, uint64_t exmask, uint64_t fixed, Excluded ex)
+{
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    for (uint64_t q = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; q < (n >> 2); q += stride) {
+        const uint64_t i = q << 2;
+        T v[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) v[j] = fill_value(compact, i + j, exmask, fixed, ex);
+        if constexpr (sizeof(T) == 8) {
+            float4* d = reinterpret_cast<float4*>(full + i);
+            d[0] = make_float4(v[0].x, v[0].y, v[1].x, v[1].y);
+            d[1] = make_float4(v[2].x, v[2].y, v[3].x, v[3].y);
+        } else {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) full[i + j] = v[j];
+        }
+    }
+}
+
 }  // namespace
 
-cudaError_t launch_scatter_subspace(void* full, const void* compact, int prec, int nbits_compact,
+cudaError_t launch_scatter_subspace(void* full, const void* compact, int prec, int nbits_full, int nbits_compact,
                                    const SubspacePositions& sp, uint64_t fixed, cudaStream_t st)
 {
+    const uint64_t n = uint64_t(1) << nbits_full;
+    const int nex = nbits_full - nbits_compact;
+    if (nex >= 0 && nex <= kFillMaxExcluded && nbits_full >= 2) {
+        Excluded ex{};
+        uint64_t in = 0;
+        for (int k = 0; k < sp.n; ++k) in |= uint64_t(1) << sp.pos[k];
+        for (int p = nbits_full - 1; p >= 0; --p)
+            if (!((in >> p) & 1)) ex.pos[ex.n++] = p;
+        const uint64_t exmask = (n - 1) & ~in;
+        const unsigned grid = blocks_for(n >> 2, kThreads) > 152 * 32 ? 152 * 32 : blocks_for(n >> 2, kThreads);
+        if (prec == kC128)
+            k_fill_subspace<double2><<<grid, kThreads, 0, st>>>((double2*)full, (const double2*)compact, n, exmask,
+                                                               fixed & exmask, ex);
+        else
+            k_fill_subspace<float2><<<grid, kThreads, 0, st>>>((float2*)full, (const float2*)compact, n, exmask,
+                                                              fixed & exmask, ex);
+        return cudaGetLastError();
+    }
+    cudaError_t e = cudaMemsetAsync(full, 0, n * (prec == kC128 ? 16 : 8), st);
+    if (e != cudaSuccess) return e;
     const uint64_t count = uint64_t(1) << nbits_compact;
     const unsigned grid = blocks_for(count, kThreads) > 152 * 32 ? 152 * 32 : blocks_for(count, kThreads);
     if (prec == kC128)
