@@ -62,7 +62,8 @@ def test_c128_fused_equals_gate_by_gate_30_qubits():
 
 def test_norm_kept_by_32_qubit_tensor_core_plan():
     """The 32-qubit state (32 GiB) after a fused plan keeps its norm (the
-    norm check after tensor-core plans restores it to 1e-12)."""
+    norm correction after tensor-core plans, applied before the compare,
+    restores it to 1e-12)."""
     n = 32
     gates = brick(n, 4, 13)
     s = VectorState(n, 1, "c64")
