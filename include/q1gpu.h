@@ -269,6 +269,18 @@ int q1g_sample_shots_noalloc(const void* d_amps, int precision, size_t nr_bits,
                              const double* d_sorted_uniforms, size_t nshots, uint64_t* d_outcomes,
                              uint64_t* d_words, const size_t* cbits, void* cuda_stream);
 
+/* Histogram of classical words, computed on the device (replaces the count
+ * loop of Circuit::histogram, src/circuit.rs:773-789, for large shot counts):
+ * the distinct words of the host array words[0..n), in no particular order
+ * (the reference's histogram is a HashMap), with their counts, into keys[]
+ * and counts[].  *nkeys receives the number of
+ * distinct words; when it exceeds capacity the call fails with
+ * Q1G_ERR_NOT_ENOUGH_SPACE and writes nothing else.  Runs on cuda_stream
+ * (NULL: the legacy default stream) and returns when the result is on the
+ * host. */
+int q1g_histogram(const uint64_t* words, size_t n, uint64_t* keys, uint64_t* counts, size_t capacity,
+                  size_t* nkeys, void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -376,12 +376,20 @@ class Circuit:
     def cstate(self):
         return self.c_state
 
+    # from this many runs the words are counted on the GPU (q1g_histogram)
+    # rather than sorted on the host
+    DEVICE_HISTOGRAM_RUNS = 1 << 16
+
     def histogram(self):
         """src/circuit.rs:773-789: {u64 key: count}, cbit 0 = LSB."""
         if self.c_state is None:
             raise NotExecuted("Circuit has not been run yet")
-        keys, cnt = np.unique(self.c_state, return_counts=True)
-        return {int(k): int(c) for k, c in zip(keys, cnt)}
+        if len(self.c_state) >= self.DEVICE_HISTOGRAM_RUNS:
+            from .vectorstate import device_histogram
+            keys, cnt = device_histogram(self.c_state, sort=False)
+        else:
+            keys, cnt = np.unique(self.c_state, return_counts=True)
+        return dict(zip(keys.tolist(), cnt.tolist()))
 
     def histogram_vec(self):
         """src/circuit.rs:800-815"""

@@ -578,6 +578,20 @@ int q1g_sample_shots_noalloc(const void* d_amps, int precision, size_t nr_bits, 
     });
 }
 
+int q1g_histogram(const uint64_t* words, size_t n, uint64_t* keys, uint64_t* counts, size_t capacity,
+                  size_t* nkeys, void* cuda_stream)
+{
+    return guarded([&] {
+        need(nkeys, "nkeys");
+        if (n) {
+            need(words, "words");
+            need(keys, "keys");
+            need(counts, "counts");
+        }
+        histogram_words(words, n, keys, counts, capacity, nkeys, (cudaStream_t)cuda_stream);
+    });
+}
+
 int q1g_profile_enable(q1g_state* s, int enable)
 {
     return guarded([&] {

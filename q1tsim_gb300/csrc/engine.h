@@ -223,4 +223,7 @@ void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n, bool subs
 void sample_shots_noalloc(const void* d_amps, int precision, size_t nr_bits, const double* d_sorted_uniforms,
                           size_t nshots, uint64_t* d_outcomes, uint64_t* d_words, const size_t* cbits,
                           cudaStream_t st);
+// histogram.cu: distinct words in ascending order with their counts.
+void histogram_words(const uint64_t* words, size_t n, uint64_t* keys, uint64_t* counts, size_t capacity,
+                     size_t* nkeys, cudaStream_t st);
 }

@@ -362,3 +362,22 @@ def device_info():
     total = ctypes.c_size_t()
     check(L.q1g_device_info(ctypes.byref(sm), ctypes.byref(free), ctypes.byref(total)))
     return {"sm_count": sm.value, "free_bytes": free.value, "total_bytes": total.value}
+
+
+def device_histogram(words, stream=None, sort=True):
+    """Distinct values of a uint64 array and their counts, counted on the
+    GPU (q1g_histogram): the classical-word histogram of a circuit with many
+    runs.  Ascending with sort, else in the device table's order."""
+    w = np.ascontiguousarray(words, dtype=np.uint64)
+    n = len(w)
+    keys = np.empty(max(n, 1), dtype=np.uint64)
+    counts = np.empty(max(n, 1), dtype=np.uint64)
+    nk = ctypes.c_size_t(0)
+    u64 = ctypes.POINTER(ctypes.c_uint64)
+    check(_lib.load().q1g_histogram(w.ctypes.data_as(u64), n, keys.ctypes.data_as(u64), counts.ctypes.data_as(u64),
+                                    len(keys), ctypes.byref(nk), stream), "histogram")
+    keys, counts = keys[:nk.value], counts[:nk.value]
+    if sort and len(keys) > 1:
+        order = np.argsort(keys)     # distinct keys: any sort order is the same
+        keys, counts = keys[order], counts[order]
+    return keys, counts
