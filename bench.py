@@ -156,7 +156,7 @@ def cpu_baseline(n_sample, depth_sample, seed, n_full):
 
 
 def qft_leg(args):
-    """configs[1]: QFT on a random normalised 28-qubit state (re, im i.i.d.
+    """QFT on a random normalised 28-qubit state (re, im i.i.d.
     N(0,1) from the seed), complex64 fused against complex128 plain."""
     import torch
     from q1tsim_gb300 import Plan, VectorState, workloads
@@ -190,11 +190,11 @@ def qft_leg(args):
     return out
 
 
-def cfg2_leg(args):
-    """configs[2]: 32-qubit U3/CX brick, depth 24, complex64 with fused
+def brick32_leg(args):
+    """32-qubit U3/CX brick, depth 24, complex64 with fused
     5-qubit tensor-core blocks (f16 hi/lo halves), then 10^6 Z-basis shots; 1 - F and
     outcome TV against a complex128 run of the same circuit on the GPU
-    (32 GiB + 64 GiB of HBM).  Opt-in (--cfg2): the complex128 run alone
+    (32 GiB + 64 GiB of HBM).  Opt-in (--brick32): the complex128 run alone
     takes tens of seconds."""
     import torch
     from q1tsim_gb300 import Plan, Rng, VectorState
@@ -239,8 +239,8 @@ def cfg2_leg(args):
     return out
 
 
-def cfg0_leg(args):
-    """configs[0]: 16-qubit U3/CX brick, 20 layers, measure_all over 8192
+def brick16_leg(args):
+    """16-qubit U3/CX brick, 20 layers, measure_all over 8192
     runs, histogram -- on the GPU (complex128 plain and complex64 fused) and
     in full on the CPU oracle."""
     from oracle import oracle as orc
@@ -266,7 +266,7 @@ def cfg0_leg(args):
 
 
 def batch_leg(args):
-    """configs[3]: independent circuits (8-20 qubits, depth 10-40, U3/CX/CZ,
+    """Independent circuits (8-20 qubits, depth 10-40, U3/CX/CZ,
     one mid-circuit measurement + conditional X, 1024 runs each) in one
     persistent launch replayed from a CUDA graph."""
     from q1tsim_gb300 import workloads
@@ -317,7 +317,7 @@ def batch_leg(args):
 
 
 def serving_leg(args):
-    """configs[4]: a Poisson stream (mean 2000 circuits/s) of GHZ, QFT and
+    """A Poisson stream (mean 2000 circuits/s) of GHZ, QFT and
     brick circuits, 10-26 qubits, depth 5-50, 4096 shots, complex64 fused,
     admitted by HBM budget into concurrent slots."""
     from q1tsim_gb300.serving import latency_stats, mixed_requests, serve
@@ -426,9 +426,9 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-circuits leg")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving leg")
     ap.add_argument("--no-qft", action="store_true", help="skip the 28-qubit QFT accuracy leg")
-    ap.add_argument("--no-cfg0", action="store_true", help="skip the 16-qubit CPU-runnable leg")
+    ap.add_argument("--no-brick16", action="store_true", help="skip the 16-qubit CPU-runnable leg")
     ap.add_argument("--qft-qubits", type=int, default=28)
-    ap.add_argument("--cfg2", action="store_true", help="add the 32-qubit complex64 vs complex128 leg")
+    ap.add_argument("--brick32", action="store_true", help="add the 32-qubit complex64 vs complex128 leg")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -593,8 +593,8 @@ def main():
     batched = None if args.no_batch else batch_leg(args)
     serving = None if args.no_serve else serving_leg(args)
     qft = None if args.no_qft else qft_leg(args)
-    cfg0 = None if args.no_cfg0 else cfg0_leg(args)
-    cfg2 = cfg2_leg(args) if args.cfg2 else None
+    brick16 = None if args.no_brick16 else brick16_leg(args)
+    brick32 = brick32_leg(args) if args.brick32 else None
 
     if rank == 0:
         line = {
@@ -623,8 +623,8 @@ def main():
             "batched": batched,
             "serving": serving,
             "qft_random_state": qft,
-            "cpu_runnable_16q": cfg0,
-            "brick_32q": cfg2,
+            "cpu_runnable_16q": brick16,
+            "brick_32q": brick32,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:

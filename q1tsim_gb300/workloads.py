@@ -29,7 +29,7 @@ def brick(n, depth, seed, precision="c64", fusion_width=5, measure=True):
 
 def qft(n, precision="c64", fusion_width=5, measure=True):
     """Quantum Fourier transform: H, controlled phases CP(pi/2^k) = CU1, then
-    the final swaps (CP is CU1 in q1tsim)."""
+    the final swaps (q1tsim names the controlled phase CU1)."""
     c = Circuit(n, n, precision=precision, fusion_width=fusion_width)
     for j in range(n):
         c.add_gate(G.H(), [j])

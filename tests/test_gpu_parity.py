@@ -352,7 +352,7 @@ def _run_plan(n, gates, width, prec, amps, kinds=True):
 def test_qft_phase_runs_match_oracle(n):
     """The QFT with its controlled-phase ladders as phase-run passes (each
     with the next Hadamard), complex64 fused: against the complex128 oracle
-    on a random state, as configs[1] runs it."""
+    on a random state, as the 28-qubit QFT workload runs it."""
     rng = np.random.default_rng(400 + n)
     amps = rand_state(n, rng)
     q = workloads.qft(n, precision="c64", fusion_width=5, measure=False)
