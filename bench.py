@@ -334,6 +334,15 @@ def serving_leg(args):
     return st
 
 
+def workload_config(args):
+    """The headline workload, named the same way on both arms: the circuit
+    and the shots (how an arm computes it goes in further keys)."""
+    ngates = len(brick_gates(args.qubits, args.depth, args.seed))
+    return {"workload": f"random U3/CX brick circuit, {args.qubits} qubits, depth {args.depth} ({ngates} gates), "
+                        f"then {args.shots} Z shots",
+            "qubits": args.qubits, "depth": args.depth, "gates": ngates, "shots": args.shots}
+
+
 def run_reference(args, rank, world):
     """Reference arm: the reference's CPU algorithm (the oracle port: the Rust
     reference cannot be built on this image) on the host cores."""
@@ -363,8 +372,7 @@ def run_reference(args, rank, world):
     line = {"metric": METRIC, "impl": "reference", "value": rate, "unit": "gates/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": f"random U3/CX brick circuit, {args.qubits} qubits, "
-                                                        f"depth {args.depth}", "qubits": args.qubits},
+            "data": "synthetic", "config": dict(workload_config(args), computation="complex128, gate by gate"),
             "cpu_baseline": {"value": rate, "unit": "gates/s", "cores": 1, "kind": "port", "sample": sample},
             "e2e": {"value": rate, "unit": "gates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -601,10 +609,9 @@ def main():
             "metric": METRIC, "value": value, "unit": "gates/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": gate_ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"random U3/CX brick circuit, {n} qubits, depth {args.depth} "
-                                   f"({ngates} gates), complex64 fused k<={args.fusion}, then {shots} Z shots",
-                       "qubits": n, "depth": args.depth, "gates": ngates, "shots": shots,
-                       "fusion_width": args.fusion, "fused_passes": plan.nblocks,
+            "config": {**workload_config(args), "computation": f"complex64 fused k<={args.fusion}",
+                       "fusion_width": args.fusion, "fused_blocks": plan.nblocks,
+                       "tensor_core_passes": dom["launches"] if dom_name == "fused_tc_c64" else None,
                        "parallelism": f"replicas{world}", "l2": "state 8 GiB > L2, no flush needed"},
             "shots_per_s": shots_per_s, "shot_sampling_ms": shot_ms / args.steps,
             "plain_c128": plain_info, "accuracy_c64_vs_c128": accuracy,
