@@ -612,7 +612,9 @@ def main():
             "config": {**workload_config(args), "computation": f"complex64 fused k<={args.fusion}",
                        "fusion_width": args.fusion, "fused_blocks": plan.nblocks,
                        "tensor_core_passes": dom["launches"] if dom_name == "fused_tc_c64" else None,
-                       "parallelism": f"replicas{world}", "l2": "state 8 GiB > L2, no flush needed"},
+                       "parallelism": f"replicas{world}",
+                       "l2": (f"state {(8 << n) / 2 ** 30:g} GiB > L2 (129 MB), no flush needed" if (8 << n) > 129e6
+                              else "state smaller than L2")},
             "shots_per_s": shots_per_s, "shot_sampling_ms": shot_ms / args.steps,
             "plain_c128": plain_info, "accuracy_c64_vs_c128": accuracy,
             "plain_kernels": plain_kernels,
