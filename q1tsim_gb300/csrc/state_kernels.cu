@@ -126,24 +126,23 @@ __device__ __forceinline__ T fill_value(const T* compact, uint64_t i, uint64_t e
     return v;
 }
 
-// Four amplitudes per thread and iteration (n a multiple of 4): 32-byte
-// (complex64) or 64-byte (complex128) stores per thread.
+// One 16-byte unit per thread and iteration (two complex64 amplitudes or
+// one complex128), so that each store instruction of a warp writes 512
+// contiguous bytes (n even).
 template <typename T>
 __global__ void k_fill_subspace(T* full, const T* compact, uint64_t n, uint64_t exmask, uint64_t fixed, Excluded ex)
 {
+    constexpr int kPer = 16 / (int)sizeof(T);
+    const uint64_t units = n / kPer;
     const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
-    for (uint64_t q = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; q < (n >> 2); q += stride) {
-        const uint64_t i = q << 2;
-        T v[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) v[j] = fill_value(compact, i + j, exmask, fixed, ex);
-        if constexpr (sizeof(T) == 8) {
-            float4* d = reinterpret_cast<float4*>(full + i);
-            d[0] = make_float4(v[0].x, v[0].y, v[1].x, v[1].y);
-            d[1] = make_float4(v[2].x, v[2].y, v[3].x, v[3].y);
+    for (uint64_t u = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; u < units; u += stride) {
+        const uint64_t i = u * kPer;
+        if constexpr (kPer == 2) {
+            const T a = fill_value(compact, i, exmask, fixed, ex);
+            const T b = fill_value(compact, i + 1, exmask, fixed, ex);
+            reinterpret_cast<float4*>(full)[u] = make_float4(a.x, a.y, b.x, b.y);
         } else {
-#pragma unroll
-            for (int j = 0; j < 4; ++j) full[i + j] = v[j];
+            full[i] = fill_value(compact, i, exmask, fixed, ex);
         }
     }
 }
@@ -162,7 +161,8 @@ cudaError_t launch_scatter_subspace(void* full, const void* compact, int prec, i
         for (int p = nbits_full - 1; p >= 0; --p)
             if (!((in >> p) & 1)) ex.pos[ex.n++] = p;
         const uint64_t exmask = (n - 1) & ~in;
-        const unsigned grid = blocks_for(n >> 2, kThreads) > 152 * 32 ? 152 * 32 : blocks_for(n >> 2, kThreads);
+        const uint64_t units = prec == kC128 ? n : n / 2;
+        const unsigned grid = blocks_for(units, kThreads) > 152 * 32 ? 152 * 32 : blocks_for(units, kThreads);
         if (prec == kC128)
             k_fill_subspace<double2><<<grid, kThreads, 0, st>>>((double2*)full, (const double2*)compact, n, exmask,
                                                                fixed & exmask, ex);
