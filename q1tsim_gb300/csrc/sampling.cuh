@@ -6,9 +6,9 @@
 // in the reduction and in the search so the two agree: p_i = |a_i|^2 in the
 // state's precision, groups of 8 consecutive p_i summed sequentially in that
 // precision, chunks of 32 groups (256 amplitudes) summed in FP64, and an FP64
-// exclusive prefix over chunks.  A shot finds its chunk by binary search on
-// that prefix, its group by an FP64 warp scan of the chunk's 32 group sums,
-// and its amplitude by a sequential scan of the group.
+// exclusive prefix over chunks.  A shot finds its chunk by a 32-ary warp
+// search on that prefix, its group by an FP64 warp scan of the chunk's 32
+// group sums, and its amplitude by a sequential scan of the group.
 #pragma once
 
 #include <cuda_runtime.h>
