@@ -184,9 +184,9 @@ __global__ void k_normalise_spacings(const double* excl, const double* e, const 
 // in the reduction and in the search so the two agree: p_i = |a_i|^2 in the
 // state's precision, groups of 8 consecutive p_i summed sequentially in that
 // precision, chunks of 32 groups (256 amplitudes) summed in FP64, and the
-// FP64 exclusive prefix over chunks.  A shot finds its chunk by binary search
-// on that prefix, its group by an FP64 warp scan of the chunk's 32 group
-// sums, and its amplitude by a sequential scan of the group.
+// FP64 exclusive prefix over chunks.  A shot finds its chunk by a 32-ary warp
+// search on that prefix, its group by an FP64 warp scan of the chunk's 32
+// group sums, and its amplitude by a sequential scan of the group.
 
 // One warp per chunk of `chunk` (<= 256) amplitudes.
 template <typename T>
