@@ -259,12 +259,16 @@ int q1g_profile_reset(q1g_state* s);
  *
  * Scratch: a fixed device array inside the library, about 0.5 MB, holding up
  * to nr_bits = 24 (larger states are rejected with Q1G_ERR_INVALID_ARGUMENT).
- * Every GPU that loads the library keeps it until the process exits.  The
- * first call on a device looks up the array's address (cudaGetSymbolAddress);
- * make that first call before any stream capture.  All calls share the one
- * array, so calls that overlap on the GPU race; serialise them (one stream).
- * The call is asynchronous on cuda_stream (NULL: the legacy default stream)
- * and allocates no device or host memory of its own. */
+ * The first call on a device looks up the array's address
+ * (cudaGetSymbolAddress).  With CUDA's lazy module loading that lookup is what
+ * loads the array onto the device, so the first call does take device memory;
+ * every GPU keeps the array until the process exits.  Make that first call
+ * (nshots = 0 is enough) before handing device memory to a pool, and before
+ * any stream capture.  All calls share the one array and it keeps the last
+ * call's contents (every call rewrites what it reads), so calls that overlap
+ * on the GPU race; serialise them (one stream).  The call is asynchronous on
+ * cuda_stream (NULL: the legacy default stream) and calls no cudaMalloc,
+ * cudaFree or other allocating routine. */
 int q1g_sample_shots_noalloc(const void* d_amps, int precision, size_t nr_bits,
                              const double* d_sorted_uniforms, size_t nshots, uint64_t* d_outcomes,
                              uint64_t* d_words, const size_t* cbits, void* cuda_stream);

@@ -11,13 +11,16 @@
 // amplitudes, the sorted uniforms and the output arrays, all in device memory.
 // The sampler's scratch lives in one file-scope device array, g_noalloc_scratch:
 // the chunk sums, the FP64 prefix scratch and total, and the classical-bit
-// table. The array is created when the library is loaded onto a device and
-// stays until the process exits. The kernels are the same as
-// q1g_peek_all_into's (measure_kernels.cu), so for the same column and
-// uniforms the outcomes are identical.
+// table. The array belongs to this file's module. With CUDA's lazy module
+// loading, the module (and with it the array, about 0.5 MB) is loaded onto a
+// device by the first call on that device, when it looks up the array's
+// address; it then stays until the process exits. A caller that hands all
+// free device memory to its own pool makes that first call (nshots = 0 is
+// enough) beforehand. The kernels are the same as q1g_peek_all_into's
+// (measure_kernels.cu), so for the same column and uniforms the outcomes are
+// identical.
 #include <mutex>
 #include <string>
-#include <vector>
 
 #include "engine.h"
 
@@ -59,6 +62,17 @@ double* noalloc_scratch()
     return static_cast<double*>(g_noalloc_addr[dev]);
 }
 
+// The classical-bit mask of every bit position, passed to the kernel by
+// value (a kernel parameter), so that no host buffer has to outlive the call.
+struct CbitTable {
+    uint64_t mask[64];
+};
+
+__global__ void k_store_cbit_table(uint64_t* __restrict__ dst, const __grid_constant__ CbitTable t)
+{
+    if (threadIdx.x < 64) dst[threadIdx.x] = t.mask[threadIdx.x];
+}
+
 }  // namespace
 
 void sample_shots_noalloc(const void* d_amps, int precision, size_t nr_bits, const double* d_sorted_uniforms,
@@ -75,14 +89,16 @@ void sample_shots_noalloc(const void* d_amps, int precision, size_t nr_bits, con
     if (!d_amps) throw Error(Q1G_ERR_INVALID_ARGUMENT, "NULL pointer: d_amps");
     if (nshots && (!d_sorted_uniforms || !d_outcomes || !d_words))
         throw Error(Q1G_ERR_INVALID_ARGUMENT, "NULL pointer: uniforms or outputs");
-    std::vector<uint64_t> cbit_of_pos(64, 0);
+    CbitTable table{};
     for (size_t q = 0; q < nr_bits; ++q) {
         const size_t cb = cbits ? cbits[q] : q;
         if (cb >= 64) throw Error(Q1G_ERR_INVALID_CBIT, "Invalid classical bit index " + std::to_string(cb));
-        cbit_of_pos[nr_bits - 1 - q] = uint64_t(1) << cb;
+        table.mask[nr_bits - 1 - q] = uint64_t(1) << cb;
     }
-    if (nshots == 0) return;
+    // the first call on a device looks the array up (and so loads it), even
+    // with no shots to sample
     double* scratch = noalloc_scratch();
+    if (nshots == 0) return;
     const uint64_t n = uint64_t(1) << nr_bits;
     const uint64_t chunk = n < 256 ? n : 256;
     const uint64_t nchunks = n / chunk;
@@ -92,8 +108,8 @@ void sample_shots_noalloc(const void* d_amps, int precision, size_t nr_bits, con
     uint64_t* d_cpos = reinterpret_cast<uint64_t*>(scratch + kNoAllocChunkSums + 256);
     // every word of the table is rewritten, so nothing left from an earlier
     // call is read; the chunk sums, prefix and total are rewritten too
-    check_cuda(cudaMemcpyAsync(d_cpos, cbit_of_pos.data(), 64 * sizeof(uint64_t), cudaMemcpyHostToDevice, st),
-               "upload classical-bit table");
+    k_store_cbit_table<<<1, 64, 0, st>>>(d_cpos, table);
+    check_cuda(cudaGetLastError(), "store classical-bit table");
     check_cuda(launch_chunk_sums_dense(d_amps, precision, n, chunk, d_sums, st), "chunk_sums");
     check_cuda(launch_exclusive_scan(d_sums, nchunks, d_stmp, d_total, st), "prefix_scan");
     SampleArgs a{};
