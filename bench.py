@@ -135,24 +135,74 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(n_sample, depth_sample, seed, n_full):
-    """The oracle (single-threaded complex128 restatement of the reference's
-    algorithm) on the first `depth_sample` brick layers at `n_sample` qubits;
-    gates/s scaled to n_full qubits by 2^(n_sample - n_full), since every
-    gate touches all 2^n amplitudes."""
+def host_cpu():
+    """The host's CPU model and its total cores (lscpu, else platform)."""
+    import platform
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.split(":", 1)[0].strip() == "Model name":
+                model = ln.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return {"model": model or platform.processor() or platform.machine(), "total_cores": os.cpu_count(),
+            "arch": platform.machine()}
+
+
+def oracle_gate_times(n_sample, seed):
+    """Seconds per U3 and per CX of the oracle (single-threaded complex128
+    restatement of the reference's algorithm) at n_sample qubits, each the
+    mean over gates spread across the qubit positions (the reference's cost
+    depends on the position: a 1-qubit gate loops over 2^q row blocks).
+    One untimed gate touches the state first."""
     from oracle import oracle as orc
     from q1tsim_gb300 import gates as G
-    gl = brick_gates(n_sample, depth_sample, seed)
-    mats = [(G.by_name(nm, p).matrix(), b) for nm, p, b in gl]
+    rng = np.random.default_rng(seed)
     s = orc.OracleState.new(n_sample, 1)
-    t0 = time.perf_counter()
-    for m, b in mats:
-        s.apply_gate(m, b)
-    dt = time.perf_counter() - t0
-    rate = len(mats) / dt
-    return {"value": rate * 2.0 ** (n_sample - n_full), "unit": "gates/s", "cores": 1, "kind": "port",
-            "sample": f"oracle (reference algorithm, 1 thread) on {depth_sample} brick layers = {len(mats)} gates "
-                      f"at {n_sample} qubits in {dt:.2f} s ({rate:.2f} gates/s), scaled by 2^({n_sample}-{n_full})"}
+    s.apply_gate(G.H().matrix(), [0])
+    n = n_sample
+    u3 = []
+    for q in (0, n // 2, n - 1):
+        m = G.U3(*rng.uniform(0.0, 2 * math.pi, 3)).matrix()
+        t0 = time.perf_counter()
+        s.apply_gate(m, [q])
+        u3.append(time.perf_counter() - t0)
+    cx = []
+    for q in (0, n - 2):
+        t0 = time.perf_counter()
+        s.apply_gate(G.CX().matrix(), [q, q + 1])
+        cx.append(time.perf_counter() - t0)
+    return sum(u3) / len(u3), sum(cx) / len(cx), sum(u3) + sum(cx)
+
+
+def oracle_rate(n_sample, n_full, depth, seed):
+    """The oracle's gates/s on the brick circuit at n_full qubits, estimated
+    from its per-gate-type times at n_sample qubits: (U3 count x U3 time + CX
+    count x CX time) x 2^(n_full - n_sample), since every gate touches all
+    2^n amplitudes."""
+    t_u3, t_cx, spent = oracle_gate_times(n_sample, seed)
+    gl = brick_gates(n_full, depth, seed)
+    n_u3 = sum(1 for nm, _, _ in gl if nm == "U3")
+    n_cx = len(gl) - n_u3
+    t_full = (n_u3 * t_u3 + n_cx * t_cx) * 2.0 ** (n_full - n_sample)
+    return len(gl) / t_full, t_u3, t_cx, spent
+
+
+def cpu_baseline(n_sample, seed, n_full, depth, n_cached=22):
+    """The oracle on a state larger than the host's caches (n_sample
+    qubits, complex128), with the same estimate from a state that fits in
+    them (n_cached qubits) beside it."""
+    rate, t_u3, t_cx, spent = oracle_rate(n_sample, n_full, depth, seed)
+    rate_c, t_u3c, t_cxc, _ = oracle_rate(n_cached, n_full, depth, seed)
+    return {"value": rate, "unit": "gates/s", "cores": 1, "kind": "port", "host": host_cpu(),
+            "sample": f"oracle (reference algorithm, 1 thread; the reference is single-threaded) at "
+                      f"{n_sample} qubits ({(16 << n_sample) / 2 ** 30:g} GiB complex128): 3 U3 and 2 CX at "
+                      f"spread positions, {t_u3:.3f} s per U3 and {t_cx:.3f} s per CX ({spent:.1f} s), "
+                      f"weighted by the circuit's U3/CX counts and scaled by 2^({n_sample}-{n_full})",
+            "in_cache": {"qubits": n_cached, "value": rate_c, "s_per_u3": t_u3c, "s_per_cx": t_cxc,
+                         "note": f"{(16 << n_cached) / 2 ** 20:g} MiB state, within the host's caches"}}
 
 
 def qft_leg(args):
@@ -194,8 +244,7 @@ def brick32_leg(args):
     """32-qubit U3/CX brick, depth 24, complex64 with fused
     5-qubit tensor-core blocks (f16 hi/lo halves), then 10^6 Z-basis shots; 1 - F and
     outcome TV against a complex128 run of the same circuit on the GPU
-    (32 GiB + 64 GiB of HBM).  Opt-in (--brick32): the complex128 run alone
-    takes tens of seconds."""
+    (32 GiB + 64 GiB of HBM; the complex128 run alone takes about 20 s)."""
     import torch
     from q1tsim_gb300 import Plan, Rng, VectorState
     from q1tsim_gb300 import gates as G
@@ -345,35 +394,30 @@ def workload_config(args):
 
 def run_reference(args, rank, world):
     """Reference arm: the reference's CPU algorithm (the oracle port: the Rust
-    reference cannot be built on this image) on the host cores."""
+    reference cannot be built on this image) on the host cores.  Each step
+    times a bounded sample at args.cpu_qubits qubits (a state larger than the
+    host's caches) and scales it to the full circuit."""
     if rank != 0:
         return
-    from oracle import oracle as orc
-    from q1tsim_gb300 import gates as G
-    n_s, depth_s = args.cpu_qubits, 1
-    gl = brick_gates(n_s, depth_s, args.seed)
-    mats = [(G.by_name(nm, p).matrix(), b) for nm, p, b in gl]
-
-    def step():
-        s = orc.OracleState.new(n_s, 1)
-        for m, b in mats:
-            s.apply_gate(m, b)
-
+    n_s = args.cpu_qubits
     for _ in range(args.warmup):
-        step()
+        oracle_rate(n_s, args.qubits, args.depth, args.seed)
+    rates = []
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        step()
+        rates.append(oracle_rate(n_s, args.qubits, args.depth, args.seed)[0])
     dt = time.perf_counter() - t0
-    rate = args.steps * len(mats) / dt * 2.0 ** (n_s - args.qubits)
-    sample = (f"oracle (reference algorithm, 1 thread; the reference is single-threaded) per step: "
-              f"1 brick layer = {len(mats)} gates at {n_s} qubits; gates/s scaled to {args.qubits} qubits "
-              f"by 2^({n_s}-{args.qubits})")
+    rate = statistics.median(rates)
+    sample = (f"oracle (reference algorithm, 1 thread; the reference is single-threaded) per step: 3 U3 and "
+              f"2 CX at spread positions on a {n_s}-qubit complex128 state ({(16 << n_s) / 2 ** 30:g} GiB); "
+              f"gates/s of the {args.qubits}-qubit circuit from its U3/CX counts, scaled by "
+              f"2^({n_s}-{args.qubits}); median over steps")
     line = {"metric": METRIC, "impl": "reference", "value": rate, "unit": "gates/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": dict(workload_config(args), computation="complex128, gate by gate"),
-            "cpu_baseline": {"value": rate, "unit": "gates/s", "cores": 1, "kind": "port", "sample": sample},
+            "cpu_baseline": {"value": rate, "unit": "gates/s", "cores": 1, "kind": "port", "sample": sample,
+                             "host": host_cpu()},
             "e2e": {"value": rate, "unit": "gates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -428,7 +472,7 @@ def main():
     ap.add_argument("--seed", type=int, default=20240601)
     ap.add_argument("--no-plain", action="store_true", help="skip the complex128 comparison run")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
-    ap.add_argument("--cpu-qubits", type=int, default=22)
+    ap.add_argument("--cpu-qubits", type=int, default=26)
     ap.add_argument("--batch-circuits", type=int, default=4096)
     ap.add_argument("--serve-requests", type=int, default=1000)
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-circuits leg")
@@ -436,7 +480,7 @@ def main():
     ap.add_argument("--no-qft", action="store_true", help="skip the 28-qubit QFT accuracy leg")
     ap.add_argument("--no-brick16", action="store_true", help="skip the 16-qubit CPU-runnable leg")
     ap.add_argument("--qft-qubits", type=int, default=28)
-    ap.add_argument("--brick32", action="store_true", help="add the 32-qubit complex64 vs complex128 leg")
+    ap.add_argument("--no-brick32", action="store_true", help="skip the 32-qubit complex64 vs complex128 leg")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -583,6 +627,7 @@ def main():
     del fused
     circ.execute(shots, Rng(args.seed))
     barrier()
+    circ.q_state.transfer_bytes(reset=True)
     t0 = time.perf_counter()
     for k in range(args.steps):
         circ.execute(shots, Rng(args.seed + k))
@@ -591,18 +636,20 @@ def main():
     e2e_s = time.perf_counter() - t0
     e2e_ms_max, e2e_gates = world_aggregate(e2e_s * 1e3, args.steps * ngates, dist, "cuda")
     e2e_value = e2e_gates / (e2e_ms_max / 1e3)
-    h2d = plan.nblocks * 32 * 32 * 8 + n * 8
-    d2h = 2 * 8 * shots
+    # bytes the engine itself copied over the host link during the timed
+    # executions (matrices, tables, uniforms in; outcomes, words, flags out)
+    h2d_all, d2h_all = circ.q_state.transfer_bytes()
+    h2d, d2h = h2d_all // args.steps, d2h_all // args.steps
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        cpu = cpu_baseline(args.cpu_qubits, 2, args.seed, n)
+        cpu = cpu_baseline(args.cpu_qubits, args.seed, n, args.depth)
     del circ
     batched = None if args.no_batch else batch_leg(args)
     serving = None if args.no_serve else serving_leg(args)
     qft = None if args.no_qft else qft_leg(args)
     brick16 = None if args.no_brick16 else brick16_leg(args)
-    brick32 = brick32_leg(args) if args.brick32 else None
+    brick32 = None if args.no_brick32 else brick32_leg(args)
 
     if rank == 0:
         line = {

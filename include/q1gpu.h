@@ -244,6 +244,11 @@ int q1g_profile_enable(q1g_state* s, int enable);
 int q1g_profile_report(q1g_state* s, char* names, uint64_t* launches, double* ms,
                        double* bytes, size_t* n);
 int q1g_profile_reset(q1g_state* s);
+/* Bytes the state's calls copied host -> device and device -> host since it
+ * was made or last reset (reset != 0 clears the counters after reading):
+ * gate matrices, uniforms, tables and amplitudes in; outcomes, words,
+ * weights, flags and amplitudes out.  Either pointer may be NULL. */
+int q1g_state_transfer_bytes(q1g_state* s, uint64_t* h2d, uint64_t* d2h, int reset);
 
 /* ---- shot sampling that allocates nothing.  No counterpart in the
  * reference: it exists for callers that cannot call cudaMalloc, such as a

@@ -324,6 +324,9 @@ class Circuit:
     def _do_execute(self, q_state, c_state, rng):
         """src/circuit.rs:643-762"""
         H, S, Sdg = G.H().matrix(), G.S().matrix(), G.Sdg().matrix()
+        # Y basis: Sdg then H before the measurement, H then S after it
+        # (src/circuit.rs:692-703), each pair as one matrix
+        to_y, from_y = H @ Sdg, S @ H
         for idx, op in enumerate(self._segments()):
             kind = op[0]
             if kind == "seq":
@@ -343,11 +346,9 @@ class Circuit:
                     fn(qbit, cbit, c_state, rng=rng)
                     q_state.apply_gate(H, [qbit])
                 elif basis == "y":
-                    q_state.apply_gate(Sdg, [qbit])
-                    q_state.apply_gate(H, [qbit])
+                    q_state.apply_gate(to_y, [qbit])
                     fn(qbit, cbit, c_state, rng=rng)
-                    q_state.apply_gate(H, [qbit])
-                    q_state.apply_gate(S, [qbit])
+                    q_state.apply_gate(from_y, [qbit])
                 else:
                     fn(qbit, cbit, c_state, rng=rng)
             elif kind in ("measure_all", "peek_all"):
@@ -358,11 +359,9 @@ class Circuit:
                     fn(cbits, c_state, rng=rng)
                     q_state.apply_unary_gate_all(H)
                 elif basis == "y":
-                    q_state.apply_unary_gate_all(Sdg)
-                    q_state.apply_unary_gate_all(H)
+                    q_state.apply_unary_gate_all(to_y)
                     fn(cbits, c_state, rng=rng)
-                    q_state.apply_unary_gate_all(H)
-                    q_state.apply_unary_gate_all(S)
+                    q_state.apply_unary_gate_all(from_y)
                 else:
                     fn(cbits, c_state, rng=rng)
             elif kind == "reset":

@@ -101,8 +101,7 @@ int q1g_state_from_qubit_coefs(const double* coefs, size_t nr_bits, size_t nr_sh
         auto* s = new q1g_state((int)nr_bits, nr_shots, precision);
         try {
             s->dscratch.ensure(std::max<size_t>(c.size(), 1) * sizeof(double));
-            check_cuda(cudaMemcpyAsync(s->dscratch.p, c.data(), c.size() * sizeof(double),
-                                       cudaMemcpyHostToDevice, s->stream), "upload coefs");
+            s->h2d(s->dscratch.p, c.data(), c.size() * sizeof(double), "upload coefs");
             s->amps.ensure(s->N * s->bsz());
             s->launch("product_state", double(s->N * s->bsz()), [&] {
                 return launch_product_state(s->amps.p, s->prec, (int)nr_bits, s->dscratch.as<double>(), s->stream);
@@ -129,12 +128,10 @@ int q1g_state_from_amplitudes(const double* amps, size_t nr_bits, size_t nr_shot
         try {
             s->amps.ensure(s->N * s->bsz());
             if (precision == Q1G_C128) {
-                check_cuda(cudaMemcpyAsync(s->amps.p, amps, s->N * 16, cudaMemcpyHostToDevice, s->stream),
-                           "upload amplitudes");
+                s->h2d(s->amps.p, amps, s->N * 16, "upload amplitudes");
             } else {
                 s->spare.ensure(s->N * 16);
-                check_cuda(cudaMemcpyAsync(s->spare.p, amps, s->N * 16, cudaMemcpyHostToDevice, s->stream),
-                           "upload amplitudes");
+                s->h2d(s->spare.p, amps, s->N * 16, "upload amplitudes");
                 s->launch("convert", double(s->N * 24), [&] {
                     return launch_convert_c128_to_c64(s->amps.as<float2>(), s->spare.as<double2>(), s->N, s->stream);
                 });
@@ -242,9 +239,7 @@ int q1g_state_compare(q1g_state* a, q1g_state* b, double* out5)
             check_cuda(launch_compare(a->amps.p, a->prec, b->amps.p, b->prec, n, wa, wb, part.as<double>(), blocks,
                                       a->stream),
                        "compare");
-            check_cuda(cudaMemcpyAsync(h.data(), part.p, h.size() * sizeof(double), cudaMemcpyDeviceToHost,
-                                       a->stream),
-                       "download compare");
+            a->d2h(h.data(), part.p, h.size() * sizeof(double), "download compare");
             a->sync();
             for (int k = 0; k < 5; ++k) sums[k] = 0.0;
             *mx = 0.0;
@@ -281,7 +276,7 @@ int q1g_apply_unary_gate_all(q1g_state* s, const double* mat)
     return guarded([&] {
         need(s, "state");
         need(mat, "mat");
-        for (size_t b = 0; b < (size_t)s->nbits; ++b) s->apply_gate(mat, 1, &b, 1);
+        s->apply_unary_all(mat);
     });
 }
 
@@ -628,6 +623,22 @@ int q1g_profile_reset(q1g_state* s)
         need(s, "state");
         s->collect_profile();
         s->totals.clear();
+    });
+}
+
+int q1g_state_transfer_bytes(q1g_state* s, uint64_t* h2d, uint64_t* d2h, int reset)
+{
+    return guarded([&] {
+        need(s, "state");
+        // the compact state that runs a plan's leading blocks counts apart
+        uint64_t in = 0, out = 0;
+        for (q1g_state* x = s; x; x = x->compact.get()) {
+            in += x->h2d_bytes;
+            out += x->d2h_bytes;
+            if (reset) x->h2d_bytes = x->d2h_bytes = 0;
+        }
+        if (h2d) *h2d = in;
+        if (d2h) *d2h = out;
     });
 }
 

@@ -129,6 +129,7 @@ q1g_state::q1g_state(int nbits_, uint64_t nshots_, int prec_, cudaStream_t share
 q1g_state::~q1g_state()
 {
     compact.reset();   // it runs on this state's stream: free it while the stream exists
+    unary_plan.reset();
     if (stream) cudaStreamSynchronize(stream);
     for (auto& p : pending) {
         cudaEventDestroy(p.a);
@@ -164,8 +165,7 @@ void q1g_state::ensure_dense()
     if (!sparse) return;
     amps.ensure(ncols * N * bsz());
     uscratch.ensure(ncols * sizeof(uint64_t));
-    check_cuda(cudaMemcpyAsync(uscratch.p, basis.data(), ncols * sizeof(uint64_t),
-                               cudaMemcpyHostToDevice, stream), "upload basis");
+    h2d(uscratch.p, basis.data(), ncols * sizeof(uint64_t), "upload basis");
     launch("fill_basis", double(ncols * N * bsz()), [&] {
         return launch_fill_basis(amps.p, prec, ncols * N, uscratch.as<uint64_t>(), ncols, N, stream);
     });
@@ -204,8 +204,7 @@ void q1g_state::apply_op(const GateOp& op, char* base, uint64_t total_amps)
                 std::vector<unsigned char> img(dense_tiled_matrix_bytes(prec, op.t));
                 dense_tiled_matrix(prec, op.t, hm.data(), img.data());
                 matbuf.ensure(img.size());
-                check_cuda(cudaMemcpyAsync(matbuf.p, img.data(), img.size(), cudaMemcpyHostToDevice, stream),
-                           "upload matrix");
+                h2d(matbuf.p, img.data(), img.size(), "upload matrix");
                 sync();
                 launch(prec == kC128 ? "dense_tiled_c128" : "dense_tiled_c64", b2 * op.touched(total_amps), [&] {
                     return launch_dense_tiled(base, prec, total_amps, nbits, op.map, op.offs, op.t, matbuf.p,
@@ -216,13 +215,11 @@ void q1g_state::apply_op(const GateOp& op, char* base, uint64_t total_amps)
             if (prec == kC64) {
                 std::vector<float> hf(hm.begin(), hm.end());
                 matbuf.ensure(hf.size() * sizeof(float));
-                check_cuda(cudaMemcpyAsync(matbuf.p, hf.data(), hf.size() * sizeof(float),
-                                           cudaMemcpyHostToDevice, stream), "upload matrix");
+                h2d(matbuf.p, hf.data(), hf.size() * sizeof(float), "upload matrix");
                 sync();
             } else {
                 matbuf.ensure(hm.size() * sizeof(double));
-                check_cuda(cudaMemcpyAsync(matbuf.p, hm.data(), hm.size() * sizeof(double),
-                                           cudaMemcpyHostToDevice, stream), "upload matrix");
+                h2d(matbuf.p, hm.data(), hm.size() * sizeof(double), "upload matrix");
                 sync();
             }
             launch(prec == kC128 ? "dense_c128" : "dense_c64", b2 * op.touched(total_amps), [&] {
@@ -263,6 +260,37 @@ void q1g_state::apply_gate(const double* mat, size_t k, const size_t* bits, size
     if (op.kind == GateOp::Noop) return;
     ensure_dense();
     apply_op(op, amps.as<char>(), total());
+}
+
+// src/vectorstate.rs:180-189: the same one-qubit gate on every qubit.  The
+// reference makes one pass per qubit.  The gates act on different qubits, so
+// they commute and fuse into blocks of up to five qubits (complex64: one
+// tensor-core pass per block, 6 passes at 30 qubits) or three (complex128:
+// double-float warp tiles).  With FP64 arithmetic requested, the gates run
+// one by one, as the reference rounds.
+void q1g_state::apply_unary_all(const double* mat)
+{
+    using namespace q1g;
+    if (fp64_exact || nbits < 2) {
+        for (size_t b = 0; b < (size_t)nbits; ++b) apply_gate(mat, 1, &b, 1);
+        return;
+    }
+    const int width = prec == kC64 ? 5 : 3;
+    if (!unary_plan || unary_plan->nbits != nbits || unary_plan->width != width) {
+        auto p = std::make_unique<q1g_plan>();
+        p->nbits = nbits;
+        p->width = width;
+        for (int q = 0; q < nbits; ++q) {
+            p->mat_off.push_back(p->mat_doubles);
+            p->mat_doubles += 8;
+            p->gate_bits.push_back({q});
+        }
+        p->blocks = fuse(p->gate_bits, nbits, width);
+        unary_plan = std::move(p);
+    }
+    std::vector<double> mats(8 * (size_t)nbits);
+    for (int q = 0; q < nbits; ++q) std::copy(mat, mat + 8, mats.begin() + 8 * (size_t)q);
+    plan_run(unary_plan.get(), this, mats.data(), mats.size());
 }
 
 // src/qustate.rs:100-127: (column, length, apply) runs of equal control bits.
@@ -315,8 +343,7 @@ void q1g_state::apply_conditional(const uint8_t* control, size_t ncontrol, const
         for (uint64_t j = 0; j < nr; ++j) cols[j] = {ranges[j].col, -1, 1.0};
         spare.ensure(nr * N * bsz());
         colbuf.ensure(nr * sizeof(CollapseCol));
-        check_cuda(cudaMemcpyAsync(colbuf.p, cols.data(), nr * sizeof(CollapseCol),
-                                   cudaMemcpyHostToDevice, stream), "upload columns");
+        h2d(colbuf.p, cols.data(), nr * sizeof(CollapseCol), "upload columns");
         launch("column_copy", 2.0 * nr * N * bsz(), [&] {
             return launch_collapse_copy(spare.p, amps.p, prec, N, 0, colbuf.as<CollapseCol>(), nr, stream);
         });
@@ -360,8 +387,7 @@ std::vector<double> q1g_state::zero_weights(size_t qbit)
     check_cuda(launch_segment_sums(d, ncols, half / chunk, d + nchunks, d + nchunks + ncols, stream),
                "segment_sums");
     hstage.ensure(ncols * sizeof(double));
-    check_cuda(cudaMemcpyAsync(hstage.p, d + nchunks, ncols * sizeof(double), cudaMemcpyDeviceToHost, stream),
-               "download weights");
+    d2h(hstage.p, d + nchunks, ncols * sizeof(double), "download weights");
     sync();
     std::memcpy(w0.data(), hstage.p, ncols * sizeof(double));
     return w0;
@@ -426,8 +452,7 @@ void q1g_state::measure(size_t qbit, size_t cbit, uint64_t* res, size_t res_len,
     const int pos = nbits - 1 - (int)qbit;
     const bool split = new_nr != ncols;
     colbuf.ensure(new_nr * sizeof(CollapseCol));
-    check_cuda(cudaMemcpyAsync(colbuf.p, cols.data(), new_nr * sizeof(CollapseCol), cudaMemcpyHostToDevice,
-                               stream), "upload columns");
+    h2d(colbuf.p, cols.data(), new_nr * sizeof(CollapseCol), "upload columns");
     if (!split) {
         launch("collapse", 2.0 * ncols * N * bsz(), [&] {
             return launch_collapse_copy(amps.p, amps.p, prec, N, pos, colbuf.as<CollapseCol>(), new_nr, stream);
@@ -506,8 +531,7 @@ void q1g_state::measure_all(const size_t* cbits, size_t ncbits, uint64_t* res, s
         uint64_t* d_out = uscratch.as<uint64_t>();
         uint64_t* d_word = d_out + nshots;
         uint64_t* d_cpos = d_word + nshots;
-        check_cuda(cudaMemcpyAsync(d_cpos, cbit_of_pos.data(), 64 * sizeof(uint64_t), cudaMemcpyHostToDevice,
-                                   stream), "upload cbits");
+        h2d(d_cpos, cbit_of_pos.data(), 64 * sizeof(uint64_t), "upload cbits");
         launch("chunk_sums", double(ncols * N * bsz()), [&] {
             return launch_chunk_sums_dense(amps.p, prec, ncols * N, chunk, d_sums, stream);
         });
@@ -523,8 +547,7 @@ void q1g_state::measure_all(const size_t* cbits, size_t ncbits, uint64_t* res, s
                 std::sort(hu.begin() + off, hu.begin() + off + counts[c]);
                 off += counts[c];
             }
-            check_cuda(cudaMemcpyAsync(d_u, hu.data(), nshots * sizeof(double), cudaMemcpyHostToDevice, stream),
-                       "upload uniforms");
+            h2d(d_u, hu.data(), nshots * sizeof(double), "upload uniforms");
         } else {
             uint64_t off = 0;
             for (uint64_t c = 0; c < ncols; ++c) {
@@ -556,8 +579,7 @@ void q1g_state::measure_all(const size_t* cbits, size_t ncbits, uint64_t* res, s
             off += counts[c];
         }
         hstage.ensure(2 * nshots * sizeof(uint64_t));
-        check_cuda(cudaMemcpyAsync(hstage.p, d_out, 2 * nshots * sizeof(uint64_t), cudaMemcpyDeviceToHost, stream),
-                   "download outcomes");
+        d2h(hstage.p, d_out, 2 * nshots * sizeof(uint64_t), "download outcomes");
         sync();
         h_outc = hstage.as<uint64_t>();
         if (!collapse) {
@@ -632,11 +654,11 @@ void q1g_state::download(double* out, size_t len)
     }
     const uint64_t n = ncols * N;
     if (prec == kC128) {
-        check_cuda(cudaMemcpyAsync(out, amps.p, n * 16, cudaMemcpyDeviceToHost, stream), "download");
+        d2h(out, amps.p, n * 16, "download");
         sync();
     } else {
         std::vector<float> tmp(2 * n);
-        check_cuda(cudaMemcpyAsync(tmp.data(), amps.p, n * 8, cudaMemcpyDeviceToHost, stream), "download");
+        d2h(tmp.data(), amps.p, n * 8, "download");
         sync();
         for (uint64_t e = 0; e < 2 * n; ++e) out[e] = tmp[e];
     }
@@ -1040,7 +1062,7 @@ void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n, bool subs
         char* h = p->hmats.as<char>() + staged;
         char* d = p->dmats.as<char>() + staged;
         std::memcpy(h, src, sz);
-        check_cuda(cudaMemcpyAsync(d, h, sz, cudaMemcpyHostToDevice, s->stream), "upload plan matrix");
+        s->h2d(d, h, sz, "upload plan matrix");
         staged += (sz + 255) & ~size_t(255);
         return d;
     };
@@ -1152,8 +1174,7 @@ void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n, bool subs
         // the tensor-core passes' bounded waits: report an expiry now
         s->hstage.ensure(sizeof(int));
         int* h_flag = s->hstage.as<int>();
-        check_cuda(cudaMemcpyAsync(h_flag, s->errbuf.p, sizeof(int), cudaMemcpyDeviceToHost, s->stream),
-                   "read error flag");
+        s->d2h(h_flag, s->errbuf.p, sizeof(int), "read error flag");
         s->sync();
         if (*h_flag) throw Error(Q1G_ERR_TIMEOUT, "a tensor-core block kernel gave up waiting on its MMAs");
         s->norm_pending = true;
@@ -1187,8 +1208,7 @@ void q1g_state::settle_norms()
                    "segment_sums");
         s->hstage.ensure(s->ncols * sizeof(double));
         double* h_norm = s->hstage.as<double>();
-        check_cuda(cudaMemcpyAsync(h_norm, d_norm, s->ncols * sizeof(double), cudaMemcpyDeviceToHost, s->stream),
-                   "read norms");
+        s->d2h(h_norm, d_norm, s->ncols * sizeof(double), "read norms");
         s->sync();
         std::vector<double> scale(s->ncols, 1.0);
         bool any_scale = false;
@@ -1198,9 +1218,7 @@ void q1g_state::settle_norms()
         }
         if (any_scale) {
             double* d_scale = d_norm + s->ncols;
-            check_cuda(cudaMemcpyAsync(d_scale, scale.data(), s->ncols * sizeof(double), cudaMemcpyHostToDevice,
-                                       s->stream),
-                       "upload scales");
+            s->h2d(d_scale, scale.data(), s->ncols * sizeof(double), "upload scales");
             s->launch("renormalise", 2.0 * total * s->bsz(), [&] {
                 return launch_scale_columns(s->amps.p, s->prec, s->N, s->ncols, d_scale, s->stream);
             });

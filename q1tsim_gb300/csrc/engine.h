@@ -69,6 +69,8 @@ double stream_uniform_host(uint64_t seed, uint64_t counter);
 
 }  // namespace q1g
 
+struct q1g_plan;
+
 struct q1g_state {
     int nbits = 0;
     uint64_t nshots = 0;
@@ -117,12 +119,28 @@ struct q1g_state {
     // A plan's leading blocks on a basis state run on this smaller state of
     // the positions they touch (plan_run); its buffers are reused.
     std::unique_ptr<q1g_state> compact;
+    // apply_unary_gate_all: the n one-qubit gates as one fused plan (kept
+    // for the next call, which differs only in the matrix).
+    std::unique_ptr<q1g_plan> unary_plan;
 
     q1g_state(int nbits_, uint64_t nshots_, int prec_);
     q1g_state(int nbits_, uint64_t nshots_, int prec_, cudaStream_t shared);   // runs on `shared`
     ~q1g_state();
 
     size_t bsz() const { return q1g::amp_bytes(prec); }
+    // Host <-> device copies on the state's stream, counted: the bytes the
+    // state's calls moved over the host link (q1g_state_transfer_bytes).
+    uint64_t h2d_bytes = 0, d2h_bytes = 0;
+    void h2d(void* dst, const void* src, size_t n, const char* what)
+    {
+        q1g::check_cuda(cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, stream), what);
+        h2d_bytes += n;
+    }
+    void d2h(void* dst, const void* src, size_t n, const char* what)
+    {
+        q1g::check_cuda(cudaMemcpyAsync(dst, src, n, cudaMemcpyDeviceToHost, stream), what);
+        d2h_bytes += n;
+    }
     int sms = 0;
     int sm_count()
     {
@@ -158,6 +176,7 @@ struct q1g_state {
     void settle_norms();
     void apply_op(const q1g::GateOp& op, char* base, uint64_t total_amps);
     void apply_gate(const double* mat, size_t k, const size_t* bits, size_t nbits_given);
+    void apply_unary_all(const double* mat);
     void apply_conditional(const uint8_t* control, size_t ncontrol, const double* mat, size_t k,
                            const size_t* bits, size_t nbits_given);
     std::vector<double> zero_weights(size_t qbit);

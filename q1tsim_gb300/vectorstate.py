@@ -281,6 +281,14 @@ class VectorState:
             check(L.q1g_profile_reset(self._h))
         return out
 
+    def transfer_bytes(self, reset=False):
+        """(host->device, device->host) bytes copied by this state's calls
+        since it was made or last reset."""
+        h2d, d2h = ctypes.c_uint64(0), ctypes.c_uint64(0)
+        check(_lib.load().q1g_state_transfer_bytes(self._h, ctypes.byref(h2d), ctypes.byref(d2h),
+                                                   1 if reset else 0))
+        return int(h2d.value), int(d2h.value)
+
 
 class Plan:
     """A gate sequence lowered once: structure, fusion grouping, passes."""

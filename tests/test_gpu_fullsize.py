@@ -2,8 +2,9 @@
 qubits), where the oracle cannot follow: a circuit followed by its inverse
 returns to |0...0>; complex128 fused into double-float blocks equals
 gate-by-gate complex128; the norm survives a 32-qubit tensor-core plan; shots
-of a 30-qubit GHZ state land only on its two outcomes.  States are compared
-on the device (q1g_state_compare)."""
+of a 30-qubit GHZ state land only on its two outcomes; complex64 fused
+against complex128 at 28 qubits meets the 1 - F and outcome-TV targets.
+States are compared on the device (q1g_state_compare)."""
 import math
 
 import numpy as np
@@ -58,6 +59,24 @@ def test_c128_fused_equals_gate_by_gate_30_qubits():
     acc = plain.compare(fused)
     assert acc["max_abs_diff"] <= 1e-12, acc
     assert abs(acc["norm_b"] - 1.0) <= 1e-12, acc
+
+
+def test_fused_c64_accuracy_against_c128_28_qubits():
+    """The bench's brick pattern at 28 qubits, depth 24, complex64 fused into
+    5-qubit tensor-core passes against plain complex128 on the GPU: 1 - F
+    <= 1e-5 and outcome total variation <= 1e-6 (the accuracy targets of the
+    FP32-fused mode)."""
+    n = 28
+    gates = brick(n, 24, 14)
+    bits, mats = [b for _, b in gates], flat(gates)
+    plain = VectorState(n, 1, "c128")
+    plain.apply_plan(Plan(n, bits, 0), mats)
+    fused = VectorState(n, 1, "c64")
+    fused.apply_plan(Plan(n, bits, 5), mats)
+    acc = plain.compare(fused)
+    assert acc["infidelity"] <= 1e-5, acc
+    assert acc["tv"] <= 1e-6, acc
+    assert abs(acc["norm_b"] - 1.0) <= 1e-6, acc
 
 
 def test_norm_kept_by_32_qubit_tensor_core_plan():

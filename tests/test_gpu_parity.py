@@ -790,6 +790,87 @@ def test_circuit_measure_all_and_basis_kats():
     assert c.histogram_vec() == [0, n, 0, 0]
 
 
+@pytest.mark.parametrize("prec,exact,tol", [("c128", False, 1e-12), ("c128", True, 1e-13), ("c64", False, TOL64)],
+                         ids=["c128", "c128-fp64", "c64"])
+@pytest.mark.parametrize("n", [3, 11, 14])
+def test_unary_gate_all_matches_oracle(n, prec, exact, tol):
+    """apply_unary_gate_all (src/vectorstate.rs:180-189) runs the n one-qubit
+    gates as fused blocks (one pass per 5 qubits in complex64, per 3 in
+    complex128; one by one with FP64 arithmetic): the oracle's amplitudes,
+    on a multi-column state."""
+    rng = np.random.default_rng(60 + n)
+    o, g = pair(n, 16, rand_state(n, rng), prec)
+    if exact:
+        g.set_fp64_exact()
+    for m in (G.H().matrix(), G.U3(*rng.uniform(0, 2 * np.pi, 3)).matrix(), G.Sdg().matrix()):
+        o.apply_unary_gate_all(m)
+        g.apply_unary_gate_all(m)
+    so, sg = o.states(), g.states()
+    assert np.max(np.abs(so - sg)) <= tol
+
+
+@pytest.mark.parametrize("prec", ["c128", "c64"])
+@pytest.mark.parametrize("basis", ["x", "y"])
+def test_basis_change_and_shots_at_20_qubits(basis, prec):
+    """The X- and Y-basis change of measure_all / peek_all
+    (src/circuit.rs:692-703) at 20 qubits: apply_unary_gate_all with H, or
+    with H Sdg, on a random state.  Amplitudes against the oracle (1e-12 in
+    complex128; 2e-6 and 1 - F <= 1e-9 in complex64), then peek_all with the
+    same uniforms: identical words in complex128; in complex64, whose
+    rounding can move a shot across an outcome boundary, at least 99 %."""
+    n, shots = 20, 4096
+    rng = np.random.default_rng(70)
+    amps = rand_state(n, rng)
+    m = G.H().matrix() if basis == "x" else G.H().matrix() @ G.Sdg().matrix()
+    o, g = pair(n, shots, amps, prec)
+    o.apply_unary_gate_all(m)
+    g.apply_unary_gate_all(m)
+    so, sg = o.states()[:, 0], g.states()[:, 0]
+    err = float(np.max(np.abs(so - sg)))
+    infid = 1.0 - abs(np.vdot(so, sg)) ** 2 / np.vdot(sg, sg).real
+    u = np.sort(rng.random(shots))
+    want = np.zeros(shots, dtype=np.uint64)
+    got = np.zeros(shots, dtype=np.uint64)
+    o.peek_all_into(list(range(n)), want, uniforms=u)
+    g.peek_all_into(list(range(n)), got, uniforms=u)
+    same_words = float(np.mean(got == want))
+    if prec == "c128":
+        assert err <= 1e-12
+        assert same_words == 1.0
+    else:
+        assert err <= TOL64 and infid <= 1e-9, (err, infid)
+        assert same_words >= 0.99, (same_words, err, infid)
+
+
+@pytest.mark.parametrize("prec", ["c128", "c64"])
+@pytest.mark.parametrize("basis", ["x", "y"])
+def test_basis_measure_all_circuit_matches_oracle(basis, prec):
+    """X- and Y-basis measure_all through the Circuit op interpreter: the
+    basis change, the collapse onto one basis column per distinct outcome and
+    the change back (src/circuit.rs:692-703), against the oracle backend for
+    the same seed.  The oracle stores the collapsed columns densely
+    (src/vectorstate.rs:150-158), so the case stays small."""
+    n, shots = 9, 256
+    def build(p, width):
+        c = Circuit(n, n, precision=p, fusion_width=width)
+        r = np.random.default_rng(99)
+        for layer in range(3):
+            for q in range(n):
+                c.add_gate(G.U3(*r.uniform(0, 2 * np.pi, 3)), [q])
+            for q in range(layer % 2, n - 1, 2):
+                c.add_gate(G.CX(), [q, q + 1])
+        c.measure_all_basis(list(range(n)), basis)
+        c.peek_all_basis(list(range(n)), basis)
+        return c
+    c = build(prec, 5 if prec == "c64" else 3)
+    c.execute(shots, Rng(31))
+    got = c.cstate().copy()
+    ref = build("c128", 0)
+    ref.execute_with(shots, Rng(31), orc.OracleState.new(n, shots))
+    want = ref.cstate()
+    assert float(np.mean(got == want)) >= (1.0 if prec == "c128" else 0.99)
+
+
 def test_circuit_peek_all_kat():
     """src/circuit.rs:1736-1760"""
     n = 1024
@@ -972,6 +1053,30 @@ def test_fused_plan_renormalises_to_the_input_norm():
     g.apply_plan(Plan(n, [b for _, b in gl], 5), mats)
     out = g.states()[:, 0]
     assert abs(np.linalg.norm(out) ** 2 / 1.7 ** 2 - 1.0) <= 2e-6
+
+
+@pytest.mark.parametrize("n", [14, 21])
+def test_fused_plan_on_a_column_of_tiny_norm(n):
+    """A column whose squared norm is 2^-20 (as a rare branch would be
+    before renormalisation) through tensor-core passes: its amplitudes enter
+    the f16 operands scaled by 2^14 / 2^ceil(log2 sqrt(norm)), so the result
+    matches the oracle to the same relative accuracy as a unit column."""
+    rng = np.random.default_rng(23 + n)
+    scale = 2.0 ** -10
+    amps = scale * rand_state(n, rng)
+    gl = [random_gate(n, rng) for _ in range(40)]
+    mats = np.concatenate([np.ascontiguousarray(gt.matrix()).ravel() for gt, _ in gl]).view(np.float64)
+    o = orc.OracleState.from_amplitudes(amps, 1)
+    for gt, b in gl:
+        o.apply_gate(gt.matrix(), b)
+    want = o.states()[:, 0]
+    g = VectorState.from_amplitudes(amps, 1, "c64")
+    g.apply_plan(Plan(n, [b for _, b in gl], 5), mats)
+    got = g.states()[:, 0]
+    assert np.max(np.abs(got - want)) <= TOL64 * scale
+    assert abs(np.linalg.norm(got) ** 2 / scale ** 2 - 1.0) <= 2e-6
+    infid = 1.0 - abs(np.vdot(want, got)) ** 2 / (np.vdot(want, want).real * np.vdot(got, got).real)
+    assert infid <= 1e-9
 
 
 def test_compare_reports_normalised_tv():
