@@ -249,6 +249,13 @@ int q1g_profile_reset(q1g_state* s);
  * gate matrices, uniforms, tables and amplitudes in; outcomes, words,
  * weights, flags and amplitudes out.  Either pointer may be NULL. */
 int q1g_state_transfer_bytes(q1g_state* s, uint64_t* h2d, uint64_t* d2h, int reset);
+/* Longest time any wait inside a tensor-core pass of this state may last
+ * before the pass gives up: its CTAs stop, drain the copies and MMAs still
+ * in flight, release their tensor memory, and the plan fails with
+ * Q1G_ERR_TIMEOUT, leaving the amplitudes undefined (reset or rebuild the
+ * state).  seconds <= 0 restores the default, 60 s.  No counterpart in the
+ * reference, whose CPU loop has no waits. */
+int q1g_state_set_wait_limit(q1g_state* s, double seconds);
 
 /* ---- shot sampling that allocates nothing.  No counterpart in the
  * reference: it exists for callers that cannot call cudaMalloc, such as a

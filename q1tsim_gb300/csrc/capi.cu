@@ -626,6 +626,19 @@ int q1g_profile_reset(q1g_state* s)
     });
 }
 
+int q1g_state_set_wait_limit(q1g_state* s, double seconds)
+{
+    return guarded([&] {
+        need(s, "state");
+        if (!(seconds > 0.0)) {
+            s->tc_wait_ns = 0;
+        } else {
+            const double ns = seconds * 1e9;
+            s->tc_wait_ns = ns < 1.0 ? 1 : (ns > 3.6e12 ? (uint64_t)3.6e12 : (uint64_t)ns);
+        }
+    });
+}
+
 int q1g_state_transfer_bytes(q1g_state* s, uint64_t* h2d, uint64_t* d2h, int reset)
 {
     return guarded([&] {

@@ -1118,7 +1118,7 @@ void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n, bool subs
             const uint64_t total = s->total();
             s->launch("fused_tc_c64", 2.0 * total * s->bsz(), [&] {
                 return launch_fused_tc(s->amps.as<float2>(), total >> 12, t.tilemap, t.offs, t.box, img,
-                                       s->errbuf.as<int>(), s->sm_count(), s->stream);
+                                       s->errbuf.as<int>(), s->sm_count(), s->stream, s->tc_wait_ns);
             });
             if (paired) ++i;   // the next block rode in this pass
         } else if (op.kind == GateOp::Dense &&

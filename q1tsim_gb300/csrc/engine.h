@@ -76,6 +76,7 @@ struct q1g_state {
     uint64_t nshots = 0;
     int prec = q1g::kC128;
     bool fp64_exact = false;   // complex128: FP64 arithmetic instead of double-float pairs
+    uint64_t tc_wait_ns = 0;   // longest wait of a tensor-core pass (0: the kernel's default, 60 s)
     uint64_t N = 1;
     uint64_t ncols = 1;
     std::vector<uint64_t> counts;

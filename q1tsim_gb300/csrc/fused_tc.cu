@@ -43,7 +43,8 @@
 //   warps 0-3 and 4-7: two consumer groups taking alternate tiles.  Each
 //            thread owns one row t (its TMEM lane): it reads the row's 32
 //            amplitudes from the stage, writes hi/lo to its group's A columns
-//            with tcgen05.st, one thread issues the MMAs, and after the commit
+//            with tcgen05.st (the MMAs of the first half's K-steps start
+//            while the second half converts), one thread issues the MMAs, and after the commit
 //            each thread reads its row of D with tcgen05.ld and writes the
 //            new amplitudes back into the stage.  While one group waits for
 //            its MMAs the other converts or writes back, so the tensor pipe,
@@ -96,12 +97,16 @@ constexpr uint32_t kOffAbort = 212;
 constexpr uint32_t kOffRunOff = 256;    // 32 x u64
 constexpr uint32_t kOffB = 1024;
 constexpr uint32_t kAlignSlack = 1024;
-// Longest any wait may last.  Normal waits last microseconds; profiler
-// replays with instrumented instructions slow a launch by four orders of
-// magnitude or more and must not trip the limit.  A CTA that does give up
-// sets the abort flag, every other wait then returns at once, and the
-// launch ends within about this time.
-constexpr uint64_t kWaitLimitNs = 60000000000ull;
+// Longest any wait may last by default (TcOffsets::wait_ns; the caller may
+// shorten it).  Normal waits last microseconds; profiler replays with
+// instrumented instructions slow a launch by four orders of magnitude or
+// more and must not trip the limit.  A CTA that does give up sets the abort
+// flag and every other wait then returns at once.  Before the CTA exits, it
+// drains what is still in flight -- issued tile loads, MMAs already
+// committed -- each for at most kDrainLimitNs (they complete in
+// microseconds), so that no copy lands and no MMA writes after its TMEM is
+// released.
+constexpr uint64_t kDrainLimitNs = 60000000000ull;
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p)
 {
@@ -257,22 +262,63 @@ __device__ __forceinline__ uint64_t global_ns()
     return t;
 }
 
-// Bounded wait on an mbarrier phase; gives up (returns false) when the CTA's
-// abort flag is set or after kWaitLimitNs, setting the flag.
-__device__ __forceinline__ bool wait_phase(uint32_t bar, uint32_t parity, volatile int* abort_flag)
+__device__ __forceinline__ bool mbar_test_wait(uint32_t bar, uint32_t parity)
 {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Limits below this are polled with the non-blocking test_wait and the clock
+// read on every poll (try_wait may suspend the thread for a while inside one
+// poll, longer than such a limit).
+constexpr uint64_t kPromptLimitNs = 1000000ull;
+
+// Bounded wait on an mbarrier phase; gives up (returns false) when the CTA's
+// abort flag is set or after limit_ns, setting the flag.  The clock is read
+// on the first failed poll and every 256th after it.
+__device__ __forceinline__ bool wait_phase(uint32_t bar, uint32_t parity, volatile int* abort_flag,
+                                           uint64_t limit_ns)
+{
+    if (limit_ns < kPromptLimitNs) {
+        const uint64_t t0 = global_ns();
+        while (!mbar_test_wait(bar, parity)) {
+            if (*abort_flag) return false;
+            if (global_ns() - t0 > limit_ns) {
+                *abort_flag = 1;
+                return false;
+            }
+        }
+        return true;
+    }
     if (mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = global_ns();
     uint32_t polls = 0;
     while (!mbar_try_wait(bar, parity)) {
         if (*abort_flag) return false;
-        if (++polls > 64) __nanosleep(64);   // long waits leave issue slots to the warps waited for
-        if ((polls & 255u) == 0 && global_ns() - t0 > kWaitLimitNs) {
+        ++polls;
+        if (polls > 64) __nanosleep(64);   // long waits leave issue slots to the warps waited for
+        if ((polls == 1 || (polls & 255u) == 0) && global_ns() - t0 > limit_ns) {
             *abort_flag = 1;
             return false;
         }
     }
     return true;
+}
+
+// Wait for a phase regardless of the abort flag, for at most kDrainLimitNs:
+// what a CTA that gave up still has in flight.
+__device__ __forceinline__ void drain_phase(uint32_t bar, uint32_t parity)
+{
+    const uint64_t t0 = global_ns();
+    while (!mbar_try_wait(bar, parity) && global_ns() - t0 <= kDrainLimitNs) {
+    }
 }
 
 // Named barrier over one consumer group (ids 1 and 2, 128 threads).
@@ -316,63 +362,80 @@ __device__ __forceinline__ void split_amp(float2 v, float sc, uint32_t& hi, uint
     lo = pack_f16x2((re - hr) * kLoScale, (im - hm) * kLoScale);
 }
 
-// Gates 16*HH .. 16*HH+15 of row `rowb` -> f16 operands in TMEM columns
+// The 32 amplitudes of row `rowb`, all loads issued before any is used.
+__device__ __forceinline__ void load_row(const uint8_t* raw, uint32_t rowb, const TcBlockGeom& G, float2 (&x)[32])
+{
+    if (G.vec2) {
+#pragma unroll
+        for (int m = 0; m < 16; ++m) {
+            const float4 p = *(const float4*)(raw + rowb + G.gateoff[2 * m]);
+            x[2 * m] = make_float2(p.x, p.y);
+            x[2 * m + 1] = make_float2(p.z, p.w);
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) x[j] = *(const float2*)(raw + rowb + G.gateoff[j]);
+    }
+}
+
+// Gates 16*HH .. 16*HH+15 of a loaded row -> f16 operands in TMEM columns
 // 32*HH .. 32*HH+31: per K-step of 8 gates (16 f16), 8 columns of hi pairs
 // then 8 of lo pairs.  SCALE: the stage holds plain amplitudes (first block
 // of a pass), which enter times sc; later blocks find them scaled already.
 template <int HH, bool SCALE>
-__device__ __forceinline__ void split_half(const uint8_t* raw, uint32_t rowb, const TcBlockGeom& G, uint32_t tl,
-                                           float sc)
+__device__ __forceinline__ void split_store_half(const float2 (&x)[32], float sc, uint32_t tl)
 {
     uint32_t v[32];
-    if (G.vec2) {
 #pragma unroll
-        for (int m = 0; m < 8; ++m) {
-            const float4 p = *(const float4*)(raw + rowb + G.gateoff[16 * HH + 2 * m]);
-            const int j = 2 * m, c = (j >> 3) * 16 + (j & 7);
-            split_amp<SCALE>(make_float2(p.x, p.y), sc, v[c], v[c + 8]);
-            split_amp<SCALE>(make_float2(p.z, p.w), sc, v[c + 1], v[c + 9]);
-        }
-    } else {
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-            const float2 p = *(const float2*)(raw + rowb + G.gateoff[16 * HH + j]);
-            const int c = (j >> 3) * 16 + (j & 7);
-            split_amp<SCALE>(p, sc, v[c], v[c + 8]);
-        }
+    for (int j = 0; j < 16; ++j) {
+        const int c = (j >> 3) * 16 + (j & 7);
+        split_amp<SCALE>(x[16 * HH + j], sc, v[c], v[c + 8]);
     }
     tmem_st32(tl + 32u * HH, v);
 }
 
-// D_main + 2^-11 D_corr for gates 16*HH .. 16*HH+15 of row `rowb`, back
-// into the stage.  UNSCALE (last block of a pass): times `unscale`, which
-// undoes the operands' powers of two; otherwise the amplitudes stay scaled
-// for the next block (whose B is not scaled).
-template <int HH, bool UNSCALE>
-__device__ __forceinline__ void writeback_half(uint8_t* raw, uint32_t rowb, const TcBlockGeom& G, uint32_t tl,
-                                               float unscale)
+// The whole row's D_main + 2^-11 D_corr back into the stage, all four TMEM
+// loads in flight before the one wait.  UNSCALE (last block of a pass):
+// times `unscale`, which undoes the operands' powers of two; otherwise the
+// amplitudes stay scaled for the next block (whose B is not scaled).
+template <bool UNSCALE>
+__device__ __forceinline__ void writeback_row(uint8_t* raw, uint32_t rowb, const TcBlockGeom& G, uint32_t tl,
+                                              float unscale)
 {
-    uint32_t dm[32], dc[32];
-    tmem_ld32(tl + 128u + 32u * HH, dm);
-    tmem_ld32(tl + 192u + 32u * HH, dc);
+    uint32_t dm[64], dc[64];
+    tmem_ld32(tl + 128u, dm);
+    tmem_ld32(tl + 192u, dc);
+    tmem_ld32(tl + 160u, dm + 32);
+    tmem_ld32(tl + 224u, dc + 32);
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-    for (int j = 0; j < 32; ++j) {
+    for (int j = 0; j < 64; ++j) {
         const float d = __fmaf_rn(__uint_as_float(dc[j]), kLoUnscale, __uint_as_float(dm[j]));
         dm[j] = __float_as_uint(UNSCALE ? d * unscale : d);
     }
     if (G.vec2) {
 #pragma unroll
-        for (int m = 0; m < 8; ++m)
-            *(float4*)(raw + rowb + G.gateoff[16 * HH + 2 * m]) =
+        for (int m = 0; m < 16; ++m)
+            *(float4*)(raw + rowb + G.gateoff[2 * m]) =
                 make_float4(__uint_as_float(dm[4 * m]), __uint_as_float(dm[4 * m + 1]), __uint_as_float(dm[4 * m + 2]),
                             __uint_as_float(dm[4 * m + 3]));
     } else {
 #pragma unroll
-        for (int j = 0; j < 16; ++j)
-            *(float2*)(raw + rowb + G.gateoff[16 * HH + j]) =
-                make_float2(__uint_as_float(dm[2 * j]), __uint_as_float(dm[2 * j + 1]));
+        for (int j = 0; j < 32; ++j)
+            *(float2*)(raw + rowb + G.gateoff[j]) = make_float2(__uint_as_float(dm[2 * j]), __uint_as_float(dm[2 * j + 1]));
     }
+}
+
+// The MMAs of K-steps k0 and k0+1 (one half of the row's gates):
+// [D_main | D_corr] (+)= A_hi [B_hi; B_lo']^T, then D_corr += A_lo' B_hi^T.
+__device__ __forceinline__ void issue_mma_ksteps(uint32_t tm, uint32_t bb, int k0)
+{
+#pragma unroll
+    for (int ks = k0; ks < k0 + 2; ++ks)
+        mma_f16_ts(tm + 128u, tm + 16u * ks, desc_sw128(bb + (uint32_t)ks * 32u), kIdescN128, ks > 0 ? 1u : 0u);
+#pragma unroll
+    for (int ks = k0; ks < k0 + 2; ++ks)
+        mma_f16_ts(tm + 192u, tm + 16u * ks + 8u, desc_sw128(bb + (uint32_t)ks * 32u), kIdescN64, 1u);
 }
 
 __global__ void __launch_bounds__(kTcThreads, 1)
@@ -430,7 +493,7 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, const __grid_constant__ Inde
         uint64_t issued = 0;
         for (uint64_t i = 0; i < my_tiles; ++i) {
             // use u of stage s waits until the store of use u-1 has read it
-            if (u > 0 && !wait_phase(sbase + kOffEmpty + 8 * s, (u - 1) & 1u, abort_flag)) break;
+            if (u > 0 && !wait_phase(sbase + kOffEmpty + 8 * s, (u - 1) & 1u, abort_flag, offs.wait_ns)) break;
             const uint64_t tile = blockIdx.x + i * gridDim.x;
             const uint32_t full = sbase + kOffFull + 8 * s;
             const uint32_t st = sbase + raw0 + s * sbytes;
@@ -461,12 +524,8 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, const __grid_constant__ Inde
         // every load issued has landed before the CTA can exit (the
         // consumers waited for all of them unless the CTA gave up)
         const uint64_t from = issued > nst ? issued - nst : 0;
-        const uint64_t t0 = global_ns();
-        for (uint64_t i = from; i < issued; ++i) {
-            while (!mbar_try_wait(sbase + kOffFull + 8 * (uint32_t)(i % nst), (uint32_t)((i / nst) & 1)) &&
-                   global_ns() - t0 <= kWaitLimitNs) {
-            }
-        }
+        for (uint64_t i = from; i < issued; ++i)
+            drain_phase(sbase + kOffFull + 8 * (uint32_t)(i % nst), (uint32_t)((i / nst) & 1));
     } else if (warp >= kStorerWarp0) {
         // --------------------------------------------------------- storers
         // storer w takes tiles w, w+2, ...; after its store has read the
@@ -474,7 +533,7 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, const __grid_constant__ Inde
         const uint32_t w = (uint32_t)(warp - kStorerWarp0);
         uint32_t s = w, u = 0;
         for (uint64_t i = w; i < my_tiles; i += 2) {
-            if (!wait_phase(sbase + kOffOut + 8 * s, u & 1u, abort_flag)) break;
+            if (!wait_phase(sbase + kOffOut + 8 * s, u & 1u, abort_flag, offs.wait_ns)) break;
             const uint64_t tile = blockIdx.x + i * gridDim.x;
             const uint32_t st = sbase + raw0 + s * sbytes;
             if (offs.use_tma) {
@@ -521,7 +580,7 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, const __grid_constant__ Inde
             }
         uint32_t s = g, u = 0, mph = 0;     // tile i lives in stage i % nst
         for (uint64_t i = g; i < my_tiles; i += 2) {
-            if (group_any(!wait_phase(sbase + kOffFull + 8 * s, u & 1u, abort_flag), gbar)) break;
+            if (group_any(!wait_phase(sbase + kOffFull + 8 * s, u & 1u, abort_flag, offs.wait_ns), gbar)) break;
             uint8_t* raw = smem + raw0 + s * sbytes;
             bool stop = false;
 #pragma unroll
@@ -530,44 +589,43 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, const __grid_constant__ Inde
                 const TcBlockGeom& G = offs.blk[b];
                 const uint32_t rowb = b ? rowb1 : rowb0;
                 if (b > 0) group_sync(gbar);    // the previous block's results are all staged
-                // row t -> hi/lo operands, columns 2g+c, in TMEM
-                if (b == 0) {
-                    split_half<0, true>(raw, rowb, G, tl, offs.ascale);
-                    split_half<1, true>(raw, rowb, G, tl, offs.ascale);
-                } else {
-                    split_half<0, false>(raw, rowb, G, tl, offs.ascale);
-                    split_half<1, false>(raw, rowb, G, tl, offs.ascale);
-                }
+                const uint32_t bb = sbase + kOffB + (uint32_t)b * kBImage;
+                // row t -> hi/lo operands in TMEM: every load of the row is
+                // issued first; after the first half is stored, its two
+                // K-steps' MMAs run while the second half converts
+                float2 x[32];
+                load_row(raw, rowb, G, x);
+                if (b == 0) split_store_half<0, true>(x, offs.ascale, tl);
+                else split_store_half<0, false>(x, offs.ascale, tl);
                 asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
                 asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
                 group_sync(gbar);
                 if (issuer) {
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                    const uint32_t bb = sbase + kOffB + (uint32_t)b * kBImage;
-                    // [D_main | D_corr] = A_hi [B_hi; B_lo']^T, then D_corr += A_lo' B_hi^T;
-                    // K-step ks (16 f16) starts 32 B into each 128 B row
-#pragma unroll
-                    for (int ks = 0; ks < 4; ++ks)
-                        mma_f16_ts(tm + 128u, tm + 16u * ks, desc_sw128(bb + (uint32_t)ks * 32u), kIdescN128,
-                                   ks > 0 ? 1u : 0u);
-#pragma unroll
-                    for (int ks = 0; ks < 4; ++ks)
-                        mma_f16_ts(tm + 192u, tm + 16u * ks + 8u, desc_sw128(bb + (uint32_t)ks * 32u), kIdescN64, 1u);
+                    issue_mma_ksteps(tm, bb, 0);
+                }
+                if (b == 0) split_store_half<1, true>(x, offs.ascale, tl);
+                else split_store_half<1, false>(x, offs.ascale, tl);
+                asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                group_sync(gbar);
+                if (issuer) {
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    issue_mma_ksteps(tm, bb, 2);
                     mma_commit(mbar);
                 }
-                if (group_any(!wait_phase(mbar, mph & 1u, abort_flag), gbar)) {
+                if (group_any(!wait_phase(mbar, mph & 1u, abort_flag, offs.wait_ns), gbar)) {
+                    // the MMAs were committed (every thread of the group is
+                    // past the issuer's commit): let them finish before the
+                    // CTA releases its TMEM
+                    drain_phase(mbar, mph & 1u);
                     stop = true;
                     break;
                 }
                 ++mph;
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                if ((uint32_t)b + 1 == nblocks) {
-                    writeback_half<0, true>(raw, rowb, G, tl, offs.unscale);
-                    writeback_half<1, true>(raw, rowb, G, tl, offs.unscale);
-                } else {
-                    writeback_half<0, false>(raw, rowb, G, tl, offs.unscale);
-                    writeback_half<1, false>(raw, rowb, G, tl, offs.unscale);
-                }
+                if ((uint32_t)b + 1 == nblocks) writeback_row<true>(raw, rowb, G, tl, offs.unscale);
+                else writeback_row<false>(raw, rowb, G, tl, offs.unscale);
                 asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             }
             if (stop) break;
@@ -860,7 +918,7 @@ EncodeTiledFn encode_tiled()
 
 cudaError_t launch_fused_tc(float2* amps, uint64_t ntiles, const IndexMap& tilemap, const TcOffsets& offs_in,
                             const TcTileBox& box, const void* d_bimage, int* d_err, int sm_count,
-                            cudaStream_t st)
+                            cudaStream_t st, uint64_t wait_ns)
 {
     static std::mutex mu;
     static int optin[64] = {0};
@@ -880,6 +938,7 @@ cudaError_t launch_fused_tc(float2* amps, uint64_t ntiles, const IndexMap& tilem
         }
     }
     TcOffsets offs = offs_in;
+    offs.wait_ns = wait_ns ? wait_ns : kTcDefaultWaitNs;
     const uint32_t fixed = kAlignSlack + kOffB + offs.nblocks * kBImage;
     if (offs.nblocks < 1 || offs.nblocks > 2 || offs.stage_bytes < kTileBytes ||
         (uint32_t)optin[dev] < fixed + 3 * offs.stage_bytes)

@@ -114,6 +114,7 @@ struct TcOffsets {
     float ascale;
     float unscale;
     uint32_t pad1_;
+    uint64_t wait_ns;        // longest any wait may last (set by launch_fused_tc)
     uint64_t run_off[32];
     TcBlockGeom blk[2];
 };
@@ -138,11 +139,13 @@ TcTileBox tc_tile_box(const int* tile_pos /* 12, ascending */, int nbits, uint64
 void tc_choose_padding(TcOffsets& offs, bool tma_ok);
 // d_bimage: nblocks consecutive 16 KB f16 hi/lo images of the blocks' real
 // 64x64 embeddings in the kernel's swizzled layout; d_err: set to 1 if a
-// bounded wait expired.
+// bounded wait expired.  wait_ns: longest any of the kernel's waits may
+// last before it gives up (0: the default, 60 s).
 // box: the tile as a tensor-map box (used for unpadded passes when usable).
+constexpr uint64_t kTcDefaultWaitNs = 60000000000ull;
 cudaError_t launch_fused_tc(float2* amps, uint64_t ntiles, const IndexMap& tilemap, const TcOffsets& offs,
                             const TcTileBox& box, const void* d_bimage, int* d_err, int sm_count,
-                            cudaStream_t st);
+                            cudaStream_t st, uint64_t wait_ns = 0);
 // Host: the 16 KB image (8192 f16) for the 32x32 complex matrix m
 // (row-major (re, im)), entries times 2^scale_log2: kTcLastBScaleLog2 for
 // the last block of a pass, 0 for the one before (whose output stays scaled).

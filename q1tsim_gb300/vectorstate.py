@@ -281,6 +281,11 @@ class VectorState:
             check(L.q1g_profile_reset(self._h))
         return out
 
+    def set_wait_limit(self, seconds=0.0):
+        """Longest wait inside a tensor-core pass before the pass gives up
+        with DeviceTimeout (amplitudes then undefined); 0 = default (60 s)."""
+        check(_lib.load().q1g_state_set_wait_limit(self._h, float(seconds)))
+
     def transfer_bytes(self, reset=False):
         """(host->device, device->host) bytes copied by this state's calls
         since it was made or last reset."""

@@ -1079,6 +1079,42 @@ def test_fused_plan_on_a_column_of_tiny_norm(n):
     assert infid <= 1e-9
 
 
+def test_tensor_core_wait_limit_expires_then_state_recovers():
+    """Tensor-core passes whose waits may last at most 1 ns give up: every
+    CTA stops, drains the tile copies and MMAs it still has in flight,
+    releases its tensor memory and reports the expiry, so the plan fails with
+    DeviceTimeout (the error path of a wait that ran out, taken without any
+    fault).  With the default limit restored, the same handle, reset, runs the
+    plan again and matches the oracle -- the expired passes left no TMEM
+    allocated and nothing in flight -- and so does a new state."""
+    rng = np.random.default_rng(90)
+    n = 16
+    gl = [random_gate(n, rng) for _ in range(60)]
+    bits = [b for _, b in gl]
+    mats = np.concatenate([np.ascontiguousarray(gt.matrix()).ravel() for gt, _ in gl]).view(np.float64)
+    plan = Plan(n, bits, 5)
+    g = VectorState.from_amplitudes(rand_state(n, rng), 1, "c64")
+    g.set_wait_limit(1e-9)
+    g.profile(True)
+    with pytest.raises(_lib.DeviceTimeout):
+        g.apply_plan(plan, mats)
+    assert g.profile_report(reset=True)["fused_tc_c64"]["launches"] > 0
+    g.profile(False)
+    g.set_wait_limit(0)
+    o = orc.OracleState.new(n, 1)
+    for gt, b in gl:
+        o.apply_gate(gt.matrix(), b)
+    want = o.states()[:, 0]
+    g.reset_all()
+    g.apply_plan(plan, mats)
+    fresh = VectorState(n, 1, "c64")
+    fresh.apply_plan(plan, mats)
+    for st in (g, fresh):
+        got = st.states()[:, 0]
+        assert np.max(np.abs(got - want)) <= TOL64
+        assert 1 - abs(np.vdot(want, got)) ** 2 <= 1e-6
+
+
 def test_compare_reports_normalised_tv():
     rng = np.random.default_rng(2)
     n = 12
