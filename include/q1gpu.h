@@ -54,7 +54,9 @@ enum q1g_status {
 
 /* Amplitude precision of a state. */
 enum q1g_precision {
-    Q1G_C128 = 0, /* complex128 amplitudes, FP64 arithmetic: the drop-in mode */
+    Q1G_C128 = 0, /* complex128 amplitudes, the drop-in mode: double-float arithmetic
+                     (pairs of FP32, a quarter of the warps on the FP64 pipe) within
+                     1e-12 by default, FP64 with q1g_state_set_fp64_exact */
     Q1G_C64 = 1   /* complex64 amplitudes, FP32 arithmetic, fused blocks on tensor cores */
 };
 
@@ -71,6 +73,15 @@ typedef struct q1g_rng {
 
 /* Message of the calling thread's last failed call ("" if none). */
 const char* q1g_last_error(void);
+/* Payload of the calling thread's last failed call, as the reference's
+ * error variant carries it (src/error.rs:135-152), so that a binding can
+ * rebuild the Error by value: InvalidNrBits(a0 = bits given, a1 = bits of
+ * the gate), InvalidQBit(a0), InvalidCBit(a0), InvalidNrControlBits(a0 =
+ * control bits given, a1 = runs), InvalidNrMeasurementBits(a0 = classical
+ * bits given, a1 = qubits), NotEnoughSpace(a0 = result length, a1 = runs)
+ * (src/vectorstate.rs:112-116, 172, 199, 242-246).  0 where the variant has
+ * no payload.  Either pointer may be NULL. */
+void q1g_last_error_args(uint64_t* a0, uint64_t* a1);
 /* Library version (major*10000 + minor*100 + patch). */
 int q1g_version(void);
 /* Visible device: SM count and memory.  Any pointer may be NULL. */

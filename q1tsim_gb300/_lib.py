@@ -34,12 +34,16 @@ _rngp = ctypes.POINTER(q1g_rng)
 # Status codes 1..7 mirror crate::error::Error (src/error.rs:135-152).
 
 class Q1Error(Exception):
+    """payload: the reference error variant's values, e.g. (q,) for
+    InvalidQBit(q) or (len, runs) for NotEnoughSpace(len, runs)."""
     code = -1
+    payload = ()
 
-    def __init__(self, msg, code=None):
+    def __init__(self, msg, code=None, payload=()):
         super().__init__(msg)
         if code is not None:
             self.code = code
+        self.payload = tuple(payload)
 
 
 class InvalidNrBits(Q1Error):
@@ -110,6 +114,7 @@ def load():
             "(python -c 'import __graft_entry__ as g; g.build()')")
     L = ctypes.CDLL(LIB_PATH)
     _proto(L, "q1g_last_error", ctypes.c_char_p, [])
+    _proto(L, "q1g_last_error_args", None, [_u64p, _u64p])
     _proto(L, "q1g_version", _int, [])
     _proto(L, "q1g_device_info", _int, [ctypes.POINTER(_int), _szp, _szp])
     _proto(L, "q1g_state_new", _int, [_sz, _sz, _int, ctypes.POINTER(_vp)])
@@ -151,11 +156,19 @@ def load():
     return L
 
 
+# how many payload values each variant carries (src/error.rs:135-152)
+_PAYLOAD_LEN = {1: 2, 2: 1, 3: 1, 4: 2, 5: 2, 6: 2}
+
+
 def check(rc, what=""):
     if rc != 0:
-        msg = load().q1g_last_error().decode("utf-8", "replace")
+        L = load()
+        msg = L.q1g_last_error().decode("utf-8", "replace")
+        a0, a1 = ctypes.c_uint64(0), ctypes.c_uint64(0)
+        L.q1g_last_error_args(ctypes.byref(a0), ctypes.byref(a1))
+        payload = (int(a0.value), int(a1.value))[:_PAYLOAD_LEN.get(rc, 0)]
         cls = _BY_CODE.get(rc, Q1Error)
-        raise cls(f"{what}: {msg}" if what else msg, rc)
+        raise cls(f"{what}: {msg}" if what else msg, rc, payload)
 
 
 def declared_symbols(header=HEADER):

@@ -14,6 +14,7 @@ namespace q1g {
 
 namespace {
 thread_local std::string g_last_error;
+thread_local uint64_t g_last_args[2] = {0, 0};
 
 template <class F>
 int guarded(F f)
@@ -23,14 +24,19 @@ int guarded(F f)
         return Q1G_OK;
     } catch (const Error& e) {
         g_last_error = e.msg;
+        g_last_args[0] = e.a0;
+        g_last_args[1] = e.a1;
         return e.code;
     } catch (const std::bad_alloc&) {
+        g_last_args[0] = g_last_args[1] = 0;
         g_last_error = "host allocation failed";
         return Q1G_ERR_OUT_OF_MEMORY;
     } catch (const std::exception& e) {
+        g_last_args[0] = g_last_args[1] = 0;
         g_last_error = e.what();
         return Q1G_ERR_INVALID_ARGUMENT;
     } catch (...) {
+        g_last_args[0] = g_last_args[1] = 0;
         g_last_error = "unknown error";
         return Q1G_ERR_INVALID_ARGUMENT;
     }
@@ -59,6 +65,12 @@ using namespace q1g;
 extern "C" {
 
 const char* q1g_last_error(void) { return g_last_error.c_str(); }
+
+void q1g_last_error_args(uint64_t* a0, uint64_t* a1)
+{
+    if (a0) *a0 = g_last_args[0];
+    if (a1) *a1 = g_last_args[1];
+}
 
 int q1g_version(void) { return 100; }
 
@@ -375,7 +387,8 @@ int q1g_plan_create(size_t nr_bits, size_t ngates, const size_t* ks, const size_
             for (size_t j = 0; j < ks[g]; ++j) {
                 if (bits_flat[bo + j] >= nr_bits) {
                     delete p;
-                    throw Error(Q1G_ERR_INVALID_QBIT, "Invalid qubit index " + std::to_string(bits_flat[bo + j]));
+                    throw Error(Q1G_ERR_INVALID_QBIT, "Invalid qubit index " + std::to_string(bits_flat[bo + j]),
+                                bits_flat[bo + j]);
                 }
                 b[j] = (int)bits_flat[bo + j];
             }

@@ -233,10 +233,12 @@ void q1g_state::apply_op(const GateOp& op, char* base, uint64_t total_amps)
 static void check_gate_bits(int nbits, size_t k, const size_t* bits, size_t nbits_given)
 {
     if (nbits_given != k)
-        throw Error(Q1G_ERR_INVALID_NR_BITS, "Expected " + std::to_string(k) + " bits for the gate, got " +
-                                                 std::to_string(nbits_given));
+        throw Error(Q1G_ERR_INVALID_NR_BITS,
+                    "Expected " + std::to_string(k) + " bits for the gate, got " + std::to_string(nbits_given),
+                    nbits_given, k);
     for (size_t m = 0; m < nbits_given; ++m)
-        if (bits[m] >= (size_t)nbits) throw Error(Q1G_ERR_INVALID_QBIT, "Invalid qubit index " + std::to_string(bits[m]));
+        if (bits[m] >= (size_t)nbits)
+            throw Error(Q1G_ERR_INVALID_QBIT, "Invalid qubit index " + std::to_string(bits[m]), bits[m]);
     for (size_t m = 0; m < nbits_given; ++m)
         for (size_t j = m + 1; j < nbits_given; ++j)
             if (bits[m] == bits[j])
@@ -328,8 +330,9 @@ void q1g_state::apply_conditional(const uint8_t* control, size_t ncontrol, const
 {
     settle_norms();
     if (ncontrol != nshots)
-        throw Error(Q1G_ERR_INVALID_NR_CONTROL_BITS, "Expected " + std::to_string(nshots) +
-                                                         " control bits, got " + std::to_string(ncontrol));
+        throw Error(Q1G_ERR_INVALID_NR_CONTROL_BITS,
+                    "Expected " + std::to_string(nshots) + " control bits, got " + std::to_string(ncontrol), ncontrol,
+                    nshots);
     check_gate_bits(nbits, k, bits, nbits_given);
     const GateOp op = classify_host(mat, k, bits, nbits);
     const auto ranges = conditional_ranges(counts, control);
@@ -396,12 +399,14 @@ std::vector<double> q1g_state::zero_weights(size_t qbit)
 void q1g_state::measure(size_t qbit, size_t cbit, uint64_t* res, size_t res_len,
                         const double* uniforms, size_t nu, q1g_rng* rng, bool collapse)
 {
-    if (qbit >= (size_t)nbits) throw Error(Q1G_ERR_INVALID_QBIT, "Invalid qubit index " + std::to_string(qbit));
+    if (qbit >= (size_t)nbits) throw Error(Q1G_ERR_INVALID_QBIT, "Invalid qubit index " + std::to_string(qbit), qbit);
     settle_norms();     // P(0) is the half's weight against the column's norm
     if (res_len < nshots)
-        throw Error(Q1G_ERR_NOT_ENOUGH_SPACE, "Unable to store " + std::to_string(nshots) +
-                                                  " measurements in array of size " + std::to_string(res_len));
-    if (cbit >= 64) throw Error(Q1G_ERR_INVALID_CBIT, "Invalid classical bit index " + std::to_string(cbit));
+        throw Error(Q1G_ERR_NOT_ENOUGH_SPACE,
+                    "Unable to store " + std::to_string(nshots) + " measurements in array of size " +
+                        std::to_string(res_len),
+                    res_len, nshots);
+    if (cbit >= 64) throw Error(Q1G_ERR_INVALID_CBIT, "Invalid classical bit index " + std::to_string(cbit), cbit);
     if (uniforms ? nu < ncols : rng == nullptr)
         throw Error(Q1G_ERR_INVALID_ARGUMENT, "need one uniform per state column or an rng");
     std::vector<double> us(ncols);
@@ -476,13 +481,17 @@ void q1g_state::measure_all(const size_t* cbits, size_t ncbits, uint64_t* res, s
                             const double* uniforms, size_t nu, q1g_rng* rng, bool collapse)
 {
     if (res_len < nshots)
-        throw Error(Q1G_ERR_NOT_ENOUGH_SPACE, "Unable to store " + std::to_string(nshots) +
-                                                  " measurements in array of size " + std::to_string(res_len));
+        throw Error(Q1G_ERR_NOT_ENOUGH_SPACE,
+                    "Unable to store " + std::to_string(nshots) + " measurements in array of size " +
+                        std::to_string(res_len),
+                    res_len, nshots);
     if (ncbits != (size_t)nbits)
-        throw Error(Q1G_ERR_INVALID_NR_MEASUREMENT_BITS, "Expected " + std::to_string(nbits) +
-                                                             " measurement bits, got " + std::to_string(ncbits));
+        throw Error(Q1G_ERR_INVALID_NR_MEASUREMENT_BITS,
+                    "Expected " + std::to_string(nbits) + " measurement bits, got " + std::to_string(ncbits), ncbits,
+                    nbits);
     for (size_t q = 0; q < ncbits; ++q)
-        if (cbits[q] >= 64) throw Error(Q1G_ERR_INVALID_CBIT, "Invalid classical bit index " + std::to_string(cbits[q]));
+        if (cbits[q] >= 64)
+            throw Error(Q1G_ERR_INVALID_CBIT, "Invalid classical bit index " + std::to_string(cbits[q]), cbits[q]);
     if (uniforms ? nu < nshots : rng == nullptr)
         throw Error(Q1G_ERR_INVALID_ARGUMENT, "need one uniform per run or an rng");
     uint64_t mask = 0;

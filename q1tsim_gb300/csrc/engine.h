@@ -20,7 +20,11 @@ namespace q1g {
 struct Error : std::exception {
     int code;
     std::string msg;
+    // The payload of the reference's error variant (src/error.rs:135-152),
+    // e.g. InvalidQBit(a0), NotEnoughSpace(a0, a1); 0 where it has none.
+    uint64_t a0 = 0, a1 = 0;
     Error(int c, std::string m) : code(c), msg(std::move(m)) {}
+    Error(int c, std::string m, uint64_t x0, uint64_t x1 = 0) : code(c), msg(std::move(m)), a0(x0), a1(x1) {}
     const char* what() const noexcept override { return msg.c_str(); }
 };
 

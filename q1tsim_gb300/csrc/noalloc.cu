@@ -92,7 +92,7 @@ void sample_shots_noalloc(const void* d_amps, int precision, size_t nr_bits, con
     CbitTable table{};
     for (size_t q = 0; q < nr_bits; ++q) {
         const size_t cb = cbits ? cbits[q] : q;
-        if (cb >= 64) throw Error(Q1G_ERR_INVALID_CBIT, "Invalid classical bit index " + std::to_string(cb));
+        if (cb >= 64) throw Error(Q1G_ERR_INVALID_CBIT, "Invalid classical bit index " + std::to_string(cb), cb);
         table.mask[nr_bits - 1 - q] = uint64_t(1) << cb;
     }
     // the first call on a device looks the array up (and so loads it), even

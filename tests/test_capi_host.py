@@ -36,10 +36,15 @@ def test_null_arguments_are_errors_not_crashes(lib):
     h = ctypes.c_void_p()
     assert lib.q1g_state_new(3, 1, 7, ctypes.byref(h)) == _lib.InvalidArgument.code
     assert lib.q1g_plan_create(4, 1, None, None, 0, ctypes.byref(h)) == _lib.InvalidArgument.code
-    with pytest.raises(_lib.InvalidQBit):
+    with pytest.raises(_lib.InvalidQBit) as ei:
         Plan(3, [[0, 5]])
-    with pytest.raises(_lib.InvalidArgument):
+    assert ei.value.payload == (5,)        # Error::InvalidQBit(5)
+    a0, a1 = ctypes.c_uint64(9), ctypes.c_uint64(9)
+    lib.q1g_last_error_args(ctypes.byref(a0), ctypes.byref(a1))
+    assert (a0.value, a1.value) == (5, 0)
+    with pytest.raises(_lib.InvalidArgument) as ei:
         Plan(3, [[0]], fusion_width=7)
+    assert ei.value.payload == ()
 
 
 def _commutes_ok(gate_bits, blocks):

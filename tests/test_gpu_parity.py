@@ -948,19 +948,25 @@ def test_circuit_gpu_equals_oracle_backend():
 # --------------------------------------------------------------- errors
 
 def test_error_codes_on_gpu():
+    """Status codes and payloads of the reference's Error variants
+    (src/vectorstate.rs:112-116, 172, 199, 242-246), so that a binding can
+    rebuild e.g. Error::NotEnoughSpace(2, 4) by value."""
     s = VectorState(3, 4)
-    with pytest.raises(_lib.InvalidNrBits):
-        s.apply_gate(G.CX(), [0])
-    with pytest.raises(_lib.InvalidQBit):
-        s.apply_gate(G.H(), [3])
-    with pytest.raises(_lib.NotEnoughSpace):
-        s.measure_into(0, 0, np.zeros(2, dtype=np.uint64), Rng(0))
-    with pytest.raises(_lib.InvalidNrMeasurementBits):
-        s.measure_all_into([0, 1], np.zeros(4, dtype=np.uint64), Rng(0))
-    with pytest.raises(_lib.InvalidNrControlBits):
-        s.apply_conditional_gate([1, 0, 1], G.X(), [0])
-    with pytest.raises(_lib.InvalidQBit):
-        s.measure_into(5, 0, np.zeros(4, dtype=np.uint64), Rng(0))
+    cases = [
+        (_lib.InvalidNrBits, (1, 2), lambda: s.apply_gate(G.CX(), [0])),
+        (_lib.InvalidQBit, (3,), lambda: s.apply_gate(G.H(), [3])),
+        (_lib.NotEnoughSpace, (2, 4), lambda: s.measure_into(0, 0, np.zeros(2, dtype=np.uint64), Rng(0))),
+        (_lib.NotEnoughSpace, (3, 4), lambda: s.peek_all_into([0, 1, 2], np.zeros(3, dtype=np.uint64), Rng(0))),
+        (_lib.InvalidNrMeasurementBits, (2, 3),
+         lambda: s.measure_all_into([0, 1], np.zeros(4, dtype=np.uint64), Rng(0))),
+        (_lib.InvalidNrControlBits, (3, 4), lambda: s.apply_conditional_gate([1, 0, 1], G.X(), [0])),
+        (_lib.InvalidQBit, (5,), lambda: s.measure_into(5, 0, np.zeros(4, dtype=np.uint64), Rng(0))),
+        (_lib.InvalidCBit, (70,), lambda: s.measure_into(0, 70, np.zeros(4, dtype=np.uint64), Rng(0))),
+    ]
+    for cls, payload, call in cases:
+        with pytest.raises(cls) as ei:
+            call()
+        assert ei.value.payload == payload, (cls, ei.value.payload)
 
 
 def test_autotuned_circuit_matches_oracle():
