@@ -109,6 +109,14 @@ int q1g_state_set_stream(q1g_state* s, void* cuda_stream);
  * 1 = FP64 (the reference's own rounding, src/gates.rs:121-152).  No
  * reference counterpart. */
 int q1g_state_set_fp64_exact(q1g_state* s, int exact);
+/* Replaces every column by a random unit vector drawn on the device: the
+ * real and imaginary parts of each amplitude i.i.d. N(0,1) (Box-Muller on
+ * the SplitMix64 stream `seed`, amplitude i of column c from draws
+ * 2(cN+i) and 2(cN+i)+1; FP64 math for Q1G_C128, FP32 for Q1G_C64), then
+ * each column normalised in FP64.  Run counts are kept.  No counterpart in
+ * the reference, whose constructors give |0...0> or product states only
+ * (src/vectorstate.rs:41-83); it is from_amplitudes without the upload. */
+int q1g_state_fill_random_normal(q1g_state* s, uint64_t seed);
 int q1g_state_synchronize(q1g_state* s);
 /* nr_bits, nr_shots, number of state columns, precision.  Any pointer may be NULL. */
 int q1g_state_info(const q1g_state* s, size_t* nr_bits, size_t* nr_shots, size_t* ncols,

@@ -134,6 +134,33 @@ def uniform(seed, counter):
     return lib().oracle_uniform(seed, counter)
 
 
+def uniforms(seed, counters):
+    """Draws `counters` (a uint64 array) of the SplitMix64 stream `seed`,
+    vectorised: mix(seed + (k+1) * gamma) >> 11, over 2^53 (the stream of
+    oracle.c's oracle_uniform and of the engine's samplers)."""
+    with np.errstate(over="ignore"):
+        k = np.asarray(counters, dtype=np.uint64)
+        z = np.uint64(seed) + (k + np.uint64(1)) * np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return (z >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+
+
+def random_normal_state(nr_bits, ncols, seed):
+    """The state q1g_state_fill_random_normal makes, in FP64: amplitude i of
+    column c has re, im = r (cos 2 pi u2, sin 2 pi u2), r = sqrt(-2 ln(1 -
+    u1)), with u1, u2 draws 2(cN+i), 2(cN+i)+1 of the stream `seed`; each
+    column then has unit norm.  Shape (2^nr_bits, ncols), as states()."""
+    n = 1 << nr_bits
+    k = np.arange(n * ncols, dtype=np.uint64)
+    u1 = uniforms(seed, 2 * k)
+    u2 = uniforms(seed, 2 * k + np.uint64(1))
+    r = np.sqrt(-2.0 * np.log1p(-u1))
+    a = (r * np.cos(2 * np.pi * u2) + 1j * r * np.sin(2 * np.pi * u2)).reshape(ncols, n).T
+    return a / np.linalg.norm(a, axis=0)
+
+
 class OracleState:
     """Complex128 VectorState restatement (src/vectorstate.rs:24-416)."""
 

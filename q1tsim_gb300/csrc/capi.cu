@@ -639,6 +639,14 @@ int q1g_profile_reset(q1g_state* s)
     });
 }
 
+int q1g_state_fill_random_normal(q1g_state* s, uint64_t seed)
+{
+    return guarded([&] {
+        need(s, "state");
+        s->fill_random_normal(seed);
+    });
+}
+
 int q1g_state_set_wait_limit(q1g_state* s, double seconds)
 {
     return guarded([&] {

@@ -295,6 +295,23 @@ void q1g_state::apply_unary_all(const double* mat)
     plan_run(unary_plan.get(), this, mats.data(), mats.size());
 }
 
+// Every column becomes a random unit vector: re and im of each amplitude
+// i.i.d. N(0,1) (column c takes amplitudes c*N .. c*N+N-1 of the stream),
+// then normalised -- the column rescale that settles pending norms.
+void q1g_state::fill_random_normal(uint64_t seed)
+{
+    using namespace q1g;
+    const uint64_t t = total();
+    amps.ensure(t * bsz());
+    launch("random_normal", double(t * bsz()),
+           [&] { return launch_random_normal(amps.p, prec, t, seed, stream); });
+    sparse = false;
+    basis.clear();
+    norms.assign(ncols, 1.0);
+    norm_pending = true;
+    settle_norms();
+}
+
 // src/qustate.rs:100-127: (column, length, apply) runs of equal control bits.
 struct CondRange {
     uint64_t col, len;

@@ -182,6 +182,7 @@ struct q1g_state {
     void apply_op(const q1g::GateOp& op, char* base, uint64_t total_amps);
     void apply_gate(const double* mat, size_t k, const size_t* bits, size_t nbits_given);
     void apply_unary_all(const double* mat);
+    void fill_random_normal(uint64_t seed);
     void apply_conditional(const uint8_t* control, size_t ncontrol, const double* mat, size_t k,
                            const size_t* bits, size_t nbits_given);
     std::vector<double> zero_weights(size_t qbit);

@@ -177,6 +177,9 @@ cudaError_t launch_scatter_subspace(void* full, const void* compact, int prec, i
 cudaError_t launch_product_state(void* amps, int prec, int nbits, const double* d_coefs,
                                  cudaStream_t st);
 cudaError_t launch_convert_c128_to_c64(float2* dst, const double2* src, uint64_t n, cudaStream_t st);
+// total amplitudes with re, im i.i.d. N(0,1) from the SplitMix64 stream
+// `seed` (amplitude i: Box-Muller of uniforms 2i, 2i+1); not normalised.
+cudaError_t launch_random_normal(void* amps, int prec, uint64_t total, uint64_t seed, cudaStream_t st);
 cudaError_t launch_convert_c64_to_c128(double2* dst, const float2* src, uint64_t n, cudaStream_t st);
 // New column j = old column src_col[j] with amplitudes whose bit `pos` differs
 // from keep[j] zeroed and the rest scaled by scale[j] (src/vectorstate.rs:91-104).

@@ -1,6 +1,7 @@
 // State construction, precision conversion and measurement collapse kernels.
 #include "common.cuh"
 #include "kernels.h"
+#include "sampling.cuh"
 
 namespace q1g {
 
@@ -40,6 +41,35 @@ __global__ void k_product_state(T* a, int nbits, const double* coefs)
             im = ni;
         }
         a[i] = cmake<T>(re, im);
+    }
+}
+
+// Amplitude i gets re, im i.i.d. N(0,1) by the Box-Muller transform of
+// uniforms 2i and 2i+1 of the SplitMix64 stream `seed`:
+// r = sqrt(-2 ln(1 - u1)), (re, im) = r (cos 2 pi u2, sin 2 pi u2).
+// complex128 in FP64, complex64 in FP32 (1 - u1 formed in FP64 first, so it
+// is never 0).
+__global__ void k_random_normal_c128(double2* a, uint64_t total, uint64_t seed)
+{
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += stride) {
+        const double u1 = stream_uniform(seed, 2 * i), u2 = stream_uniform(seed, 2 * i + 1);
+        const double r = sqrt(-2.0 * log1p(-u1));
+        double sn, cs;
+        sincospi(2.0 * u2, &sn, &cs);
+        a[i] = make_double2(r * cs, r * sn);
+    }
+}
+
+__global__ void k_random_normal_c64(float2* a, uint64_t total, uint64_t seed)
+{
+    const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+    for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += stride) {
+        const double u1 = stream_uniform(seed, 2 * i), u2 = stream_uniform(seed, 2 * i + 1);
+        const float r = sqrtf(-2.0f * logf((float)(1.0 - u1)));
+        float sn, cs;
+        sincospif(2.0f * (float)u2, &sn, &cs);
+        a[i] = make_float2(r * cs, r * sn);
     }
 }
 
@@ -207,6 +237,16 @@ cudaError_t launch_product_state(void* amps, int prec, int nbits, const double* 
         k_product_state<double2><<<grid, kThreads, 0, st>>>((double2*)amps, nbits, d_coefs);
     else
         k_product_state<float2><<<grid, kThreads, 0, st>>>((float2*)amps, nbits, d_coefs);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_random_normal(void* amps, int prec, uint64_t total, uint64_t seed, cudaStream_t st)
+{
+    const unsigned grid = blocks_for(total, kThreads) > 152 * 64 ? 152 * 64 : blocks_for(total, kThreads);
+    if (prec == kC128)
+        k_random_normal_c128<<<grid, kThreads, 0, st>>>((double2*)amps, total, seed);
+    else
+        k_random_normal_c64<<<grid, kThreads, 0, st>>>((float2*)amps, total, seed);
     return cudaGetLastError();
 }
 

@@ -18,18 +18,21 @@ import time
 
 import numpy as np
 
-from .circuit import Circuit
 from .vectorstate import Rng, VectorState
 
 
 class Request:
-    __slots__ = ("rid", "circuit", "shots", "seed", "arrival", "admitted", "done", "result", "error")
+    """A circuit to run `shots` times with Rng(seed).  init_seed: start from
+    a random normalised state drawn on the device (re, im i.i.d. N(0,1),
+    VectorState.fill_random_normal) instead of |0...0>."""
+    __slots__ = ("rid", "circuit", "shots", "seed", "init_seed", "arrival", "admitted", "done", "result", "error")
 
-    def __init__(self, rid, circuit, shots, seed, arrival=0.0):
+    def __init__(self, rid, circuit, shots, seed, arrival=0.0, init_seed=None):
         self.rid = rid
         self.circuit = circuit
         self.shots = shots
         self.seed = seed
+        self.init_seed = init_seed
         self.arrival = arrival
         self.admitted = None
         self.done = None
@@ -46,10 +49,22 @@ class Request:
         return None if self.done is None else self.done - self.arrival
 
 
+def prepare_state(req, st):
+    """The request's initial state in `st`: |0...0> or its random state (one
+    column: a reused state may hold the basis columns a previous request's
+    measure_all left)."""
+    st.reset_all()
+    if req.init_seed is not None:
+        st.fill_random_normal(req.init_seed)
+
+
 def run_alone(req):
-    """What the request computes when nothing else runs: Circuit.execute."""
+    """What the request computes when nothing else runs: Circuit.execute
+    from its initial state."""
     c = req.circuit
-    c.execute(req.shots, Rng(req.seed))
+    st = VectorState(c.nr_qbits, req.shots, c.precision)
+    prepare_state(req, st)
+    c.execute_with(req.shots, Rng(req.seed), st)
     return c.cstate().copy()
 
 
@@ -127,8 +142,7 @@ class Server:
                     st = VectorState(c.nr_qbits, req.shots, c.precision)
                     st.set_stream(stream.cuda_stream)
                     states[key] = st
-                else:
-                    st.reset_all()
+                prepare_state(req, st)
                 c.execute_with(req.shots, Rng(req.seed), st)
                 req.result = c.cstate().copy()
             except Exception as e:    # reported with the request
@@ -179,24 +193,36 @@ def mixed_requests(count, seed, qmin=10, qmax=26, dmin=5, dmax=50, shots=4096):
     for i in range(count):
         n = int(rng.integers(qmin, qmax + 1))
         kind = int(rng.integers(3))
+        init_seed = None
         if kind == 0:
             c = workloads.ghz(n)
         elif kind == 1:
-            c = _qft_on_random_state(n, int(rng.integers(2 ** 62)))
+            # the QFT of a random state whose amplitudes are i.i.d. N(0,1),
+            # drawn on the device from init_seed
+            c = workloads.qft(n)
+            init_seed = int(rng.integers(2 ** 62))
         else:
             c = workloads.brick(n, int(rng.integers(dmin, dmax + 1)), int(rng.integers(2 ** 62)))
-        out.append(Request(i, c.freeze(), shots, int(rng.integers(2 ** 62))))
+        out.append(Request(i, c.freeze(), shots, int(rng.integers(2 ** 62)), init_seed=init_seed))
     return out
 
 
-def _qft_on_random_state(n, seed):
-    """A random product state prepared by one U3 per qubit, then the QFT."""
-    from . import gates as G
-    from . import workloads
-    rng = np.random.default_rng(seed)
-    prep = Circuit(n, n, precision="c64", fusion_width=5)
-    for q in range(n):
-        prep.add_gate(G.U3(*rng.uniform(0, 2 * np.pi, 3)), [q])
-    q = workloads.qft(n)
-    prep.ops.extend(q.ops)
-    return prep
+def device_seconds(requests):
+    """Device time of each request run alone (the sum of its kernels'
+    CUDA-event times): the bound on how many requests per second the device
+    can serve, whatever the batching."""
+    total = 0.0
+    states = {}
+    for req in requests:
+        c = req.circuit
+        key = (c.nr_qbits, req.shots, c.precision)
+        st = states.get(key)
+        if st is None:
+            st = states[key] = VectorState(c.nr_qbits, req.shots, c.precision)
+        st.profile(True)
+        st.profile_report(reset=True)
+        prepare_state(req, st)
+        c.execute_with(req.shots, Rng(req.seed), st)
+        total += sum(v["ms"] for v in st.profile_report(reset=True).values()) / 1e3
+        st.profile(False)
+    return total

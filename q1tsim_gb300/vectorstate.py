@@ -281,6 +281,11 @@ class VectorState:
             check(L.q1g_profile_reset(self._h))
         return out
 
+    def fill_random_normal(self, seed):
+        """Every column a random unit vector drawn on the device (re, im
+        i.i.d. N(0,1) from the SplitMix64 stream `seed`, then normalised)."""
+        check(_lib.load().q1g_state_fill_random_normal(self._h, int(seed) & (2 ** 64 - 1)))
+
     def set_wait_limit(self, seconds=0.0):
         """Longest wait inside a tensor-core pass before the pass gives up
         with DeviceTimeout (amplitudes then undefined); 0 = default (60 s)."""

@@ -1121,6 +1121,41 @@ def test_tensor_core_wait_limit_expires_then_state_recovers():
         assert 1 - abs(np.vdot(want, got)) ** 2 <= 1e-6
 
 
+@pytest.mark.parametrize("prec,tol", [("c128", 1e-12), ("c64", 2e-6)])
+def test_random_normal_state_matches_oracle(prec, tol):
+    """fill_random_normal draws re, im i.i.d. N(0,1) on the device from the
+    SplitMix64 stream and normalises each column: the oracle's FP64
+    restatement of the same draws (complex64 computes the transform in FP32),
+    the same seed the same state, another seed another one."""
+    n, seed = 12, 2024
+    s = VectorState(n, 8, prec)
+    s.fill_random_normal(seed)
+    got = s.states()
+    want = orc.random_normal_state(n, 1, seed)
+    assert got.shape == want.shape
+    assert np.max(np.abs(got - want)) <= tol
+    assert abs(np.linalg.norm(got) - 1.0) <= (1e-12 if prec == "c128" else 1e-6)
+    s.fill_random_normal(seed)
+    assert np.array_equal(s.states(), got)
+    s.fill_random_normal(seed + 1)
+    assert np.max(np.abs(s.states() - got)) > 1e-3
+
+
+def test_random_normal_state_statistics_at_24_qubits():
+    """At 24 qubits the drawn state has the Porter-Thomas statistics of a
+    random state: N |a|^2 ~ Exp(1), so its mean is 1 and its second moment 2
+    (to 6 standard errors), and it equals the oracle's draws."""
+    n = 24
+    s = VectorState(n, 1, "c64")
+    s.fill_random_normal(77)
+    a = s.states()[:, 0].astype(np.complex128)
+    x = (1 << n) * np.abs(a) ** 2
+    se1, se2 = np.sqrt(1.0 / x.size), np.sqrt(20.0 / x.size)
+    assert abs(x.mean() - 1.0) <= 6 * se1
+    assert abs((x ** 2).mean() - 2.0) <= 6 * se2
+    assert np.max(np.abs(a - orc.random_normal_state(n, 1, 77)[:, 0])) <= 2e-6 / 64
+
+
 def test_compare_reports_normalised_tv():
     rng = np.random.default_rng(2)
     n = 12
