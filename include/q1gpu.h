@@ -117,6 +117,20 @@ int q1g_state_set_fp64_exact(q1g_state* s, int exact);
  * the reference, whose constructors give |0...0> or product states only
  * (src/vectorstate.rs:41-83); it is from_amplitudes without the upload. */
 int q1g_state_fill_random_normal(q1g_state* s, uint64_t seed);
+/* Each column's squared norm, summed in FP64, into out[0..ncols). */
+int q1g_state_column_norms(q1g_state* s, double* out, size_t len);
+/* The state's amplitudes in device memory, densified and with any pending
+ * norm correction applied: interleaved (re, im) in the state's precision,
+ * column c at element c * 2^nr_bits, *bytes in all.  Valid until a call that
+ * changes the state's shape (a measurement, a reset).  Work on the pointer
+ * after this call returns, on a stream ordered after the state's; a caller
+ * that wrote amplitudes calls q1g_state_amplitudes_written before the state's
+ * next call.  It serves an exchange between shards of a larger state (the
+ * sharded state of q1tsim_gb300/sharded.py). */
+int q1g_state_device_amplitudes(q1g_state* s, void** ptr, size_t* bytes);
+/* The caller changed the amplitudes in place: the state takes their column
+ * norms as the norms its later tensor-core plans keep. */
+int q1g_state_amplitudes_written(q1g_state* s);
 int q1g_state_synchronize(q1g_state* s);
 /* nr_bits, nr_shots, number of state columns, precision.  Any pointer may be NULL. */
 int q1g_state_info(const q1g_state* s, size_t* nr_bits, size_t* nr_shots, size_t* ncols,

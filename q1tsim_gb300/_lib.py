@@ -151,6 +151,9 @@ def load():
     _proto(L, "q1g_state_transfer_bytes", _int, [_vp, _u64p, _u64p, _int])
     _proto(L, "q1g_state_set_wait_limit", _int, [_vp, ctypes.c_double])
     _proto(L, "q1g_state_fill_random_normal", _int, [_vp, ctypes.c_uint64])
+    _proto(L, "q1g_state_column_norms", _int, [_vp, _dp, _sz])
+    _proto(L, "q1g_state_device_amplitudes", _int, [_vp, ctypes.POINTER(_vp), _szp])
+    _proto(L, "q1g_state_amplitudes_written", _int, [_vp])
     _proto(L, "q1g_sample_shots_noalloc", _int, [_vp, _int, _sz, _dp, _sz, _u64p, _u64p, _szp, _vp])
     _proto(L, "q1g_histogram", _int, [_u64p, _sz, _u64p, _u64p, _sz, _szp, _vp])
     _lib = L

@@ -639,6 +639,41 @@ int q1g_profile_reset(q1g_state* s)
     });
 }
 
+int q1g_state_column_norms(q1g_state* s, double* out, size_t len)
+{
+    return guarded([&] {
+        need(s, "state");
+        if (len) need(out, "out");
+        if (len < s->ncols) throw Error(Q1G_ERR_NOT_ENOUGH_SPACE, "norms buffer too small", len, s->ncols);
+        s->settle_norms();
+        const std::vector<double> v = s->measure_norms();
+        std::copy(v.begin(), v.end(), out);
+    });
+}
+
+int q1g_state_device_amplitudes(q1g_state* s, void** ptr, size_t* bytes)
+{
+    return guarded([&] {
+        need(s, "state");
+        need(ptr, "ptr");
+        s->ensure_dense();
+        s->settle_norms();
+        s->sync();
+        *ptr = s->amps.p;
+        if (bytes) *bytes = s->total() * s->bsz();
+    });
+}
+
+int q1g_state_amplitudes_written(q1g_state* s)
+{
+    return guarded([&] {
+        need(s, "state");
+        if (s->sparse) throw Error(Q1G_ERR_INVALID_ARGUMENT, "the state has no dense amplitudes to write");
+        s->norm_pending = false;
+        s->norms = s->measure_norms();
+    });
+}
+
 int q1g_state_fill_random_normal(q1g_state* s, uint64_t seed)
 {
     return guarded([&] {

@@ -1209,6 +1209,30 @@ void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n, bool subs
 
 }  // namespace q1g
 
+std::vector<double> q1g_state::measure_norms()
+{
+    using namespace q1g;
+    if (sparse) return std::vector<double>(ncols, 1.0);
+    q1g_state* s = this;
+    const uint64_t total = s->total();
+    const uint64_t chunk = std::min<uint64_t>(s->N, 256);
+    const uint64_t nch = s->N / chunk;
+    const uint64_t ntmp = segment_sums_tmp_doubles(s->ncols, nch);
+    s->dscratch.ensure((s->ncols * nch + 2 * s->ncols + ntmp) * sizeof(double));
+    double* d_sums = s->dscratch.as<double>();
+    double* d_norm = d_sums + s->ncols * nch;
+    s->launch("column_norms", double(total * s->bsz()), [&] {
+        return launch_chunk_sums_dense(s->amps.p, s->prec, total, chunk, d_sums, s->stream);
+    });
+    check_cuda(launch_segment_sums(d_sums, s->ncols, nch, d_norm, d_norm + 2 * s->ncols, s->stream),
+               "segment_sums");
+    s->hstage.ensure(s->ncols * sizeof(double));
+    double* h_norm = s->hstage.as<double>();
+    s->d2h(h_norm, d_norm, s->ncols * sizeof(double), "read norms");
+    s->sync();
+    return std::vector<double>(h_norm, h_norm + s->ncols);
+}
+
 void q1g_state::settle_norms()
 {
     using namespace q1g;
@@ -1220,22 +1244,8 @@ void q1g_state::settle_norms()
     {
         // per-column squared norms now, then rescale each column to the norm
         // it should have (the plans since the last settle were unitary)
+        const std::vector<double> h_norm = s->measure_norms();
         const uint64_t total = s->total();
-        const uint64_t chunk = std::min<uint64_t>(s->N, 256);
-        const uint64_t nch = s->N / chunk;
-        const uint64_t ntmp = segment_sums_tmp_doubles(s->ncols, nch);
-        s->dscratch.ensure((s->ncols * nch + 2 * s->ncols + ntmp) * sizeof(double));
-        double* d_sums = s->dscratch.as<double>();
-        double* d_norm = d_sums + s->ncols * nch;
-        s->launch("norm_check", double(total * s->bsz()), [&] {
-            return launch_chunk_sums_dense(s->amps.p, s->prec, total, chunk, d_sums, s->stream);
-        });
-        check_cuda(launch_segment_sums(d_sums, s->ncols, nch, d_norm, d_norm + 2 * s->ncols, s->stream),
-                   "segment_sums");
-        s->hstage.ensure(s->ncols * sizeof(double));
-        double* h_norm = s->hstage.as<double>();
-        s->d2h(h_norm, d_norm, s->ncols * sizeof(double), "read norms");
-        s->sync();
         std::vector<double> scale(s->ncols, 1.0);
         bool any_scale = false;
         for (uint64_t c = 0; c < s->ncols; ++c) {
@@ -1243,7 +1253,9 @@ void q1g_state::settle_norms()
             any_scale |= scale[c] != 1.0;
         }
         if (any_scale) {
-            double* d_scale = d_norm + s->ncols;
+            // measure_norms left its sums in dscratch: the scales go after them
+            const uint64_t nch = s->N / std::min<uint64_t>(s->N, 256);
+            double* d_scale = s->dscratch.as<double>() + s->ncols * nch + s->ncols;
             s->h2d(d_scale, scale.data(), s->ncols * sizeof(double), "upload scales");
             s->launch("renormalise", 2.0 * total * s->bsz(), [&] {
                 return launch_scale_columns(s->amps.p, s->prec, s->N, s->ncols, d_scale, s->stream);

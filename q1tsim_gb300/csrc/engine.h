@@ -179,6 +179,7 @@ struct q1g_state {
 
     void ensure_dense();
     void settle_norms();
+    std::vector<double> measure_norms();   // each column's squared norm, FP64, now
     void apply_op(const q1g::GateOp& op, char* base, uint64_t total_amps);
     void apply_gate(const double* mat, size_t k, const size_t* bits, size_t nbits_given);
     void apply_unary_all(const double* mat);
