@@ -232,11 +232,13 @@ int q1g_plan_run(q1g_plan* p, q1g_state* s, const double* mats_flat, size_t n_do
 int q1g_plan_set_tensor_cores(q1g_plan* p, int enable);
 
 /* ---- batches of independent circuits: one persistent launch, replayed from a
- * CUDA graph.  Each circuit runs on its own complex64 state of at most two run
- * columns.  A circuit is a program of gates, at most one mid-circuit Z
- * measurement (measure_into, src/vectorstate.rs:237-329), gates conditioned on
- * that measured bit (apply_conditional_gate, src/vectorstate.rs:193-227), and a
- * final measure_all (src/vectorstate.rs:106-161).  This is what
+ * CUDA graph.  Each circuit runs on its own complex64 state of at most 16 run
+ * columns.  A circuit is a program of gates, up to four mid-circuit Z
+ * measurements, each splitting every run column by its outcome (measure_into,
+ * src/vectorstate.rs:237-329), gates conditioned on one classical bit
+ * (apply_conditional_gate, src/vectorstate.rs:193-227: every run of a column
+ * holds the same bits, 0 for bits no measurement wrote), and a final
+ * measure_all (src/vectorstate.rs:106-161).  This is what
  * Circuit::execute (src/circuit.rs:562-762) does for each circuit, for many
  * circuits at once.  Uniforms come from the SplitMix64 stream `seed` of each
  * circuit, drawn in the order the single-state entry points draw them. */

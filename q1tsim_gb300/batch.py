@@ -1,7 +1,8 @@
 """Many independent circuits in one persistent GPU launch.
 
-`Batch` lowers `Circuit` programs of gates, one mid-circuit Z measurement,
-gates conditioned on that bit and a final `measure_all` into the engine's
+`Batch` lowers `Circuit` programs of gates, up to four mid-circuit Z
+measurements, gates conditioned on one classical bit and a final
+`measure_all` into the engine's
 batch op list (include/q1gpu.h, q1g_batch_*), then runs them all in one
 persistent kernel launch replayed from a CUDA graph.  Each circuit's
 classical words equal what `Circuit.execute` with the same `Rng(seed)` gives

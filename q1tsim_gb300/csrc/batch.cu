@@ -1,10 +1,11 @@
 // Batched execution of many independent circuits in one persistent launch.
 //
-// Each circuit is a short program over its own complex64 state of up to two
-// run columns (src/vectorstate.rs:24-35): fused gate blocks, at most one
-// mid-circuit measurement (src/vectorstate.rs:237-329), gates conditioned on
-// that measured bit (src/vectorstate.rs:193-227) and a final measure_all
-// (src/vectorstate.rs:106-161).  The kernel keeps one CTA per SM slot; a CTA
+// Each circuit is a short program over its own complex64 state of up to
+// kBatchMaxCols run columns (src/vectorstate.rs:24-35): fused gate blocks,
+// up to four mid-circuit measurements, each splitting every column by its
+// outcome (src/vectorstate.rs:237-329), gates conditioned on a classical bit
+// (src/vectorstate.rs:193-227; every run of a column holds the same bits)
+// and a final measure_all (src/vectorstate.rs:106-161).  The kernel keeps one CTA per SM slot; a CTA
 // takes the next circuit from an atomic queue (largest circuits first) and
 // runs its whole program: the gate passes stream the circuit's columns
 // through registers, the measurement reduces and splits the column, and the
@@ -174,10 +175,12 @@ k_batch(BatchArgs args)
     float2* stage = stage_all + (threadIdx.x >> 5) * (1 << 10);
     __shared__ double red[kBatchWarps];
     __shared__ int s_circ;
-    __shared__ int s_ncols, s_colbit[2];
-    __shared__ uint64_t s_counts[2];
-    __shared__ double s_scale[2];
-    __shared__ int s_keep[2];
+    // per run column: runs, classical bits of its runs, and during a
+    // measurement the weight of outcome 0, the draw and the first new slot
+    __shared__ int s_ncols, s_nnew;
+    __shared__ uint64_t s_counts[kBatchMaxCols], s_colword[kBatchMaxCols], s_n0k[kBatchMaxCols];
+    __shared__ double s_w0[kBatchMaxCols];
+    __shared__ int s_newidx[kBatchMaxCols];
     double* scratch = args.scratch + (uint64_t)blockIdx.x * args.scratch_per_cta;
     // algorithmic bytes (each pass's reads and writes of amplitudes and
     // classical words), counted by thread 0 in shared memory (no register is
@@ -194,15 +197,15 @@ k_batch(BatchArgs args)
         if (c >= args.ncircuits) break;
         const BatchCircuit C = args.circuits[c];
         const uint64_t N = uint64_t(1) << C.nbits;
-        float2* col[2] = {args.arena + C.state_off, args.arena + C.state_off + N};
+        float2* const col0 = args.arena + C.state_off;
+        auto col = [&](int k) { return col0 + (uint64_t)k * N; };
         uint64_t* res = args.results + C.res_off;
         for (uint64_t v = threadIdx.x; v < N / 2; v += kBatchThreads)
-            reinterpret_cast<float4*>(col[0])[v] = make_float4(v == 0 ? 1.f : 0.f, 0.f, 0.f, 0.f);
+            reinterpret_cast<float4*>(col0)[v] = make_float4(v == 0 ? 1.f : 0.f, 0.f, 0.f, 0.f);
         if (threadIdx.x == 0) {
             s_ncols = 1;
             s_counts[0] = C.nshots;
-            s_counts[1] = 0;
-            s_colbit[0] = s_colbit[1] = -1;
+            s_colword[0] = 0;
         }
         uint64_t ctr = 0;   // position in the circuit's uniform stream
         if (threadIdx.x == 0) {
@@ -224,78 +227,107 @@ k_batch(BatchArgs args)
                 for (int e = threadIdx.x; e < D * D; e += kBatchThreads) smat[e] = args.mats[sop.mat + e];
                 __syncthreads();
                 for (int k = 0; k < s_ncols; ++k) {
-                    if (sop.cond >= 0 && s_colbit[k] != sop.cond) continue;
+                    if (sop.cond >= 0 && (int)((s_colword[k] >> sop.ccbit) & 1u) != sop.cond) continue;
                     if (threadIdx.x == 0) ++s_cpass;
                     switch (sop.t) {
-                        case 1: apply_dense<1>(col[k], N, sop, smat, stage); break;
-                        case 2: apply_dense<2>(col[k], N, sop, smat, stage); break;
-                        case 3: apply_dense<3>(col[k], N, sop, smat, stage); break;
-                        default: apply_dense<4>(col[k], N, sop, smat, stage); break;
+                        case 1: apply_dense<1>(col(k), N, sop, smat, stage); break;
+                        case 2: apply_dense<2>(col(k), N, sop, smat, stage); break;
+                        case 3: apply_dense<3>(col(k), N, sop, smat, stage); break;
+                        default: apply_dense<4>(col(k), N, sop, smat, stage); break;
                     }
                 }
                 __syncthreads();
             } else if (kind == kBatchMeasure) {
-                // P(bit = 0) of the single column (src/vectorstate.rs:252-261)
+                // per column: P(bit = 0) (src/vectorstate.rs:252-261) and
+                // n0 ~ Binomial(runs, P) from the next uniform of the stream
                 const uint64_t bit = uint64_t(1) << sop.pos;
-                double acc = 0.0;
-                const float4* c4 = reinterpret_cast<const float4*>(col[0]);   // two amplitudes (N >= 2)
+                const int nc = s_ncols;
+                for (int k = 0; k < nc; ++k) {
+                    double acc = 0.0;
+                    const float4* c4 = reinterpret_cast<const float4*>(col(k));   // two amplitudes (N >= 2)
 #pragma unroll 4
-                for (uint64_t v = threadIdx.x; v < N / 2; v += kBatchThreads) {
-                    const float4 q = c4[v];
-                    if (!((2 * v) & bit)) acc += (double)psq(make_float2(q.x, q.y));
-                    if (!((2 * v + 1) & bit)) acc += (double)psq(make_float2(q.z, q.w));
-                }
-                const double w0 = block_reduce(acc, red);
-                const uint64_t n0 = binomial_inv_block(C.nshots, fmin(w0, 1.0), stream_uniform(C.seed, ctr),
-                                                       reinterpret_cast<double*>(stage_all), &s_n0);
-                if (threadIdx.x == 0) {
-                    if (n0 == C.nshots || n0 == 0) {
-                        s_ncols = 1;
-                        s_keep[0] = n0 == 0 ? 1 : 0;
-                        s_scale[0] = 1.0 / sqrt(n0 == 0 ? 1.0 - w0 : w0);
-                        s_colbit[0] = s_keep[0];
-                        s_counts[0] = C.nshots;
-                    } else {
-                        s_ncols = 2;
-                        s_keep[0] = 0;
-                        s_keep[1] = 1;
-                        s_scale[0] = 1.0 / sqrt(w0);
-                        s_scale[1] = 1.0 / sqrt(1.0 - w0);
-                        s_colbit[0] = 0;
-                        s_colbit[1] = 1;
-                        s_counts[0] = n0;
-                        s_counts[1] = C.nshots - n0;
+                    for (uint64_t v = threadIdx.x; v < N / 2; v += kBatchThreads) {
+                        const float4 q = c4[v];
+                        if (!((2 * v) & bit)) acc += (double)psq(make_float2(q.x, q.y));
+                        if (!((2 * v + 1) & bit)) acc += (double)psq(make_float2(q.z, q.w));
                     }
+                    const double w0 = block_reduce(acc, red);
+                    const uint64_t n0 = binomial_inv_block(s_counts[k], fmin(w0, 1.0), stream_uniform(C.seed, ctr + k),
+                                                           reinterpret_cast<double*>(stage_all), &s_n0);
+                    if (threadIdx.x == 0) {
+                        s_w0[k] = w0;
+                        s_n0k[k] = n0;
+                    }
+                    __syncthreads();
                 }
-                ++ctr;
-                __syncthreads();
+                ctr += nc;
+                // results: a column's first n0 runs read 0, the rest 1
+                // (src/vectorstate.rs:290-297)
                 {
                     const uint64_t one = uint64_t(1) << sop.cbit;
-                    for (uint64_t r = threadIdx.x; r < C.nshots; r += kBatchThreads)
-                        res[r] = r < n0 ? (res[r] & ~one) : (res[r] | one);
-                }
-                // collapse (src/vectorstate.rs:91-104), splitting into two columns
-                if (threadIdx.x == 0) s_moved += (2 + (uint64_t)s_ncols) * N * sizeof(float2) + 2 * C.nshots * sizeof(uint64_t);
-                const float f0 = (float)s_scale[0];
-                const float f1 = s_ncols == 2 ? (float)s_scale[1] : 0.f;
-                const bool two = s_ncols == 2;
-                const uint64_t keep0 = s_keep[0] ? bit : 0;
-                float4* c0 = reinterpret_cast<float4*>(col[0]);
-                float4* c1 = reinterpret_cast<float4*>(col[1]);
-#pragma unroll 4
-                for (uint64_t v = threadIdx.x; v < N / 2; v += kBatchThreads) {
-                    const float4 q = c0[v];
-                    const bool b0 = ((2 * v) & bit) != 0, b1 = ((2 * v + 1) & bit) != 0;
-                    if (two) {
-                        c1[v] = make_float4(b0 ? q.x * f1 : 0.f, b0 ? q.y * f1 : 0.f, b1 ? q.z * f1 : 0.f,
-                                            b1 ? q.w * f1 : 0.f);
-                        c0[v] = make_float4(b0 ? 0.f : q.x * f0, b0 ? 0.f : q.y * f0, b1 ? 0.f : q.z * f0,
-                                            b1 ? 0.f : q.w * f0);
-                    } else {
-                        const bool k0 = ((2 * v) & bit) == keep0, k1 = ((2 * v + 1) & bit) == keep0;
-                        c0[v] = make_float4(k0 ? q.x * f0 : 0.f, k0 ? q.y * f0 : 0.f, k1 ? q.z * f0 : 0.f,
-                                            k1 ? q.w * f0 : 0.f);
+                    uint64_t r0 = 0;
+                    for (int k = 0; k < nc; ++k) {
+                        const uint64_t m = s_counts[k], n0 = s_n0k[k];
+                        for (uint64_t r = threadIdx.x; r < m; r += kBatchThreads)
+                            res[r0 + r] = r < n0 ? (res[r0 + r] & ~one) : (res[r0 + r] | one);
+                        r0 += m;
                     }
+                }
+                // the new columns: outcome 0 then outcome 1 of each old column,
+                // the empty ones left out (src/vectorstate.rs:299-322)
+                if (threadIdx.x == 0) {
+                    int nn = 0;
+                    for (int k = 0; k < nc; ++k) {
+                        s_newidx[k] = nn;
+                        nn += (s_n0k[k] > 0 ? 1 : 0) + (s_n0k[k] < s_counts[k] ? 1 : 0);
+                    }
+                    s_nnew = nn;
+                    s_moved += (uint64_t)(2 * nc + nn) * N * sizeof(float2) + 2 * C.nshots * sizeof(uint64_t);
+                }
+                __syncthreads();
+                // collapse (src/vectorstate.rs:91-104), in place from the last
+                // column down: column k's new slots lie at or above k and
+                // below the slots of the columns after it
+                for (int k = nc - 1; k >= 0; --k) {
+                    const uint64_t m = s_counts[k], n0 = s_n0k[k];
+                    const bool has0 = n0 > 0, has1 = n0 < m;
+                    const double w0 = s_w0[k];
+                    const float f0 = has0 ? (float)(1.0 / sqrt(w0)) : 0.f;
+                    const float f1 = has1 ? (float)(1.0 / sqrt(1.0 - w0)) : 0.f;
+                    const int base = s_newidx[k];
+                    const float4* src = reinterpret_cast<const float4*>(col(k));
+                    float4* d0 = reinterpret_cast<float4*>(col(base));
+                    float4* d1 = reinterpret_cast<float4*>(col(base + (has0 ? 1 : 0)));
+#pragma unroll 4
+                    for (uint64_t v = threadIdx.x; v < N / 2; v += kBatchThreads) {
+                        const float4 q = src[v];
+                        const bool b0 = ((2 * v) & bit) != 0, b1 = ((2 * v + 1) & bit) != 0;
+                        if (has1)
+                            d1[v] = make_float4(b0 ? q.x * f1 : 0.f, b0 ? q.y * f1 : 0.f, b1 ? q.z * f1 : 0.f,
+                                                b1 ? q.w * f1 : 0.f);
+                        if (has0)
+                            d0[v] = make_float4(b0 ? 0.f : q.x * f0, b0 ? 0.f : q.y * f0, b1 ? 0.f : q.z * f0,
+                                                b1 ? 0.f : q.w * f0);
+                    }
+                    __syncthreads();
+                }
+                // the column list (runs and classical bits) follows the split
+                if (threadIdx.x == 0) {
+                    const uint64_t one = uint64_t(1) << sop.cbit;
+                    for (int k = nc - 1; k >= 0; --k) {
+                        const uint64_t m = s_counts[k], n0 = s_n0k[k], w = s_colword[k] & ~one;
+                        int slot = s_newidx[k];
+                        if (n0 > 0) {
+                            s_counts[slot] = n0;
+                            s_colword[slot] = w;
+                            ++slot;
+                        }
+                        if (n0 < m) {
+                            s_counts[slot] = m - n0;
+                            s_colword[slot] = w | one;
+                        }
+                    }
+                    s_ncols = s_nnew;
                 }
                 __syncthreads();
             } else if (kind == kBatchSample) {
@@ -310,7 +342,7 @@ k_batch(BatchArgs args)
                     const uint64_t m = s_counts[k];
                     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
                     for (uint64_t ch = warp; ch < nch; ch += kBatchWarps) {
-                        const double sum = chunk_sum(col[k], ch * chunk, chunk, lane);
+                        const double sum = chunk_sum(col(k), ch * chunk, chunk, lane);
                         if (lane == 0) excl[ch] = sum;
                     }
                     __syncthreads();
@@ -324,7 +356,7 @@ k_batch(BatchArgs args)
                     for (uint64_t j = warp; j < m; j += kBatchWarps) {
                         const double u = us[j + 1] / esum;
                         uint64_t idx;
-                        if (sample_one((const float2*)col[k], chunk, excl, nch, total, u, lane, &idx)) {
+                        if (sample_one((const float2*)col(k), chunk, excl, nch, total, u, lane, &idx)) {
                             const uint64_t r = r0 + j;
                             res[r] = (res[r] & mask) | outcome_word(idx, C.nbits, cpos);
                         }

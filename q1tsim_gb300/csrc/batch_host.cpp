@@ -31,13 +31,14 @@ void batch_tile_layout(BatchOp& op, const int* pos, int tb, int nbits)
     warp_tile_layout(op.tile, pos, tb, op.offs, nbits, 10, 4);
 }
 
-static BatchOp dense_op(const std::vector<cd>& m, const std::vector<int>& qubits, int nbits, int cond,
+static BatchOp dense_op(const std::vector<cd>& m, const std::vector<int>& qubits, int nbits, int cond, int ccbit,
                         std::vector<float2>& pool)
 {
     BatchOp op{};
     op.kind = kBatchDense;
     op.t = (int)qubits.size();
     op.cond = cond;
+    op.ccbit = ccbit;
     op.map.nz = op.t;
     std::vector<int> pos(op.t);
     for (int j = 0; j < op.t; ++j) pos[j] = nbits - 1 - qubits[j];
@@ -78,11 +79,11 @@ void batch_add_circuit(q1g_batch* b, size_t nr_bits, size_t nr_shots, uint64_t s
         for (const auto& blk : fuse(gb, n, b->width)) {
             const auto m = blk.gates.size() == 1 ? embed_matrix(seg[blk.gates[0]].mat, seg[blk.gates[0]].bits, blk.qubits)
                                                  : block_matrix(blk, seg);
-            b->ops.push_back(dense_op(m, blk.qubits, n, -1, b->mats));
+            b->ops.push_back(dense_op(m, blk.qubits, n, -1, 0, b->mats));
         }
         seg.clear();
     };
-    int measured_cbit = -1;
+    int nmeasure = 0;
     bool sampled = false;
     size_t bo = 0, mo = 0;
     for (size_t i = 0; i < nops; ++i) {
@@ -105,26 +106,31 @@ void batch_add_circuit(q1g_batch* b, size_t nr_bits, size_t nr_shots, uint64_t s
                 seg.push_back(g);
             } else {
                 flush();
+                // every run of a column holds the same classical bits (set by
+                // the measurements that split the columns, 0 before any), so
+                // a gate conditioned on one bit applies to whole columns
                 const size_t cbit = args[2 * i], value = args[2 * i + 1];
-                if ((int)cbit != measured_cbit || value > 1)
-                    throw Error(Q1G_ERR_INVALID_ARGUMENT,
-                                "a batched conditional gate must test the bit of the circuit's measurement");
+                if (cbit >= 64) throw Error(Q1G_ERR_INVALID_CBIT, "Invalid classical bit " + std::to_string(cbit), cbit);
+                if (value > 1)
+                    throw Error(Q1G_ERR_INVALID_ARGUMENT, "a batched conditional gate tests one classical bit for 0 or 1");
                 std::vector<int> q = g.bits;
                 std::sort(q.begin(), q.end());
-                b->ops.push_back(dense_op(embed_matrix(g.mat, g.bits, q), q, n, (int)value, b->mats));
+                b->ops.push_back(dense_op(embed_matrix(g.mat, g.bits, q), q, n, (int)value, (int)cbit, b->mats));
             }
         } else if (kinds[i] == Q1G_OP_MEASURE) {
             flush();
-            if (measured_cbit >= 0) throw Error(Q1G_ERR_INVALID_ARGUMENT, "one measurement per batched circuit");
+            if ((1 << (nmeasure + 1)) > kBatchMaxCols)
+                throw Error(Q1G_ERR_INVALID_ARGUMENT, "at most 4 mid-circuit measurements per batched circuit (" +
+                                                          std::to_string(kBatchMaxCols) + " run columns)");
             const size_t q = args[2 * i], cbit = args[2 * i + 1];
-            if (q >= nr_bits) throw Error(Q1G_ERR_INVALID_QBIT, "Invalid qubit index " + std::to_string(q));
-            if (cbit >= 64) throw Error(Q1G_ERR_INVALID_CBIT, "Invalid classical bit " + std::to_string(cbit));
+            if (q >= nr_bits) throw Error(Q1G_ERR_INVALID_QBIT, "Invalid qubit index " + std::to_string(q), q);
+            if (cbit >= 64) throw Error(Q1G_ERR_INVALID_CBIT, "Invalid classical bit " + std::to_string(cbit), cbit);
             BatchOp op{};
             op.kind = kBatchMeasure;
             op.pos = n - 1 - (int)q;
             op.cbit = (int)cbit;
             b->ops.push_back(op);
-            measured_cbit = (int)cbit;
+            ++nmeasure;
         } else if (kinds[i] == Q1G_OP_MEASURE_ALL) {
             flush();
             if (k != nr_bits)
@@ -147,6 +153,9 @@ void batch_add_circuit(q1g_batch* b, size_t nr_bits, size_t nr_shots, uint64_t s
     }
     flush();
     C.op_end = (uint32_t)b->ops.size();
+    // every measurement at most doubles the columns, and a column holds at
+    // least one run
+    C.maxcols = (int)std::min<uint64_t>(uint64_t(1) << nmeasure, std::max<uint64_t>(nr_shots, 1));
     b->circuits.push_back(C);
 }
 
@@ -165,8 +174,8 @@ static void batch_build(q1g_batch* b)
     // queue order: most work first (longest-processing-time order), so the
     // long circuits start early and the short ones fill in at the end.  The
     // work estimate counts amplitude reads and writes: every gate pass over
-    // every column (two after the measurement), the measurement, and the
-    // sampling's chunk sums and searched chunks.
+    // every column (their number at most doubling at each measurement), the
+    // measurements, and the sampling's chunk sums and searched chunks.
     const size_t nc = b->circuits.size();
     std::vector<double> work(nc, 0.0);
     for (size_t i = 0; i < nc; ++i) {
@@ -178,8 +187,8 @@ static void batch_build(q1g_batch* b)
             if (op.kind == kBatchDense) {
                 w += 2.0 * N * (op.cond >= 0 ? 1.0 : cols);
             } else if (op.kind == kBatchMeasure) {
-                w += 4.0 * N;
-                cols = 2.0;
+                w += 4.0 * N * cols;
+                cols = std::min(2.0 * cols, (double)C.maxcols);
             } else {
                 w += N * cols + (double)C.nshots * std::min(N, 256.0);
             }
@@ -200,7 +209,7 @@ static void batch_build(q1g_batch* b)
     for (size_t i : order) {
         BatchCircuit C = b->circuits[i];
         C.state_off = off;
-        off += 2 * (uint64_t(1) << C.nbits);
+        off += (uint64_t)C.maxcols * (uint64_t(1) << C.nbits);
         const uint64_t n = uint64_t(1) << C.nbits;
         per_cta = std::max<uint64_t>(per_cta, n / std::min<uint64_t>(n, 256) + C.nshots + 2);
         queue.push_back(C);

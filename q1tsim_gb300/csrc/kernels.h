@@ -243,12 +243,12 @@ enum { kBatchDense = 0, kBatchMeasure = 1, kBatchSample = 2 };
 struct BatchOp {
     int kind;
     int t;            // dense: target qubits (1..4)
-    int cond;         // dense: -1 all columns, else only columns whose measured bit equals it
+    int cond;         // dense: -1 all columns, else only columns whose classical bit ccbit equals it
     int pos;          // measure: bit position
     int cbit;         // measure: classical bit
     uint32_t mat;     // dense: first float2 of the 2^t x 2^t matrix in the pool
     uint32_t cpos;    // sample: index of the 64-entry classical-bit table
-    int pad_;
+    int ccbit;        // dense with cond >= 0: the classical bit tested
     uint64_t cmask;   // sample: classical bits the outcome overwrites
     IndexMap map;     // dense: the gate positions, zeroed
     uint64_t offs[16];
@@ -257,12 +257,15 @@ struct BatchOp {
     WarpTile tile;
 };
 
+// Run columns a batched circuit may reach: each mid-circuit measurement
+// splits every column in two, so at most four measurements per circuit.
+constexpr int kBatchMaxCols = 16;
 struct BatchCircuit {
-    uint64_t state_off;   // amplitude offset of column 0 (column 1 follows)
+    uint64_t state_off;   // amplitude offset of column 0 (the others follow, 2^nbits apart)
     uint64_t res_off;     // first classical word of this circuit's runs
     uint32_t op_begin, op_end;
     int nbits;
-    int pad_;
+    int maxcols;          // column slots reserved in the arena
     uint64_t nshots;
     uint64_t seed;        // SplitMix64 stream of this circuit's uniforms
 };

@@ -53,24 +53,32 @@ def ghz(n, precision="c64", fusion_width=5, measure=True):
     return c
 
 
-def mid_measure_circuit(n, depth, seed):
-    """Layers of seeded U3 / CX / CZ gates with one mid-circuit Z measurement
-    on a random qubit (classical bit 0) followed by an X on that qubit
-    conditioned on the result, then measure_all into classical bits 1..n."""
+def mid_measure_circuit(n, depth, seed, nmeasure=1):
+    """Layers of seeded U3 / CX / CZ gates with `nmeasure` mid-circuit Z
+    measurements: measurement j on a random qubit into classical bit j,
+    followed by an X on that qubit conditioned on the result (from the second
+    on, every other one conditioned on the previous bit being 0 instead);
+    then measure_all into classical bits nmeasure .. nmeasure+n-1."""
     rng = np.random.default_rng(seed)
-    c = Circuit(n, n + 1, precision="c64", fusion_width=4)
+    c = Circuit(n, n + nmeasure, precision="c64", fusion_width=4)
     mid = int(rng.integers(1, depth))
     mq = int(rng.integers(n))
+    extra = [(int(rng.integers(1, depth + 1)), int(rng.integers(n))) for _ in range(nmeasure - 1)]
+    meas = sorted([(mid, mq)] + extra, key=lambda x: x[0])
     for layer in range(depth):
         for q in range(n):
             c.add_gate(G.U3(*rng.uniform(0.0, 2 * math.pi, 3)), [q])
         start = layer % 2
         for q in range(start, n - 1, 2):
             c.add_gate(G.CX() if rng.random() < 0.5 else G.CZ(), [q, q + 1])
-        if layer + 1 == mid:
-            c.measure(mq, 0)
-            c.add_conditional_gate([0], 1, G.X(), [mq])
-    c.measure_all(list(range(1, n + 1)))
+        for j, (at, q) in enumerate(meas):
+            if at == layer + 1:
+                c.measure(q, j)
+                if j > 0 and j % 2 == 0:
+                    c.add_conditional_gate([j - 1], 0, G.X(), [q])
+                else:
+                    c.add_conditional_gate([j], 1, G.X(), [q])
+    c.measure_all(list(range(nmeasure, n + nmeasure)))
     return c
 
 
