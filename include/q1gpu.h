@@ -230,6 +230,15 @@ int q1g_plan_run(q1g_plan* p, q1g_state* s, const double* mats_flat, size_t n_do
  * 1 (default) = tcgen05 tensor cores (FP32-accurate: three f16 products of
  * 11-bit operand halves), 0 = CUDA cores (FP32). */
 int q1g_plan_set_tensor_cores(q1g_plan* p, int enable);
+/* Tiling of the plan's tensor-core passes (tuned per circuit structure by
+ * q1tsim_gb300/autotune.py): allow_pairs lets two consecutive blocks whose
+ * qubits fit one 12-position tile share a pass; a pair's tile may hold at
+ * most max_high_positions positions at or above 2 MB strides (default 5: at
+ * most 32 large pages per tile); an unpadded tile, one tensor-map copy, is
+ * kept while its shared-memory bank wavefronts stay within conflict_slack
+ * times the minimum (default 2), else it is padded and copied in pieces.
+ * No counterpart in the reference. */
+int q1g_plan_set_tc_tiling(q1g_plan* p, int allow_pairs, int max_high_positions, int conflict_slack);
 
 /* ---- batches of independent circuits: one persistent launch, replayed from a
  * CUDA graph.  Each circuit runs on its own complex64 state of at most 16 run

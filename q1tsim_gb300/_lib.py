@@ -144,6 +144,7 @@ def load():
     _proto(L, "q1g_plan_block_matrix", _int, [_vp, _sz, _dp, _sz, _dp, _szp])
     _proto(L, "q1g_plan_run", _int, [_vp, _vp, _dp, _sz])
     _proto(L, "q1g_plan_set_tensor_cores", _int, [_vp, _int])
+    _proto(L, "q1g_plan_set_tc_tiling", _int, [_vp, _int, _int, _int])
     _proto(L, "q1g_plan_set_gate_kinds", _int, [_vp, ctypes.POINTER(ctypes.c_ubyte), _sz])
     _proto(L, "q1g_profile_enable", _int, [_vp, _int])
     _proto(L, "q1g_profile_report", _int, [_vp, ctypes.c_char_p, _u64p, _dp, _dp, _szp])

@@ -306,15 +306,17 @@ class Circuit:
             if plan is None:
                 bits = [op[2] for op in seq]
                 kinds = [op[1].plan_kind() for op in seq]
-                width, tc = self.fusion_width, True
+                width, tc, tiling = self.fusion_width, True, None
                 if width == "auto":
                     from . import autotune
-                    width, tc = autotune.tune(self.nr_qbits, q_state.precision, bits, flat, kinds=kinds)
+                    width, tc, tiling = autotune.tune(self.nr_qbits, q_state.precision, bits, flat, kinds=kinds)
                 if q_state.precision == "c128" and width > 3:
                     # complex128 blocks of up to 3 qubits run on double-float
                     # pairs in warp tiles; larger ones would take the FP64 pipe
                     width = 3
                 plan = Plan(self.nr_qbits, bits, width, tensor_cores=tc, kinds=kinds)
+                if tiling is not None and tiling != Plan.DEFAULT_TC_TILING:
+                    plan.set_tc_tiling(*tiling)
                 self._plans[key] = plan
             q_state.apply_plan(plan, flat)
         else:

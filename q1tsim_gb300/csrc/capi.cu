@@ -491,6 +491,20 @@ int q1g_plan_block_matrix(const q1g_plan* p, size_t i, const double* mats_flat, 
     });
 }
 
+int q1g_plan_set_tc_tiling(q1g_plan* p, int allow_pairs, int max_high_positions, int conflict_slack)
+{
+    return guarded([&] {
+        need(p, "plan");
+        if (max_high_positions < 0 || max_high_positions > 12)
+            throw Error(Q1G_ERR_INVALID_ARGUMENT, "max_high_positions must be in 0..12");
+        if (conflict_slack < 1 || conflict_slack > 64)
+            throw Error(Q1G_ERR_INVALID_ARGUMENT, "conflict_slack must be in 1..64");
+        p->tc_pairs = allow_pairs != 0;
+        p->tc_max_high = max_high_positions;
+        p->tc_slack = conflict_slack;
+    });
+}
+
 int q1g_plan_set_tensor_cores(q1g_plan* p, int enable)
 {
     return guarded([&] {

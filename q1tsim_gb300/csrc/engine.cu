@@ -737,13 +737,13 @@ static int tile_run_bits(const std::vector<int>& T)
 // at most 32 runs per tile.  Shorter runs need the tile to be one
 // tensor-map box, unpadded.
 constexpr int kMinTcRunBits = 7;
-// At most this many tile positions at or above 2 MB strides (position 18 of
-// complex64): a tile then touches at most 32 large pages.
-constexpr int kMaxTcHighPositions = 5;
+// Tile positions at or above this one are 2 MB (a large page) or more apart
+// in complex64; a pair's tile may have q1g_plan::tc_max_high of them (5 by
+// default: at most 32 large pages per tile).
 constexpr int kHighPosition = 18;
 
 static TcPass lower_tc_pass(const std::vector<const std::vector<cd>*>& mats,
-                            const std::vector<const std::vector<int>*>& bits, int nbits, uint64_t ncols)
+                            const std::vector<const std::vector<int>*>& bits, int nbits, uint64_t ncols, int slack)
 {
     TcPass t;
     const std::vector<int> T = tile_positions(bits, nbits);
@@ -793,7 +793,7 @@ static TcPass lower_tc_pass(const std::vector<const std::vector<cd>*>& mats,
         }
         G.vec2 = G.jgate[1] == 1u ? 1u : 0u;
     }
-    tc_choose_padding(t.offs, t.box.usable != 0);
+    tc_choose_padding(t.offs, t.box.usable != 0, slack);
     return t;
 }
 
@@ -1051,14 +1051,16 @@ void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n, bool subs
     auto lower_tc_cached = [&](size_t i, int nblk) -> TcPass {
         if (p->tc_memo.size() != 2 * nb) p->tc_memo.assign(2 * nb, TcPassMemo{});
         TcPassMemo& e = p->tc_memo[2 * i + (size_t)(nblk - 1)];
-        bool hit = e.nblocks == nblk && e.nbits == s->nbits && e.ncols == s->ncols;
+        bool hit = e.nblocks == nblk && e.nbits == s->nbits && e.ncols == s->ncols && e.slack == p->tc_slack;
         for (int j = 0; hit && j < nblk; ++j) hit = e.bits[j] == bbits[i + j] && e.mats[j] == bmats[i + j];
         if (!hit) {
             if (nblk == 2)
-                e.pass = lower_tc_pass({&bmats[i], &bmats[i + 1]}, {&bbits[i], &bbits[i + 1]}, s->nbits, s->ncols);
+                e.pass = lower_tc_pass({&bmats[i], &bmats[i + 1]}, {&bbits[i], &bbits[i + 1]}, s->nbits, s->ncols,
+                                       p->tc_slack);
             else
-                e.pass = lower_tc_pass({&bmats[i]}, {&bbits[i]}, s->nbits, s->ncols);
+                e.pass = lower_tc_pass({&bmats[i]}, {&bbits[i]}, s->nbits, s->ncols, p->tc_slack);
             e.nblocks = nblk;
+            e.slack = p->tc_slack;
             e.nbits = s->nbits;
             e.ncols = s->ncols;
             for (int j = 0; j < nblk; ++j) {
@@ -1119,13 +1121,13 @@ void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n, bool subs
             // 12-position tile with runs of >= 128 amplitudes
             TcPass t;
             bool paired = false;
-            if (i + 1 < nb && eligible(i + 1) &&
+            if (p->tc_pairs && i + 1 < nb && eligible(i + 1) &&
                 union_size(positions_of(bbits[i], s->nbits), positions_of(bbits[i + 1], s->nbits)) <= 12) {
                 const auto T2 = tile_positions({&bbits[i], &bbits[i + 1]}, s->nbits);
                 int high = 0;
                 for (int p : T2) high += p >= kHighPosition;
                 const int L2 = tile_run_bits(T2);
-                if (high <= kMaxTcHighPositions &&
+                if (high <= p->tc_max_high &&
                     (L2 >= kMinTcRunBits || tc_tile_box(T2.data(), s->nbits, s->ncols).usable)) {
                     t = lower_tc_cached(i, 2);
                     // short runs only as one unpadded tensor-map copy

@@ -709,10 +709,10 @@ int best_row_order(const TcBlockGeom& G, uint32_t pad, uint32_t* order)
 
 }  // namespace
 
-void tc_choose_padding(TcOffsets& o, bool tma_ok)
+void tc_choose_padding(TcOffsets& o, bool tma_ok, int conflict_slack)
 {
-    // The choice depends only on the tile geometry, which repeats from run to
-    // run of a plan: remember it.
+    // The choice depends only on the tile geometry (and the slack), which
+    // repeats from run to run of a plan: remember it.
     struct Choice {
         uint32_t pad;
         uint32_t order[2][7];
@@ -720,6 +720,7 @@ void tc_choose_padding(TcOffsets& o, bool tma_ok)
     static std::mutex mu;
     static std::unordered_map<std::string, Choice> memo;
     std::string key(1, tma_ok ? 'T' : 'P');
+    key.append((const char*)&conflict_slack, sizeof(conflict_slack));
     key.append((const char*)&o.nblocks, sizeof(o.nblocks));
     key.append((const char*)&o.run_bits, sizeof(o.run_bits));
     for (uint32_t b = 0; b < o.nblocks; ++b) {
@@ -743,7 +744,7 @@ void tc_choose_padding(TcOffsets& o, bool tma_ok)
         long best = -1, ideal = 0;
         for (uint32_t b = 0; b < o.nblocks; ++b) ideal += o.blk[b].vec2 ? 16 * 4 : 32 * 2;
         for (uint32_t pad : cands) {
-            if (pad < 31 && tma_ok && best >= 0 && best <= 2 * ideal) break;   // keep the tensor-map copy
+            if (pad < 31 && tma_ok && best >= 0 && best <= conflict_slack * ideal) break;   // keep the tensor-map copy
             long cost = 0;
             uint32_t order[2][7] = {};
             for (uint32_t b = 0; b < o.nblocks; ++b)

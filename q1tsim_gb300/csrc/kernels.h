@@ -134,9 +134,9 @@ TcTileBox tc_tile_box(const int* tile_pos /* 12, ascending */, int nbits, uint64
 // Picks pad_shift (and piece_bits, npieces, stage_bytes, the blocks' staged
 // offsets) that minimise shared-memory bank conflicts of the per-row reads.
 // With tma_ok (the tile is one tensor-map box) an unpadded tile is kept when
-// its conflicts stay within twice the minimum: one tensor copy per tile beats
-// padded piece copies.
-void tc_choose_padding(TcOffsets& offs, bool tma_ok);
+// its conflicts stay within conflict_slack times the minimum: one tensor copy
+// per tile beats padded piece copies.
+void tc_choose_padding(TcOffsets& offs, bool tma_ok, int conflict_slack = 2);
 // d_bimage: nblocks consecutive 16 KB f16 hi/lo images of the blocks' real
 // 64x64 embeddings in the kernel's swizzled layout; d_err: set to 1 if a
 // bounded wait expired.  wait_ns: longest any of the kernel's waits may

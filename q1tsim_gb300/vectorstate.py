@@ -304,6 +304,9 @@ class Plan:
     """A gate sequence lowered once: structure, fusion grouping, passes."""
 
     KIND_GENERAL, KIND_DIAGONAL, KIND_SWAP = 0, 1, 2
+    # (pairs of blocks per pass allowed, tile positions at >= 2 MB strides a
+    # pair may have, bank-conflict slack of an unpadded tile)
+    DEFAULT_TC_TILING = (True, 5, 2)
 
     def __init__(self, nr_bits, gate_bits, fusion_width=0, tensor_cores=True, diagonal=None, kinds=None):
         """kinds: per gate, KIND_DIAGONAL for gates whose matrix is always
@@ -324,6 +327,7 @@ class Plan:
         self.ngates = len(ks)
         self.tensor_cores = bool(tensor_cores)
         check(L.q1g_plan_set_tensor_cores(h, 1 if tensor_cores else 0), "plan_set_tensor_cores")
+        self.tc_tiling = self.DEFAULT_TC_TILING
         if kinds is None and diagonal is not None:
             kinds = [self.KIND_DIAGONAL if d else self.KIND_GENERAL for d in diagonal]
         if kinds is not None and any(kinds):
@@ -334,6 +338,12 @@ class Plan:
     @property
     def handle(self):
         return self._h
+
+    def set_tc_tiling(self, allow_pairs=True, max_high_positions=5, conflict_slack=2):
+        """Tiling of the tensor-core passes (q1g_plan_set_tc_tiling)."""
+        check(_lib.load().q1g_plan_set_tc_tiling(self.handle, 1 if allow_pairs else 0, int(max_high_positions),
+                                                 int(conflict_slack)), "plan_set_tc_tiling")
+        self.tc_tiling = (bool(allow_pairs), int(max_high_positions), int(conflict_slack))
 
     @property
     def nblocks(self):

@@ -45,6 +45,12 @@ def test_null_arguments_are_errors_not_crashes(lib):
     with pytest.raises(_lib.InvalidArgument) as ei:
         Plan(3, [[0]], fusion_width=7)
     assert ei.value.payload == ()
+    p = Plan(3, [[0]], fusion_width=2)
+    p.set_tc_tiling(False, 8, 4)
+    assert p.tc_tiling == (False, 8, 4)
+    for bad in ((True, 13, 2), (True, 5, 0), (True, -1, 2)):
+        with pytest.raises(_lib.InvalidArgument):
+            p.set_tc_tiling(*bad)
 
 
 def _commutes_ok(gate_bits, blocks):

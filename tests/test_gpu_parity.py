@@ -984,6 +984,33 @@ def test_autotuned_circuit_matches_oracle():
     assert 1 - abs(np.vdot(ref, out)) ** 2 / np.linalg.norm(out) ** 2 <= 1e-9
     assert len(autotune.tune.last_timings) >= 5
     assert autotune.tune.last_timings[0]["seconds"] <= autotune.tune.last_timings[-1]["seconds"]
+    # the tensor-core tilings were among the candidates timed
+    tilings = {(t["pairs"], t["max_high_positions"], t["conflict_slack"]) for t in autotune.tune.last_timings}
+    assert set(autotune.TC_TILINGS) <= tilings
+
+
+@pytest.mark.parametrize("tiling", [(True, 5, 2), (False, 5, 2), (True, 8, 2), (True, 5, 4), (True, 12, 64)])
+def test_tc_tilings_match_oracle(tiling):
+    """Every tensor-core tiling (pairs or not, pairs over more large pages,
+    unpadded tiles kept at more bank conflicts) gives the oracle's state."""
+    rng = np.random.default_rng(31)
+    n = 19
+    gl = [random_gate(n, rng) for _ in range(80)]
+    bits = [b for _, b in gl]
+    mats = np.concatenate([np.ascontiguousarray(gt.matrix()).ravel() for gt, _ in gl]).view(np.float64)
+    amps = rand_state(n, rng)
+    o = orc.OracleState.from_amplitudes(amps, 1)
+    for gt, b in gl:
+        o.apply_gate(gt.matrix(), b)
+    plan = Plan(n, bits, 5)
+    plan.set_tc_tiling(*tiling)
+    g = VectorState.from_amplitudes(amps, 1, "c64")
+    g.profile(True)
+    g.apply_plan(plan, mats)
+    assert g.profile_report()["fused_tc_c64"]["launches"] > 0
+    want, got = o.states()[:, 0], g.states()[:, 0]
+    assert np.max(np.abs(got - want)) <= TOL64
+    assert 1 - abs(np.vdot(want, got)) ** 2 <= 1e-6
 
 
 def test_tensor_core_plan_with_many_tiles_per_sm_matches_oracle():
