@@ -18,8 +18,9 @@ from .vectorstate import Plan, VectorState
 
 DEFAULT_TILING = Plan.DEFAULT_TC_TILING
 # tensor-core tilings tried beside the default at the widest fusion width:
-# no pairs; pairs over more large pages; a looser conflict slack
-TC_TILINGS = (DEFAULT_TILING, (False, 5, 2), (True, 8, 2), (True, 5, 4))
+# pairs through registers (warp shuffles) instead of the staged tile; no
+# pairs; pairs over more large pages; a looser conflict slack
+TC_TILINGS = (DEFAULT_TILING, (2, 5, 2), (0, 5, 2), (1, 8, 2), (1, 5, 4))
 
 # (fusion width, dense complex64 blocks on tensor cores, tiling)
 CANDIDATES_C64 = tuple((5, True, t) for t in TC_TILINGS) + (

@@ -743,7 +743,8 @@ constexpr int kMinTcRunBits = 7;
 constexpr int kHighPosition = 18;
 
 static TcPass lower_tc_pass(const std::vector<const std::vector<cd>*>& mats,
-                            const std::vector<const std::vector<int>*>& bits, int nbits, uint64_t ncols, int slack)
+                            const std::vector<const std::vector<int>*>& bits, int nbits, uint64_t ncols, int slack,
+                            bool shuffle)
 {
     TcPass t;
     const std::vector<int> T = tile_positions(bits, nbits);
@@ -792,6 +793,22 @@ static TcPass lower_tc_pass(const std::vector<const std::vector<cd>*>& mats,
             G.jgate[g] = jc;
         }
         G.vec2 = G.jgate[1] == 1u ? 1u : 0u;
+    }
+    t.offs.shuffle = 0;
+    int reg1[5];
+    if (mats.size() == 2 && shuffle && tc_shuffle_layout(t.offs.blk[0], t.offs.blk[1], t.offs.swap_lane, reg1)) {
+        // the second block takes the first block's results in registers:
+        // its image in their order, matrix index bit k = tile bit reg1[k]
+        t.offs.shuffle = 1;
+        std::vector<int> q2(5);
+        for (int k = 0; k < 5; ++k) q2[4 - k] = nbits - 1 - T[reg1[k]];
+        const auto m32 = embed_matrix(*mats[1], *bits[1], q2);
+        std::vector<double> md(2 * 32 * 32);
+        for (size_t e = 0; e < m32.size(); ++e) {
+            md[2 * e] = m32[e].real();
+            md[2 * e + 1] = m32[e].imag();
+        }
+        build_tc_image(md.data(), t.images.data() + kTcImageHalves, kTcLastBScaleLog2);
     }
     tc_choose_padding(t.offs, t.box.usable != 0, slack);
     return t;
@@ -1051,16 +1068,26 @@ void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n, bool subs
     auto lower_tc_cached = [&](size_t i, int nblk) -> TcPass {
         if (p->tc_memo.size() != 2 * nb) p->tc_memo.assign(2 * nb, TcPassMemo{});
         TcPassMemo& e = p->tc_memo[2 * i + (size_t)(nblk - 1)];
-        bool hit = e.nblocks == nblk && e.nbits == s->nbits && e.ncols == s->ncols && e.slack == p->tc_slack;
+        const int variant = 4 * p->tc_slack + p->tc_pairs;
+        bool hit = e.nblocks == nblk && e.nbits == s->nbits && e.ncols == s->ncols && e.slack == variant;
         for (int j = 0; hit && j < nblk; ++j) hit = e.bits[j] == bbits[i + j] && e.mats[j] == bmats[i + j];
         if (!hit) {
-            if (nblk == 2)
+            if (nblk == 2) {
                 e.pass = lower_tc_pass({&bmats[i], &bmats[i + 1]}, {&bbits[i], &bbits[i + 1]}, s->nbits, s->ncols,
-                                       p->tc_slack);
-            else
-                e.pass = lower_tc_pass({&bmats[i]}, {&bbits[i]}, s->nbits, s->ncols, p->tc_slack);
+                                       p->tc_slack, p->tc_pairs == 2);
+                if (e.pass.offs.shuffle && e.pass.offs.pad_shift < 31) {
+                    // the shuffled row layout needs padding (bank conflicts);
+                    // the staged one, free to order its rows, may not: one
+                    // tensor-map copy per tile is kept if it can be
+                    TcPass staged =
+                        lower_tc_pass({&bmats[i], &bmats[i + 1]}, {&bbits[i], &bbits[i + 1]}, s->nbits, s->ncols,
+                                      p->tc_slack, false);
+                    if (staged.offs.pad_shift >= 31) e.pass = std::move(staged);
+                }
+            } else
+                e.pass = lower_tc_pass({&bmats[i]}, {&bbits[i]}, s->nbits, s->ncols, p->tc_slack, false);
             e.nblocks = nblk;
-            e.slack = p->tc_slack;
+            e.slack = variant;
             e.nbits = s->nbits;
             e.ncols = s->ncols;
             for (int j = 0; j < nblk; ++j) {

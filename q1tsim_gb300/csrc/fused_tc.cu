@@ -394,35 +394,82 @@ __device__ __forceinline__ void split_store_half(const float2 (&x)[32], float sc
     tmem_st32(tl + 32u * HH, v);
 }
 
-// The whole row's D_main + 2^-11 D_corr back into the stage, all four TMEM
-// loads in flight before the one wait.  UNSCALE (last block of a pass):
-// times `unscale`, which undoes the operands' powers of two; otherwise the
-// amplitudes stay scaled for the next block (whose B is not scaled).
+// The whole row's D_main + 2^-11 D_corr back into the stage, half a row per
+// TMEM wait.  UNSCALE (last block of a pass): times `unscale`, which undoes
+// the operands' powers of two; otherwise the amplitudes stay scaled for the
+// next block (whose B is not scaled).
 template <bool UNSCALE>
 __device__ __forceinline__ void writeback_row(uint8_t* raw, uint32_t rowb, const TcBlockGeom& G, uint32_t tl,
                                               float unscale)
 {
-    uint32_t dm[64], dc[64];
-    tmem_ld32(tl + 128u, dm);
-    tmem_ld32(tl + 192u, dc);
-    tmem_ld32(tl + 160u, dm + 32);
-    tmem_ld32(tl + 224u, dc + 32);
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-    for (int j = 0; j < 64; ++j) {
-        const float d = __fmaf_rn(__uint_as_float(dc[j]), kLoUnscale, __uint_as_float(dm[j]));
-        dm[j] = __float_as_uint(UNSCALE ? d * unscale : d);
+    for (int hh = 0; hh < 2; ++hh) {
+        uint32_t dm[32], dc[32];
+        tmem_ld32(tl + 128u + 32u * hh, dm);
+        tmem_ld32(tl + 192u + 32u * hh, dc);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            const float d = __fmaf_rn(__uint_as_float(dc[j]), kLoUnscale, __uint_as_float(dm[j]));
+            dm[j] = __float_as_uint(UNSCALE ? d * unscale : d);
+        }
+        if (G.vec2) {
+#pragma unroll
+            for (int m = 0; m < 8; ++m)
+                *(float4*)(raw + rowb + G.gateoff[16 * hh + 2 * m]) =
+                    make_float4(__uint_as_float(dm[4 * m]), __uint_as_float(dm[4 * m + 1]),
+                                __uint_as_float(dm[4 * m + 2]), __uint_as_float(dm[4 * m + 3]));
+        } else {
+#pragma unroll
+            for (int j = 0; j < 16; ++j)
+                *(float2*)(raw + rowb + G.gateoff[16 * hh + j]) =
+                    make_float2(__uint_as_float(dm[2 * j]), __uint_as_float(dm[2 * j + 1]));
+        }
     }
-    if (G.vec2) {
+}
+
+// The first block's results of a shuffled pair, kept in registers:
+// D_main + 2^-11 D_corr of the row, still scaled for the second block.
+__device__ __forceinline__ void writeback_regs(uint32_t tl, float2 (&x)[32])
+{
 #pragma unroll
-        for (int m = 0; m < 16; ++m)
-            *(float4*)(raw + rowb + G.gateoff[2 * m]) =
-                make_float4(__uint_as_float(dm[4 * m]), __uint_as_float(dm[4 * m + 1]), __uint_as_float(dm[4 * m + 2]),
-                            __uint_as_float(dm[4 * m + 3]));
-    } else {
+    for (int hh = 0; hh < 2; ++hh) {
+        uint32_t dm[32], dc[32];
+        tmem_ld32(tl + 128u + 32u * hh, dm);
+        tmem_ld32(tl + 192u + 32u * hh, dc);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-        for (int j = 0; j < 32; ++j)
-            *(float2*)(raw + rowb + G.gateoff[j]) = make_float2(__uint_as_float(dm[2 * j]), __uint_as_float(dm[2 * j + 1]));
+        for (int j = 0; j < 16; ++j)
+            x[16 * hh + j] = make_float2(__fmaf_rn(__uint_as_float(dc[2 * j]), kLoUnscale, __uint_as_float(dm[2 * j])),
+                                         __fmaf_rn(__uint_as_float(dc[2 * j + 1]), kLoUnscale,
+                                                   __uint_as_float(dm[2 * j + 1])));
+    }
+}
+
+// Register bit a of every row swaps roles with lane bit swap_lane[a] (when
+// >= 0): a lane whose bit is 0 keeps its registers with bit a = 0 and sends
+// those with bit a = 1 to its partner lane, which sends back its registers
+// with bit a = 0.  Afterwards each thread holds its row of the second block,
+// in that block's gate order.
+__device__ __forceinline__ void swap_reg_lane_bits(float2 (&x)[32], const int32_t* swap_lane, uint32_t lane)
+{
+#pragma unroll
+    for (int a = 0; a < 5; ++a) {
+        const int bl = swap_lane[a];
+        if (bl < 0) continue;
+        const uint32_t m = 1u << bl;
+        const bool up = (lane & m) != 0;
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            if (j & (1 << a)) continue;
+            const int j1 = j | (1 << a);
+            const float2 send = up ? x[j] : x[j1];
+            float2 got;
+            got.x = __shfl_xor_sync(0xffffffffu, send.x, m);
+            got.y = __shfl_xor_sync(0xffffffffu, send.y, m);
+            if (up) x[j] = got;
+            else x[j1] = got;
+        }
     }
 }
 
@@ -583,18 +630,21 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, const __grid_constant__ Inde
             if (group_any(!wait_phase(sbase + kOffFull + 8 * s, u & 1u, abort_flag, offs.wait_ns), gbar)) break;
             uint8_t* raw = smem + raw0 + s * sbytes;
             bool stop = false;
+            const bool shuf = offs.shuffle != 0;
+            float2 x[32];
 #pragma unroll
             for (int b = 0; b < 2; ++b) {
                 if ((uint32_t)b >= nblocks) break;
                 const TcBlockGeom& G = offs.blk[b];
                 const uint32_t rowb = b ? rowb1 : rowb0;
-                if (b > 0) group_sync(gbar);    // the previous block's results are all staged
+                // the previous block's results are all staged (or, shuffled,
+                // already in this thread's registers)
+                if (b > 0 && !shuf) group_sync(gbar);
                 const uint32_t bb = sbase + kOffB + (uint32_t)b * kBImage;
                 // row t -> hi/lo operands in TMEM: every load of the row is
                 // issued first; after the first half is stored, its two
                 // K-steps' MMAs run while the second half converts
-                float2 x[32];
-                load_row(raw, rowb, G, x);
+                if (b == 0 || !shuf) load_row(raw, rowb, G, x);
                 if (b == 0) split_store_half<0, true>(x, offs.ascale, tl);
                 else split_store_half<0, false>(x, offs.ascale, tl);
                 asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
@@ -624,8 +674,14 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, const __grid_constant__ Inde
                 }
                 ++mph;
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                if ((uint32_t)b + 1 == nblocks) writeback_row<true>(raw, rowb, G, tl, offs.unscale);
-                else writeback_row<false>(raw, rowb, G, tl, offs.unscale);
+                if ((uint32_t)b + 1 == nblocks) {
+                    writeback_row<true>(raw, rowb, G, tl, offs.unscale);
+                } else if (shuf) {
+                    writeback_regs(tl, x);
+                    swap_reg_lane_bits(x, offs.swap_lane, (uint32_t)lane);
+                } else {
+                    writeback_row<false>(raw, rowb, G, tl, offs.unscale);
+                }
                 asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             }
             if (stop) break;
@@ -720,6 +776,7 @@ void tc_choose_padding(TcOffsets& o, bool tma_ok, int conflict_slack)
     static std::mutex mu;
     static std::unordered_map<std::string, Choice> memo;
     std::string key(1, tma_ok ? 'T' : 'P');
+    key.append(1, o.shuffle ? 'S' : 'N');
     key.append((const char*)&conflict_slack, sizeof(conflict_slack));
     key.append((const char*)&o.nblocks, sizeof(o.nblocks));
     key.append((const char*)&o.run_bits, sizeof(o.run_bits));
@@ -740,6 +797,8 @@ void tc_choose_padding(TcOffsets& o, bool tma_ok, int conflict_slack)
     if (!found) {
         // candidates: unpadded, then 16 B every 2^pad amplitudes (fewest
         // pieces first); per block the row order that suits the padding best
+        // (a shuffled pass keeps its row layout: only block 0 reads the stage
+        // and only block 1 writes it)
         const uint32_t cands[] = {31, 11, 10, 9, 8, 7, 6, 5};
         long best = -1, ideal = 0;
         for (uint32_t b = 0; b < o.nblocks; ++b) ideal += o.blk[b].vec2 ? 16 * 4 : 32 * 2;
@@ -747,8 +806,14 @@ void tc_choose_padding(TcOffsets& o, bool tma_ok, int conflict_slack)
             if (pad < 31 && tma_ok && best >= 0 && best <= conflict_slack * ideal) break;   // keep the tensor-map copy
             long cost = 0;
             uint32_t order[2][7] = {};
-            for (uint32_t b = 0; b < o.nblocks; ++b)
-                cost += (o.blk[b].vec2 ? 16 : 32) * best_row_order(o.blk[b], pad, order[b]);
+            for (uint32_t b = 0; b < o.nblocks; ++b) {
+                if (o.shuffle) {
+                    std::memcpy(order[b], o.blk[b].jrow_bit, sizeof(order[b]));
+                    cost += (o.blk[b].vec2 ? 16 : 32) * warp_wavefronts(order[b], pad, o.blk[b].vec2 ? 16 : 8);
+                } else {
+                    cost += (o.blk[b].vec2 ? 16 : 32) * best_row_order(o.blk[b], pad, order[b]);
+                }
+            }
             if (best < 0 || cost < best) {
                 best = cost;
                 ch.pad = pad;
@@ -774,6 +839,61 @@ void tc_choose_padding(TcOffsets& o, bool tma_ok, int conflict_slack)
         }
         for (int g = 0; g < 32; ++g) G.gateoff[g] = staged_offset(G.jgate[g], best_pad);
     }
+}
+
+bool tc_shuffle_layout(TcBlockGeom& b0, TcBlockGeom& b1, int32_t* swap_lane, int* reg1)
+{
+    // register bit k of block 0 holds tile bit r0[k]; block 1's gates are the
+    // tile bits set in its jgate table
+    int r0[5];
+    uint32_t gates0 = 0, gates1 = 0;
+    for (int k = 0; k < 5; ++k) {
+        r0[k] = __builtin_ctz(b0.jgate[1 << k]);
+        gates0 |= 1u << r0[k];
+        gates1 |= b1.jgate[1 << k];
+    }
+    if (__builtin_popcount(gates0) != 5 || __builtin_popcount(gates1) != 5) return false;
+    std::vector<int> s1, s2, common;   // leaving the gates, entering them, rows of both
+    for (int j = 0; j < 12; ++j) {
+        const bool in0 = (gates0 >> j) & 1u, in1 = (gates1 >> j) & 1u;
+        if (in0 && !in1) s1.push_back(j);
+        if (in1 && !in0) s2.push_back(j);
+        if (!in0 && !in1) common.push_back(j);
+    }
+    const int s = (int)s1.size();
+    if ((int)s2.size() != s || (int)common.size() != 7 - s) return false;
+    // lanes: the lowest common rows first (one warp phase reads them as
+    // contiguous amplitudes), the bits that swap at the top; the two other
+    // common rows select the warp
+    int lane0[5], lane1[5];
+    for (int b = 0; b < 5 - s; ++b) lane0[b] = lane1[b] = common[b];
+    for (int i = 0; i < s; ++i) {
+        lane0[5 - s + i] = s2[i];
+        lane1[5 - s + i] = s1[i];
+    }
+    for (int k = 0; k < 5; ++k) {
+        swap_lane[k] = -1;
+        reg1[k] = r0[k];
+    }
+    for (int i = 0; i < s; ++i)
+        for (int k = 0; k < 5; ++k)
+            if (r0[k] == s1[i]) {
+                swap_lane[k] = 5 - s + i;
+                reg1[k] = s2[i];
+            }
+    for (int b = 0; b < 5; ++b) {
+        b0.jrow_bit[b] = 1u << lane0[b];
+        b1.jrow_bit[b] = 1u << lane1[b];
+    }
+    for (int w = 0; w < 2; ++w) b0.jrow_bit[5 + w] = b1.jrow_bit[5 + w] = 1u << common[5 - s + w];
+    for (int g = 0; g < 32; ++g) {
+        uint32_t jc = 0;
+        for (int k = 0; k < 5; ++k)
+            if ((g >> k) & 1) jc |= 1u << reg1[k];
+        b1.jgate[g] = jc;
+    }
+    b1.vec2 = b1.jgate[1] == 1u ? 1u : 0u;
+    return true;
 }
 
 void build_tc_image(const double* m, uint16_t* image, int scale_log2)

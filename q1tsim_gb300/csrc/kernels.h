@@ -113,6 +113,14 @@ struct TcOffsets {
     // as f16 times ascale; (D_main + 2^-11 D_corr) * unscale after the last
     float ascale;
     float unscale;
+    // Two-block passes whose second block takes the first block's results
+    // from registers (a plan's pair mode 2): the rows are laid out so that the tile bits that
+    // change between gate and row role are lane bits, and register bit a of
+    // a row swaps with lane bit swap_lane[a] (-1: kept) by warp shuffles.
+    // The second block's gate order (its image, gateoff) is the register
+    // order after the swaps.
+    uint32_t shuffle;
+    int32_t swap_lane[5];
     uint32_t pad1_;
     uint64_t wait_ns;        // longest any wait may last (set by launch_fused_tc)
     uint64_t run_off[32];
@@ -137,6 +145,13 @@ TcTileBox tc_tile_box(const int* tile_pos /* 12, ascending */, int nbits, uint64
 // its conflicts stay within conflict_slack times the minimum: one tensor copy
 // per tile beats padded piece copies.
 void tc_choose_padding(TcOffsets& offs, bool tma_ok, int conflict_slack = 2);
+// Row layout of a shuffled two-block pass (TcOffsets::shuffle): from block
+// 0's gate order (jgate) and block 1's gate set, sets both blocks' row bits
+// (lanes: the lowest common rows, then the bits that swap; warps: the other
+// two common rows), swap_lane[k] for block 0's register bits, and block 1's
+// gate order after the swaps (jgate, vec2), its register bit k holding tile
+// bit reg1[k].  False if the blocks do not have five gate bits each.
+bool tc_shuffle_layout(TcBlockGeom& b0, TcBlockGeom& b1, int32_t* swap_lane, int* reg1);
 // d_bimage: nblocks consecutive 16 KB f16 hi/lo images of the blocks' real
 // 64x64 embeddings in the kernel's swizzled layout; d_err: set to 1 if a
 // bounded wait expired.  wait_ns: longest any of the kernel's waits may

@@ -304,9 +304,10 @@ class Plan:
     """A gate sequence lowered once: structure, fusion grouping, passes."""
 
     KIND_GENERAL, KIND_DIAGONAL, KIND_SWAP = 0, 1, 2
-    # (pairs of blocks per pass allowed, tile positions at >= 2 MB strides a
-    # pair may have, bank-conflict slack of an unpadded tile)
-    DEFAULT_TC_TILING = (True, 5, 2)
+    # (pairs of blocks per pass: 0 none, 1 through the staged tile, 2 through
+    # registers; tile positions at >= 2 MB strides a pair may have;
+    # bank-conflict slack of an unpadded tile)
+    DEFAULT_TC_TILING = (1, 5, 2)
 
     def __init__(self, nr_bits, gate_bits, fusion_width=0, tensor_cores=True, diagonal=None, kinds=None):
         """kinds: per gate, KIND_DIAGONAL for gates whose matrix is always
@@ -339,11 +340,11 @@ class Plan:
     def handle(self):
         return self._h
 
-    def set_tc_tiling(self, allow_pairs=True, max_high_positions=5, conflict_slack=2):
+    def set_tc_tiling(self, allow_pairs=1, max_high_positions=5, conflict_slack=2):
         """Tiling of the tensor-core passes (q1g_plan_set_tc_tiling)."""
-        check(_lib.load().q1g_plan_set_tc_tiling(self.handle, 1 if allow_pairs else 0, int(max_high_positions),
+        check(_lib.load().q1g_plan_set_tc_tiling(self.handle, int(allow_pairs), int(max_high_positions),
                                                  int(conflict_slack)), "plan_set_tc_tiling")
-        self.tc_tiling = (bool(allow_pairs), int(max_high_positions), int(conflict_slack))
+        self.tc_tiling = (int(allow_pairs), int(max_high_positions), int(conflict_slack))
 
     @property
     def nblocks(self):

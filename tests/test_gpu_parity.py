@@ -989,10 +989,11 @@ def test_autotuned_circuit_matches_oracle():
     assert set(autotune.TC_TILINGS) <= tilings
 
 
-@pytest.mark.parametrize("tiling", [(True, 5, 2), (False, 5, 2), (True, 8, 2), (True, 5, 4), (True, 12, 64)])
+@pytest.mark.parametrize("tiling", [(2, 5, 2), (1, 5, 2), (0, 5, 2), (2, 8, 2), (2, 5, 4), (2, 12, 64), (1, 12, 64)])
 def test_tc_tilings_match_oracle(tiling):
-    """Every tensor-core tiling (pairs or not, pairs over more large pages,
-    unpadded tiles kept at more bank conflicts) gives the oracle's state."""
+    """Every tensor-core tiling (pairs through registers or through the
+    staged tile or none, pairs over more large pages, unpadded tiles kept at
+    more bank conflicts) gives the oracle's state."""
     rng = np.random.default_rng(31)
     n = 19
     gl = [random_gate(n, rng) for _ in range(80)]

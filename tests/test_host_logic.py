@@ -11,6 +11,9 @@
   groups (tests/cpp/batch_tile_check.cpp, same library).
 - swap_run.cu: the swap-run pass replayed on the host against the direct
   permutation (tests/cpp/swap_run_check.cpp, same library).
+- fused_tc.cu: the row layouts and register/lane swaps of shuffled
+  two-block tensor-core passes, replayed on tile coordinates
+  (tests/cpp/shuffle_check.cpp, same library).
 - f16_host.h / fused_tc.cu: binary16 rounding against numpy's float16, the
   f16 image of a block read back through its swizzle, the operand scales and
   the row-norm bound of tensor-core blocks (tests/cpp/tc_image_check.cpp).
@@ -79,6 +82,11 @@ def _link_against_library(gxx, tmp_path, name):
 def test_tile_box_and_padding(gxx, tmp_path):
     out = _run(_link_against_library(gxx, tmp_path, "tile_check"))
     assert "bad 0" in out, out
+
+
+def test_shuffled_pairs_redeal_the_rows(gxx, tmp_path):
+    out = _run(_link_against_library(gxx, tmp_path, "shuffle_check"))
+    assert out.startswith("bad 0"), out
 
 
 def test_batch_warp_tiles(gxx, tmp_path):
