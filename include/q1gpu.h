@@ -235,8 +235,8 @@ int q1g_plan_set_tensor_cores(q1g_plan* p, int enable);
  * qubits fit one 12-position tile share a pass (0: no; 1, the default: the
  * second block reads the first one's results back from the staged tile; 2:
  * from registers, the rows re-dealt by warp shuffles); a pair's tile may hold at
- * most max_high_positions positions at or above 2 MB strides (default 5: at
- * most 32 large pages per tile); an unpadded tile, one tensor-map copy, is
+ * most max_high_positions positions at or above 2 MB strides (default 8: at
+ * most 256 large pages per tile); an unpadded tile, one tensor-map copy, is
  * kept while its shared-memory bank wavefronts stay within conflict_slack
  * times the minimum (default 2), else it is padded and copied in pieces.
  * No counterpart in the reference. */

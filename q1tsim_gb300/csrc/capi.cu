@@ -399,6 +399,7 @@ int q1g_plan_create(size_t nr_bits, size_t ngates, const size_t* ks, const size_
         }
         if (fusion_width > 0) {
             p->blocks = fuse(p->gate_bits, (int)nr_bits, fusion_width);
+            order_blocks_for_tc_pairs(p->blocks, (int)nr_bits, p->tc_max_high);
         } else {
             for (size_t g = 0; g < ngates; ++g) {
                 FusedBlock b;
@@ -435,7 +436,10 @@ int q1g_plan_set_gate_kinds(q1g_plan* p, const unsigned char* kinds, size_t ngat
                 throw Error(Q1G_ERR_INVALID_ARGUMENT, "a swap acts on two qubits");
         }
         p->kinds.assign(kinds, kinds + ngates);
-        if (p->width > 0) p->blocks = fuse_runs(p->gate_bits, p->kinds, p->nbits, p->width);
+        if (p->width > 0) {
+            p->blocks = fuse_runs(p->gate_bits, p->kinds, p->nbits, p->width);
+            order_blocks_for_tc_pairs(p->blocks, p->nbits, p->tc_max_high);
+        }
         p->prefix_known = false;
         p->prefix_plan.reset();
     });

@@ -8,6 +8,7 @@
 
 #include <algorithm>
 #include <memory>
+#include <set>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -288,6 +289,7 @@ void q1g_state::apply_unary_all(const double* mat)
             p->gate_bits.push_back({q});
         }
         p->blocks = fuse(p->gate_bits, nbits, width);
+        order_blocks_for_tc_pairs(p->blocks, nbits, p->tc_max_high);
         unary_plan = std::move(p);
     }
     std::vector<double> mats(8 * (size_t)nbits);
@@ -738,8 +740,9 @@ static int tile_run_bits(const std::vector<int>& T)
 // tensor-map box, unpadded.
 constexpr int kMinTcRunBits = 7;
 // Tile positions at or above this one are 2 MB (a large page) or more apart
-// in complex64; a pair's tile may have q1g_plan::tc_max_high of them (5 by
-// default: at most 32 large pages per tile).
+// in complex64; a pair's tile may have q1g_plan::tc_max_high of them (8 by
+// default: at most 256 large pages per tile; a tile over 512 ran 2.4x
+// slower, one over 256 as fast as any).
 constexpr int kHighPosition = 18;
 
 static TcPass lower_tc_pass(const std::vector<const std::vector<cd>*>& mats,
@@ -812,6 +815,71 @@ static TcPass lower_tc_pass(const std::vector<const std::vector<cd>*>& mats,
     }
     tc_choose_padding(t.offs, t.box.usable != 0, slack);
     return t;
+}
+
+// Whether blocks on qubits qa and qb could share a tensor-core pass: their
+// positions fit one 12-position tile, at most max_high of its positions lie
+// at 2 MB strides or more, and the tile has runs of >= 128 amplitudes or is
+// one tensor-map box (the rule plan_run applies, before any padding choice).
+static bool tc_pairable(const std::vector<int>& qa, const std::vector<int>& qb, int nbits, int max_high)
+{
+    std::vector<int> u = qa;
+    for (int q : qb)
+        if (std::find(u.begin(), u.end(), q) == u.end()) u.push_back(q);
+    if (u.size() > 12 || nbits < 12) return false;
+    const auto T = tile_positions({&qa, &qb}, nbits);
+    int high = 0;
+    for (int p : T) high += p >= kHighPosition;
+    return high <= max_high && (tile_run_bits(T) >= kMinTcRunBits || tc_tile_box(T.data(), nbits, 1).usable);
+}
+
+void order_blocks_for_tc_pairs(std::vector<FusedBlock>& blocks, int nbits, int max_high)
+{
+    // Blocks on disjoint qubits commute.  Take the earliest block whose
+    // predecessors (the last earlier block on each of its qubits) are all
+    // taken, then, if one is ready, the earliest ready block that can share
+    // its tensor-core pass, so that plan_run finds them next to each other.
+    const int m = (int)blocks.size();
+    if (m < 3 || nbits < 12) return;
+    auto candidate = [&](int i) {
+        return !blocks[i].phase_run && !blocks[i].swap_run && blocks[i].qubits.size() >= 3 &&
+               blocks[i].qubits.size() <= 5;
+    };
+    std::vector<std::vector<int>> succ(m);
+    std::vector<int> indeg(m, 0), last(nbits, -1);
+    for (int j = 0; j < m; ++j) {
+        std::vector<int> preds;
+        for (int q : blocks[j].qubits) {
+            if (last[q] >= 0 && std::find(preds.begin(), preds.end(), last[q]) == preds.end()) preds.push_back(last[q]);
+            last[q] = j;
+        }
+        for (int i : preds) succ[i].push_back(j);
+        indeg[j] = (int)preds.size();
+    }
+    std::set<int> ready;
+    for (int j = 0; j < m; ++j)
+        if (indeg[j] == 0) ready.insert(j);
+    std::vector<int> order;
+    auto take = [&](int j) {
+        ready.erase(j);
+        order.push_back(j);
+        for (int k : succ[j])
+            if (--indeg[k] == 0) ready.insert(k);
+    };
+    while (!ready.empty()) {
+        const int a = *ready.begin();
+        take(a);
+        if (!candidate(a)) continue;
+        for (int b : ready)
+            if (candidate(b) && tc_pairable(blocks[a].qubits, blocks[b].qubits, nbits, max_high)) {
+                take(b);
+                break;
+            }
+    }
+    std::vector<FusedBlock> out;
+    out.reserve(m);
+    for (int j : order) out.push_back(std::move(blocks[j]));
+    blocks.swap(out);
 }
 
 static size_t union_size(const std::vector<int>& a, const std::vector<int>& b)

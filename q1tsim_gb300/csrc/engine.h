@@ -244,7 +244,7 @@ struct q1g_plan {
     // 2 MB strides, and how many times the minimum bank wavefronts an
     // unpadded one-box tile may take.
     int tc_pairs = 1;
-    int tc_max_high = 5;
+    int tc_max_high = 8;
     int tc_slack = 2;
     q1g::HostBuf hmats;            // pinned staging of dense matrices
     q1g::DevBuf dmats;
@@ -255,6 +255,10 @@ struct q1g_plan {
 
 namespace q1g {
 void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n, bool subspace_prefix = true);
+// Reorders a plan's blocks (blocks on disjoint qubits commute) so that blocks
+// that can share a tensor-core pass follow each other; max_high as
+// q1g_plan::tc_max_high.
+void order_blocks_for_tc_pairs(std::vector<FusedBlock>& blocks, int nbits, int max_high);
 // noalloc.cu: the sampler whose scratch is a fixed device array.
 void sample_shots_noalloc(const void* d_amps, int precision, size_t nr_bits, const double* d_sorted_uniforms,
                           size_t nshots, uint64_t* d_outcomes, uint64_t* d_words, const size_t* cbits,

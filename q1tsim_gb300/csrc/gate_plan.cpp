@@ -218,7 +218,7 @@ bool intersects(const std::vector<int>& a, const std::vector<int>& b)
 
 }  // namespace
 
-std::vector<FusedBlock> fuse(const std::vector<std::vector<int>>& gate_bits, int nbits, int width)
+std::vector<FusedBlock> fuse_greedy(const std::vector<std::vector<int>>& gate_bits, int nbits, int width)
 {
     std::vector<FusedBlock> out;
     std::vector<FusedBlock> open;  // pairwise disjoint
@@ -287,6 +287,148 @@ std::vector<FusedBlock> fuse(const std::vector<std::vector<int>>& gate_bits, int
     }
     (void)nbits;
     return res;
+}
+
+std::vector<FusedBlock> fuse_windows(const std::vector<std::vector<int>>& gate_bits, int nbits, int width)
+{
+    const int ng = (int)gate_bits.size();
+    std::vector<FusedBlock> out;
+    if (ng == 0) return out;
+    if (width <= 0) return fuse_greedy(gate_bits, nbits, width);
+    // the gates of each qubit in order, and how far each qubit is done
+    std::vector<std::vector<int>> perq(nbits);
+    for (int g = 0; g < ng; ++g)
+        for (int q : gate_bits[g]) perq[q].push_back(g);
+    std::vector<int> ptr(nbits, 0);
+    auto next_of = [&](const std::vector<int>& p, int q) { return p[q] < (int)perq[q].size() ? perq[q][p[q]] : -1; };
+    auto ready = [&](const std::vector<int>& p, int g) {
+        for (int q : gate_bits[g])
+            if (next_of(p, q) != g) return false;
+        return true;
+    };
+    // every gate whose qubits lie in `in` and whose predecessors are done,
+    // taken in a valid order; p advances past them
+    auto absorb = [&](const std::vector<char>& in, const std::vector<int>& qs, std::vector<int>& p,
+                      std::vector<int>* taken) {
+        int count = 0;
+        for (bool progress = true; progress;) {
+            progress = false;
+            for (int q : qs) {
+                for (;;) {
+                    const int g = next_of(p, q);
+                    if (g < 0 || !ready(p, g)) break;
+                    bool inside = true;
+                    for (int x : gate_bits[g]) inside = inside && in[x];
+                    if (!inside) break;
+                    for (int x : gate_bits[g]) ++p[x];
+                    if (taken) taken->push_back(g);
+                    ++count;
+                    progress = true;
+                }
+            }
+        }
+        return count;
+    };
+    int remaining = ng;
+    std::vector<char> in(nbits, 0);
+    while (remaining > 0) {
+        // a ready gate wider than a block goes alone
+        int wide = -1;
+        for (int q = 0; q < nbits && wide < 0; ++q) {
+            const int g = next_of(ptr, q);
+            if (g >= 0 && (int)gate_bits[g].size() > width && ready(ptr, g)) wide = g;
+        }
+        if (wide >= 0) {
+            FusedBlock b;
+            b.qubits = gate_bits[wide];
+            std::sort(b.qubits.begin(), b.qubits.end());
+            b.gates = {wide};
+            for (int x : gate_bits[wide]) ++ptr[x];
+            out.push_back(b);
+            --remaining;
+            continue;
+        }
+        // candidate qubit sets: every window of `width` consecutive qubits,
+        // and for every ready gate the set grown from its qubits by the ready
+        // gates that add the fewest new qubits
+        std::vector<std::vector<int>> cands;
+        for (int a = 0; a + width <= nbits; ++a) {
+            std::vector<int> w;
+            for (int q = a; q < a + width; ++q) w.push_back(q);
+            cands.push_back(w);
+        }
+        if (nbits < width) {
+            std::vector<int> w;
+            for (int q = 0; q < nbits; ++q) w.push_back(q);
+            cands.push_back(w);
+        }
+        for (int q0 = 0; q0 < nbits; ++q0) {
+            const int g0 = next_of(ptr, q0);
+            if (g0 < 0 || !ready(ptr, g0) || gate_bits[g0][0] != q0) continue;
+            std::vector<int> s = gate_bits[g0];
+            std::sort(s.begin(), s.end());
+            std::vector<int> p = ptr;
+            std::fill(in.begin(), in.end(), 0);
+            for (int x : s) in[x] = 1;
+            absorb(in, s, p, nullptr);
+            for (;;) {
+                int best = -1, best_new = width + 1;
+                for (int q = 0; q < nbits; ++q) {
+                    const int g = next_of(p, q);
+                    if (g < 0 || !ready(p, g)) continue;
+                    int add = 0;
+                    for (int x : gate_bits[g]) add += in[x] ? 0 : 1;
+                    if (add == 0 || (int)s.size() + add > width) continue;
+                    if (add < best_new) {
+                        best_new = add;
+                        best = g;
+                    }
+                }
+                if (best < 0) break;
+                for (int x : gate_bits[best])
+                    if (!in[x]) {
+                        in[x] = 1;
+                        s.push_back(x);
+                    }
+                std::sort(s.begin(), s.end());
+                absorb(in, s, p, nullptr);
+            }
+            cands.push_back(s);
+        }
+        // the candidate that absorbs the most gates
+        int best_count = -1;
+        std::vector<int> best_set;
+        for (const auto& c : cands) {
+            std::fill(in.begin(), in.end(), 0);
+            for (int x : c) in[x] = 1;
+            std::vector<int> p = ptr;
+            const int cnt = absorb(in, c, p, nullptr);
+            if (cnt > best_count) {
+                best_count = cnt;
+                best_set = c;
+            }
+        }
+        std::fill(in.begin(), in.end(), 0);
+        for (int x : best_set) in[x] = 1;
+        FusedBlock b;
+        absorb(in, best_set, ptr, &b.gates);
+        if (b.gates.empty()) throw std::logic_error("window fusion made no progress");
+        for (int g : b.gates)
+            for (int x : gate_bits[g])
+                if (std::find(b.qubits.begin(), b.qubits.end(), x) == b.qubits.end()) b.qubits.push_back(x);
+        std::sort(b.qubits.begin(), b.qubits.end());
+        remaining -= (int)b.gates.size();
+        out.push_back(b);
+    }
+    return out;
+}
+
+std::vector<FusedBlock> fuse(const std::vector<std::vector<int>>& gate_bits, int nbits, int width)
+{
+    auto greedy = fuse_greedy(gate_bits, nbits, width);
+    if (width <= 1) return greedy;
+    auto windows = fuse_windows(gate_bits, nbits, width);
+    return windows.size() < greedy.size() ? windows : greedy;
 }
 
 int phase_run_pivot(const FusedBlock& b, const std::vector<std::vector<int>>& gate_bits)

@@ -63,6 +63,18 @@ enum GateKind : unsigned char { kGateGeneral = 0, kGateDiagonal = 1, kGateSwap =
 // emitted first.  A final pass merges an emitted block into an earlier one
 // when every block in between is disjoint from it.  Only the qubit lists are
 // used, so the grouping can be computed once per circuit structure.
+std::vector<FusedBlock> fuse_greedy(const std::vector<std::vector<int>>& gate_bits, int nbits, int width);
+
+// Window fusion: blocks are chosen one at a time, each the qubit set of at
+// most `width` qubits that absorbs the most gates whose predecessors are all
+// done (every gate on its qubits whose own qubits lie in the set, in a valid
+// order).  The candidate sets are the windows of `width` consecutive qubits
+// and, for every ready gate, the set grown from its qubits by the ready gates
+// adding the fewest new qubits.  A gate wider than `width` is a block alone.
+std::vector<FusedBlock> fuse_windows(const std::vector<std::vector<int>>& gate_bits, int nbits, int width);
+
+// The fusion of a gate sequence: of fuse_greedy and fuse_windows, the one
+// with fewer blocks.
 std::vector<FusedBlock> fuse(const std::vector<std::vector<int>>& gate_bits, int nbits, int width);
 
 // Shortest run of consecutive diagonal gates taken as one phase pass.
