@@ -232,9 +232,13 @@ int q1g_plan_run(q1g_plan* p, q1g_state* s, const double* mats_flat, size_t n_do
 int q1g_plan_set_tensor_cores(q1g_plan* p, int enable);
 /* Tiling of the plan's tensor-core passes (tuned per circuit structure by
  * q1tsim_gb300/autotune.py): allow_pairs lets two consecutive blocks whose
- * qubits fit one 12-position tile share a pass (0: no; 1, the default: the
+ * qubits fit one 12-position tile share a pass (0: no; 1: the
  * second block reads the first one's results back from the staged tile; 2:
- * from registers, the rows re-dealt by warp shuffles); a pair's tile may hold at
+ * from registers, the rows re-dealt by warp shuffles; 3: the first block's
+ * write-back stores them as the second block's f16 operands in shared
+ * memory, which its MMAs read directly; 4, the default: the same in a
+ * kernel with four consumer groups, every pass's operands in shared
+ * memory); a pair's tile may hold at
  * most max_high_positions positions at or above 2 MB strides (default 8: at
  * most 256 large pages per tile); an unpadded tile, one tensor-map copy, is
  * kept while its shared-memory bank wavefronts stay within conflict_slack

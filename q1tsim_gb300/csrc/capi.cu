@@ -503,10 +503,14 @@ int q1g_plan_set_tc_tiling(q1g_plan* p, int allow_pairs, int max_high_positions,
             throw Error(Q1G_ERR_INVALID_ARGUMENT, "max_high_positions must be in 0..12");
         if (conflict_slack < 1 || conflict_slack > 64)
             throw Error(Q1G_ERR_INVALID_ARGUMENT, "conflict_slack must be in 1..64");
-        if (allow_pairs < 0 || allow_pairs > 2) throw Error(Q1G_ERR_INVALID_ARGUMENT, "allow_pairs must be 0, 1 or 2");
+        if (allow_pairs < 0 || allow_pairs > 4)
+            throw Error(Q1G_ERR_INVALID_ARGUMENT, "allow_pairs must be in 0..4", (uint64_t)allow_pairs);
         p->tc_pairs = allow_pairs;
         p->tc_max_high = max_high_positions;
         p->tc_slack = conflict_slack;
+        // the compact prefix plan copies the tiling when it is made
+        p->prefix_known = false;
+        p->prefix_plan.reset();
     });
 }
 

@@ -747,8 +747,9 @@ constexpr int kHighPosition = 18;
 
 static TcPass lower_tc_pass(const std::vector<const std::vector<cd>*>& mats,
                             const std::vector<const std::vector<int>*>& bits, int nbits, uint64_t ncols, int slack,
-                            bool shuffle)
+                            int pair_mode)
 {
+    const bool shuffle = pair_mode == 2;
     TcPass t;
     const std::vector<int> T = tile_positions(bits, nbits);
     auto tbit = [&](int pos) { return (int)(std::find(T.begin(), T.end(), pos) - T.begin()); };
@@ -813,7 +814,33 @@ static TcPass lower_tc_pass(const std::vector<const std::vector<cd>*>& mats,
         }
         build_tc_image(md.data(), t.images.data() + kTcImageHalves, kTcLastBScaleLog2);
     }
+    // pair mode 4: the four-group kernel, every A operand in shared memory
+    const bool quad = pair_mode == 4;
+    auto finish = [&] {
+        if (quad) {
+            t.offs.groups = 4;
+            t.offs.stage_bytes = (t.offs.stage_bytes + 1023u) & ~1023u;
+        }
+    };
+    int gbit1[5];
+    if (mats.size() == 2 && (pair_mode == 3 || quad) && tc_direct_layout(t.offs, t.box.usable != 0, slack, gbit1)) {
+        // the second block reads the operands the first block's write-back
+        // scattered: its image in the gate order that layout chose, matrix
+        // index bit k = tile bit gbit1[k]
+        std::vector<int> q2(5);
+        for (int k = 0; k < 5; ++k) q2[4 - k] = nbits - 1 - T[gbit1[k]];
+        const auto m32 = embed_matrix(*mats[1], *bits[1], q2);
+        std::vector<double> md(2 * 32 * 32);
+        for (size_t e = 0; e < m32.size(); ++e) {
+            md[2 * e] = m32[e].real();
+            md[2 * e + 1] = m32[e].imag();
+        }
+        build_tc_image(md.data(), t.images.data() + kTcImageHalves, kTcLastBScaleLog2);
+        finish();
+        return t;
+    }
     tc_choose_padding(t.offs, t.box.usable != 0, slack);
+    finish();
     return t;
 }
 
@@ -1036,6 +1063,9 @@ static size_t run_subspace_prefix(q1g_plan* p, q1g_state* s, const double* mats,
             tp->nbits = na;
             tp->width = p->width;
             tp->tensor_cores = p->tensor_cores;
+            tp->tc_pairs = p->tc_pairs;
+            tp->tc_max_high = p->tc_max_high;
+            tp->tc_slack = p->tc_slack;
             tp->gate_bits = p->gate_bits;
             tp->mat_off = p->mat_off;
             tp->mat_doubles = p->mat_doubles;
@@ -1136,24 +1166,25 @@ void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n, bool subs
     auto lower_tc_cached = [&](size_t i, int nblk) -> TcPass {
         if (p->tc_memo.size() != 2 * nb) p->tc_memo.assign(2 * nb, TcPassMemo{});
         TcPassMemo& e = p->tc_memo[2 * i + (size_t)(nblk - 1)];
-        const int variant = 4 * p->tc_slack + p->tc_pairs;
+        const int variant = 8 * p->tc_slack + p->tc_pairs;
         bool hit = e.nblocks == nblk && e.nbits == s->nbits && e.ncols == s->ncols && e.slack == variant;
         for (int j = 0; hit && j < nblk; ++j) hit = e.bits[j] == bbits[i + j] && e.mats[j] == bmats[i + j];
         if (!hit) {
             if (nblk == 2) {
                 e.pass = lower_tc_pass({&bmats[i], &bmats[i + 1]}, {&bbits[i], &bbits[i + 1]}, s->nbits, s->ncols,
-                                       p->tc_slack, p->tc_pairs == 2);
-                if (e.pass.offs.shuffle && e.pass.offs.pad_shift < 31) {
-                    // the shuffled row layout needs padding (bank conflicts);
-                    // the staged one, free to order its rows, may not: one
-                    // tensor-map copy per tile is kept if it can be
+                                       p->tc_slack, p->tc_pairs);
+                if ((e.pass.offs.shuffle || e.pass.offs.direct) && e.pass.offs.pad_shift < 31) {
+                    // the shuffled or direct row layout needs padding (bank
+                    // conflicts); the staged one, free to order its rows,
+                    // may not: one tensor-map copy per tile is kept if it can
                     TcPass staged =
                         lower_tc_pass({&bmats[i], &bmats[i + 1]}, {&bbits[i], &bbits[i + 1]}, s->nbits, s->ncols,
-                                      p->tc_slack, false);
+                                      p->tc_slack, 1);
                     if (staged.offs.pad_shift >= 31) e.pass = std::move(staged);
                 }
             } else
-                e.pass = lower_tc_pass({&bmats[i]}, {&bbits[i]}, s->nbits, s->ncols, p->tc_slack, false);
+                e.pass = lower_tc_pass({&bmats[i]}, {&bbits[i]}, s->nbits, s->ncols, p->tc_slack,
+                                       p->tc_pairs == 4 ? 4 : 1);
             e.nblocks = nblk;
             e.slack = variant;
             e.nbits = s->nbits;

@@ -211,7 +211,7 @@ struct TcPass {
 struct TcPassMemo {
     int nblocks = 0;
     int nbits = -1;
-    int slack = 0;          // 4 x conflict slack + pair mode the lowering was made for
+    int slack = 0;          // 8 x conflict slack + pair mode the lowering was made for
     uint64_t ncols = 0;
     std::vector<int> bits[2];
     std::vector<std::complex<double>> mats[2];
@@ -240,10 +240,12 @@ struct q1g_plan {
     // Tensor-core tiling (q1g_plan_set_tc_tiling, tuned by autotune.py):
     // whether two blocks may share a pass (0 no; 1 the second block reads
     // the first's results from the staged tile; 2 from registers, by warp
-    // shuffles), how many tile positions a pair's tile may have at or above
+    // shuffles; 3 as operands the first block's write-back stored in the
+    // stage, with no split of its own; 4 the same in the four-group kernel,
+    // whose single-block passes also keep A in shared memory), how many tile positions a pair's tile may have at or above
     // 2 MB strides, and how many times the minimum bank wavefronts an
     // unpadded one-box tile may take.
-    int tc_pairs = 1;
+    int tc_pairs = 4;
     int tc_max_high = 8;
     int tc_slack = 2;
     q1g::HostBuf hmats;            // pinned staging of dense matrices

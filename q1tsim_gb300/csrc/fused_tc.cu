@@ -76,10 +76,24 @@ namespace q1g {
 namespace {
 
 constexpr int kGroupThreads = 128;              // 4 warps: one per TMEM lane quarter
-constexpr int kConsumers = 2 * kGroupThreads;   // warps 0-7
-constexpr int kLoaderWarp = 8;
-constexpr int kStorerWarp0 = 9;                 // storers: warps 9 and 10
-constexpr int kTcThreads = kConsumers + 96;
+// The kernel comes in two shapes, by its number of consumer groups NG:
+//   NG = 2: each group's A operand (of a pass's first block, and of every
+//           block in the staged and shuffled pair modes) in TMEM beside its
+//           accumulators, 256 columns per group;
+//   NG = 4: every A operand in the group's stage in shared memory (the
+//           first block's split writes it there over the tile it has read),
+//           only the accumulators in TMEM, 128 columns per group, so that
+//           four tiles are in flight per SM.
+// Warps 0 .. 4NG-1 are the consumers, then the loader and two storers.
+template <int NG>
+struct TcShape {
+    static constexpr int kLoaderWarp = 4 * NG;
+    static constexpr int kStorerWarp0 = 4 * NG + 1;
+    static constexpr int kThreads = 32 * (4 * NG + 3);
+    static constexpr uint32_t kGroupCols = 512u / NG;
+    static constexpr uint32_t kDCol = NG == 2 ? 128u : 0u;   // D_main within the group's columns
+    static constexpr bool kSmemA = NG == 4;
+};
 constexpr uint32_t kTileBytes = 4096 * 8;        // one tile (complex64), without padding
 constexpr uint32_t kTmemCols = 512;
 constexpr float kLoScale = 2048.0f;     // 2^11: lo halves are stored scaled up
@@ -91,12 +105,18 @@ constexpr uint32_t kMaxStages = 8;
 constexpr uint32_t kOffFull = 0;        // 8 B per stage
 constexpr uint32_t kOffEmpty = 64;
 constexpr uint32_t kOffOut = 128;
-constexpr uint32_t kOffMma = 192;       // one per group
-constexpr uint32_t kOffSlot = 208;
-constexpr uint32_t kOffAbort = 212;
+constexpr uint32_t kOffMma = 192;       // one per group, up to 4
+constexpr uint32_t kOffSlot = 224;
+constexpr uint32_t kOffAbort = 228;
 constexpr uint32_t kOffRunOff = 256;    // 32 x u64
 constexpr uint32_t kOffB = 1024;
 constexpr uint32_t kAlignSlack = 1024;
+static_assert(kOffEmpty >= kOffFull + 8 * kMaxStages && kOffOut >= kOffEmpty + 8 * kMaxStages &&
+                  kOffMma >= kOffOut + 8 * kMaxStages,
+              "stage barriers overlap");
+static_assert(kOffSlot >= kOffMma + 8 * 4 && kOffAbort >= kOffSlot + 4 && kOffRunOff >= kOffAbort + 4 &&
+                  kOffB >= kOffRunOff + 8 * 32,
+              "shared-memory header fields overlap");
 // Longest any wait may last by default (TcOffsets::wait_ns; the caller may
 // shorten it).  Normal waits last microseconds; profiler replays with
 // instrumented instructions slow a launch by four orders of magnitude or
@@ -169,6 +189,21 @@ __device__ __forceinline__ void mma_f16_ts(uint32_t d_tmem, uint32_t a_tmem, uin
         "setp.ne.b32 p, %4, 0;\n\t"
         "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
         "r"(a_tmem), "l"(b), "r"(idesc), "r"(acc));
+}
+
+// D (TMEM) (+)= A (SMEM descriptor) * B (SMEM descriptor)^T
+__device__ __forceinline__ void mma_f16_ss(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void st_shared_u32(uint32_t addr, uint32_t v)
+{
+    asm volatile("st.shared.u32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
 }
 
 __device__ __forceinline__ void mma_commit(uint32_t bar)
@@ -399,14 +434,14 @@ __device__ __forceinline__ void split_store_half(const float2 (&x)[32], float sc
 // the operands' powers of two; otherwise the amplitudes stay scaled for the
 // next block (whose B is not scaled).
 template <bool UNSCALE>
-__device__ __forceinline__ void writeback_row(uint8_t* raw, uint32_t rowb, const TcBlockGeom& G, uint32_t tl,
+__device__ __forceinline__ void writeback_row(uint8_t* raw, uint32_t rowb, const TcBlockGeom& G, uint32_t td,
                                               float unscale)
 {
 #pragma unroll
     for (int hh = 0; hh < 2; ++hh) {
         uint32_t dm[32], dc[32];
-        tmem_ld32(tl + 128u + 32u * hh, dm);
-        tmem_ld32(tl + 192u + 32u * hh, dc);
+        tmem_ld32(td + 32u * hh, dm);
+        tmem_ld32(td + 64u + 32u * hh, dc);
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
@@ -428,15 +463,42 @@ __device__ __forceinline__ void writeback_row(uint8_t* raw, uint32_t rowb, const
     }
 }
 
-// The first block's results of a shuffled pair, kept in registers:
-// D_main + 2^-11 D_corr of the row, still scaled for the second block.
-__device__ __forceinline__ void writeback_regs(uint32_t tl, float2 (&x)[32])
+// The first block's results of a direct pair (TcOffsets::direct): each
+// output amplitude, still scaled, split into hi/lo f16 pairs and stored as
+// the second block's A operand -- hi plane at abase, lo plane 16 KB above --
+// at offset rowpart ^ scat_gate[g].
+__device__ __forceinline__ void writeback_scatter(uint32_t abase, uint32_t rowpart, const uint32_t* scat_gate,
+                                                  uint32_t td)
 {
 #pragma unroll
     for (int hh = 0; hh < 2; ++hh) {
         uint32_t dm[32], dc[32];
-        tmem_ld32(tl + 128u + 32u * hh, dm);
-        tmem_ld32(tl + 192u + 32u * hh, dc);
+        tmem_ld32(td + 32u * hh, dm);
+        tmem_ld32(td + 64u + 32u * hh, dc);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            const float2 d = make_float2(__fmaf_rn(__uint_as_float(dc[2 * j]), kLoUnscale, __uint_as_float(dm[2 * j])),
+                                         __fmaf_rn(__uint_as_float(dc[2 * j + 1]), kLoUnscale,
+                                                   __uint_as_float(dm[2 * j + 1])));
+            uint32_t hi, lo;
+            split_amp<false>(d, 1.0f, hi, lo);
+            const uint32_t a = abase + (rowpart ^ scat_gate[16 * hh + j]);
+            st_shared_u32(a, hi);
+            st_shared_u32(a + 16384u, lo);
+        }
+    }
+}
+
+// The first block's results of a shuffled pair, kept in registers:
+// D_main + 2^-11 D_corr of the row, still scaled for the second block.
+__device__ __forceinline__ void writeback_regs(uint32_t td, float2 (&x)[32])
+{
+#pragma unroll
+    for (int hh = 0; hh < 2; ++hh) {
+        uint32_t dm[32], dc[32];
+        tmem_ld32(td + 32u * hh, dm);
+        tmem_ld32(td + 64u + 32u * hh, dc);
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
         for (int j = 0; j < 16; ++j)
@@ -485,11 +547,49 @@ __device__ __forceinline__ void issue_mma_ksteps(uint32_t tm, uint32_t bb, int k
         mma_f16_ts(tm + 192u, tm + 16u * ks + 8u, desc_sw128(bb + (uint32_t)ks * 32u), kIdescN64, 1u);
 }
 
-__global__ void __launch_bounds__(kTcThreads, 1)
+// The MMAs of K-steps k0 and k0+1 with A in shared memory at abase (hi
+// plane, then the lo plane 16 KB above, K-major SWIZZLE_128B): D_main at
+// TMEM column td, D_corr at td + 64.
+__device__ __forceinline__ void issue_mma_smem_ksteps(uint32_t td, uint32_t abase, uint32_t bb, int k0)
+{
+#pragma unroll
+    for (int ks = k0; ks < k0 + 2; ++ks)
+        mma_f16_ss(td, desc_sw128(abase + (uint32_t)ks * 32u), desc_sw128(bb + (uint32_t)ks * 32u), kIdescN128,
+                   ks > 0 ? 1u : 0u);
+#pragma unroll
+    for (int ks = k0; ks < k0 + 2; ++ks)
+        mma_f16_ss(td + 64u, desc_sw128(abase + 16384u + (uint32_t)ks * 32u), desc_sw128(bb + (uint32_t)ks * 32u),
+                   kIdescN64, 1u);
+}
+
+// Half HH of a loaded row (gates 16HH .. 16HH+15) split into hi/lo f16
+// pairs and stored as row t of the A operand in shared memory: 16-byte
+// chunk c (gates 4c .. 4c+3) of each plane at its SWIZZLE_128B place.
+template <int HH, bool SCALE>
+__device__ __forceinline__ void split_store_smem(const float2 (&x)[32], float sc, uint32_t arow, uint32_t t)
+{
+#pragma unroll
+    for (int c = 4 * HH; c < 4 * HH + 4; ++c) {
+        uint32_t hi[4], lo[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) split_amp<SCALE>(x[4 * c + e], sc, hi[e], lo[e]);
+        const uint32_t a = arow + ((((uint32_t)c ^ t) & 7u) << 4);
+        asm volatile("st.shared.v4.u32 [%0], {%1, %2, %3, %4};" ::"r"(a), "r"(hi[0]), "r"(hi[1]), "r"(hi[2]),
+                     "r"(hi[3])
+                     : "memory");
+        asm volatile("st.shared.v4.u32 [%0], {%1, %2, %3, %4};" ::"r"(a + 16384u), "r"(lo[0]), "r"(lo[1]),
+                     "r"(lo[2]), "r"(lo[3])
+                     : "memory");
+    }
+}
+
+template <int NG>
+__global__ void __launch_bounds__(TcShape<NG>::kThreads, 1)
 k_fused_tc(float2* __restrict__ a, uint64_t ntiles, const __grid_constant__ IndexMap tilemap,
            const __grid_constant__ TcOffsets offs, const __grid_constant__ CUtensorMap tmap,
            const uint4* __restrict__ bimage, int* __restrict__ err)
 {
+    using Sh = TcShape<NG>;
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     const uint32_t sbase = smem_addr(smem);
@@ -504,7 +604,7 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, const __grid_constant__ Inde
     {
         uint4* dst = (uint4*)(smem + kOffB);
         const uint32_t n16 = nblocks * kBImage / 16;
-        for (uint32_t i = tid; i < n16; i += kTcThreads) dst[i] = bimage[i];
+        for (uint32_t i = tid; i < n16; i += Sh::kThreads) dst[i] = bimage[i];
         if (tid < 32) run_off[tid] = offs.run_off[tid];
     }
     if (tid == 0) {
@@ -513,8 +613,7 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, const __grid_constant__ Inde
             mbar_init(sbase + kOffEmpty + 8 * s, 1);
             mbar_init(sbase + kOffOut + 8 * s, kGroupThreads);
         }
-        mbar_init(sbase + kOffMma, 1);
-        mbar_init(sbase + kOffMma + 8, 1);
+        for (int g = 0; g < NG; ++g) mbar_init(sbase + kOffMma + 8 * g, 1);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -534,7 +633,7 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, const __grid_constant__ Inde
     const uint32_t piece_bytes = 8u << pb;
     const uint64_t run_mask = (uint64_t(1) << rb) - 1u;
 
-    if (warp == kLoaderWarp) {
+    if (warp == Sh::kLoaderWarp) {
         // ---------------------------------------------------------- loader
         uint32_t s = 0, u = 0;
         uint64_t issued = 0;
@@ -573,13 +672,18 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, const __grid_constant__ Inde
         const uint64_t from = issued > nst ? issued - nst : 0;
         for (uint64_t i = from; i < issued; ++i)
             drain_phase(sbase + kOffFull + 8 * (uint32_t)(i % nst), (uint32_t)((i / nst) & 1));
-    } else if (warp >= kStorerWarp0) {
+    } else if (warp >= Sh::kStorerWarp0) {
         // --------------------------------------------------------- storers
         // storer w takes tiles w, w+2, ...; after its store has read the
-        // stage it frees the stage at once
-        const uint32_t w = (uint32_t)(warp - kStorerWarp0);
+        // stage it frees the stage at once.  A parity wait on the stage's
+        // out phase u is only unambiguous once phase u-1 has completed; with
+        // an odd number of stages the stage's previous use is the other
+        // storer's tile, so first wait until that tile has been stored (the
+        // stage's empty phase u-1; it follows its out phase u-1)
+        const uint32_t w = (uint32_t)(warp - Sh::kStorerWarp0);
         uint32_t s = w, u = 0;
         for (uint64_t i = w; i < my_tiles; i += 2) {
+            if (u > 0 && !wait_phase(sbase + kOffEmpty + 8 * s, (u - 1) & 1u, abort_flag, offs.wait_ns)) break;
             if (!wait_phase(sbase + kOffOut + 8 * s, u & 1u, abort_flag, offs.wait_ns)) break;
             const uint64_t tile = blockIdx.x + i * gridDim.x;
             const uint32_t st = sbase + raw0 + s * sbytes;
@@ -615,22 +719,35 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, const __grid_constant__ Inde
         const uint32_t t = 32u * q + (uint32_t)lane;       // row = TMEM lane
         const bool issuer = t == 0;
         const uint32_t gbar = 1u + g;
-        const uint32_t tm = tmem + 256u * g;                // the group's columns
+        const uint32_t tm = tmem + Sh::kGroupCols * g;      // the group's columns
         const uint32_t tl = tm + ((32u * q) << 16);         // this warp's lanes
+        const uint32_t td = tl + Sh::kDCol;                 // its accumulators
         const uint32_t mbar = sbase + kOffMma + 8u * g;
-        uint32_t rowb0 = 0, rowb1 = 0;
+        // row t of an A operand in shared memory (SWIZZLE_128B, 128 B rows)
+        const uint32_t arow = (t >> 3) * 1024u + (t & 7u) * 128u;
+        uint32_t rowb0 = 0, rowb1 = 0, rowpart = 0;
 #pragma unroll
         for (int r = 0; r < 7; ++r)
             if ((t >> r) & 1u) {
                 rowb0 += offs.blk[0].rowoff[r];
                 rowb1 += offs.blk[1].rowoff[r];
+                rowpart ^= offs.scat_row[r];
             }
+        const bool direct = offs.direct != 0;
         uint32_t s = g, u = 0, mph = 0;     // tile i lives in stage i % nst
-        for (uint64_t i = g; i < my_tiles; i += 2) {
-            if (group_any(!wait_phase(sbase + kOffFull + 8 * s, u & 1u, abort_flag, offs.wait_ns), gbar)) break;
+        for (uint64_t i = g; i < my_tiles; i += NG) {
+            // the stage's full phase u is unambiguous by parity once phase
+            // u-1 has completed, which its previous tile's store implies
+            // (copies may land out of order); tile i's copy is only issued
+            // after that store, so that wait costs nothing
+            const bool ready =
+                (u == 0 || wait_phase(sbase + kOffEmpty + 8 * s, (u - 1) & 1u, abort_flag, offs.wait_ns)) &&
+                wait_phase(sbase + kOffFull + 8 * s, u & 1u, abort_flag, offs.wait_ns);
+            if (group_any(!ready, gbar)) break;
             uint8_t* raw = smem + raw0 + s * sbytes;
+            const uint32_t abase = smem_addr(raw);
             bool stop = false;
-            const bool shuf = offs.shuffle != 0;
+            const bool shuf = !Sh::kSmemA && offs.shuffle != 0;
             float2 x[32];
 #pragma unroll
             for (int b = 0; b < 2; ++b) {
@@ -639,30 +756,71 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, const __grid_constant__ Inde
                 const uint32_t rowb = b ? rowb1 : rowb0;
                 // the previous block's results are all staged (or, shuffled,
                 // already in this thread's registers)
-                if (b > 0 && !shuf) group_sync(gbar);
+                if (b > 0 && !shuf && !direct) group_sync(gbar);
                 const uint32_t bb = sbase + kOffB + (uint32_t)b * kBImage;
-                // row t -> hi/lo operands in TMEM: every load of the row is
-                // issued first; after the first half is stored, its two
-                // K-steps' MMAs run while the second half converts
-                if (b == 0 || !shuf) load_row(raw, rowb, G, x);
-                if (b == 0) split_store_half<0, true>(x, offs.ascale, tl);
-                else split_store_half<0, false>(x, offs.ascale, tl);
-                asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
-                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-                group_sync(gbar);
-                if (issuer) {
-                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                    issue_mma_ksteps(tm, bb, 0);
-                }
-                if (b == 0) split_store_half<1, true>(x, offs.ascale, tl);
-                else split_store_half<1, false>(x, offs.ascale, tl);
-                asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
-                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-                group_sync(gbar);
-                if (issuer) {
-                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                    issue_mma_ksteps(tm, bb, 2);
-                    mma_commit(mbar);
+                if (b > 0 && direct) {
+                    // the first block's write-back left this block's
+                    // operands in the stage: make them visible to the
+                    // tensor cores, then the MMAs
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                    group_sync(gbar);
+                    if (issuer) {
+                        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                        issue_mma_smem_ksteps(td, abase, bb, 0);
+                        issue_mma_smem_ksteps(td, abase, bb, 2);
+                        mma_commit(mbar);
+                    }
+                } else if (Sh::kSmemA) {
+                    // row t -> hi/lo operands over the tile in the stage:
+                    // every load of the group is performed first (the
+                    // barrier), then each half is split, stored and its two
+                    // K-steps' MMAs issued while the second half converts
+                    load_row(raw, rowb, G, x);
+                    group_sync(gbar);
+                    if (b == 0) split_store_smem<0, true>(x, offs.ascale, abase + arow, t);
+                    else split_store_smem<0, false>(x, offs.ascale, abase + arow, t);
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                    group_sync(gbar);
+                    if (issuer) {
+                        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                        issue_mma_smem_ksteps(td, abase, bb, 0);
+                    }
+                    if (b == 0) split_store_smem<1, true>(x, offs.ascale, abase + arow, t);
+                    else split_store_smem<1, false>(x, offs.ascale, abase + arow, t);
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                    group_sync(gbar);
+                    if (issuer) {
+                        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                        issue_mma_smem_ksteps(td, abase, bb, 2);
+                        mma_commit(mbar);
+                    }
+                } else {
+                    // row t -> hi/lo operands in TMEM: every load of the row is
+                    // issued first; after the first half is stored, its two
+                    // K-steps' MMAs run while the second half converts
+                    if (b == 0 || !shuf) load_row(raw, rowb, G, x);
+                    if (b == 0) split_store_half<0, true>(x, offs.ascale, tl);
+                    else split_store_half<0, false>(x, offs.ascale, tl);
+                    asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+                    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                    group_sync(gbar);
+                    if (issuer) {
+                        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                        issue_mma_ksteps(tm, bb, 0);
+                    }
+                    if (b == 0) split_store_half<1, true>(x, offs.ascale, tl);
+                    else split_store_half<1, false>(x, offs.ascale, tl);
+                    asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+                    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                    group_sync(gbar);
+                    if (issuer) {
+                        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                        issue_mma_ksteps(tm, bb, 2);
+                        mma_commit(mbar);
+                    }
                 }
                 if (group_any(!wait_phase(mbar, mph & 1u, abort_flag, offs.wait_ns), gbar)) {
                     // the MMAs were committed (every thread of the group is
@@ -675,19 +833,21 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, const __grid_constant__ Inde
                 ++mph;
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 if ((uint32_t)b + 1 == nblocks) {
-                    writeback_row<true>(raw, rowb, G, tl, offs.unscale);
+                    writeback_row<true>(raw, rowb, G, td, offs.unscale);
                 } else if (shuf) {
-                    writeback_regs(tl, x);
+                    writeback_regs(td, x);
                     swap_reg_lane_bits(x, offs.swap_lane, (uint32_t)lane);
+                } else if (direct) {
+                    writeback_scatter(abase, rowpart, offs.scat_gate, td);
                 } else {
-                    writeback_row<false>(raw, rowb, G, tl, offs.unscale);
+                    writeback_row<false>(raw, rowb, G, td, offs.unscale);
                 }
                 asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             }
             if (stop) break;
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             mbar_arrive(sbase + kOffOut + 8 * s);
-            s += 2;
+            s += NG;
             if (s >= nst) {
                 s -= nst;
                 ++u;
@@ -763,7 +923,213 @@ int best_row_order(const TcBlockGeom& G, uint32_t pad, uint32_t* order)
     return best;
 }
 
+// Sets the padding fields and both blocks' row orders and staged offsets.
+void apply_layout(TcOffsets& o, uint32_t pad, const uint32_t (&order)[2][7])
+{
+    o.pad_shift = pad;
+    o.stage_bytes = kTileBytes + (pad < 31 ? 16u * (4096u >> pad) : 0u);
+    o.piece_bits = std::min(pad, o.run_bits);
+    o.npieces = 4096u >> o.piece_bits;
+    for (uint32_t b = 0; b < o.nblocks; ++b) {
+        TcBlockGeom& G = o.blk[b];
+        for (int r = 0; r < 7; ++r) {
+            G.jrow_bit[r] = order[b][r];
+            G.rowoff[r] = staged_offset(G.jrow_bit[r], pad);
+        }
+        for (int g = 0; g < 32; ++g) G.gateoff[g] = staged_offset(G.jgate[g], pad);
+    }
+}
+
+// Byte offset, in the second block's A operand (tc_sw128_offset of row r2,
+// K index 2 g2), that tile bit j contributes in a direct pass: the offset
+// is linear over GF(2) in the bits of r2 and g2, so it is the XOR of its
+// tile bits' contributions.  gbit1[k]: tile bit of gate bit k; order1[i]:
+// tile bit of row bit i (one-hot coordinates).
+uint32_t direct_bit_offset(int j, const int* gbit1, const uint32_t* order1)
+{
+    for (int k = 0; k < 5; ++k)
+        if (gbit1[k] == j) return tc_sw128_offset(0, 2u << k);
+    for (int i = 0; i < 7; ++i)
+        if (order1[i] == (1u << j)) return tc_sw128_offset(1u << i, 0);
+    return 0;
+}
+
+// Wavefronts of one warp's 4-byte scattered stores (all 32 lanes in one
+// phase): lanes = rows with row bit r at offset pattern pat[r], r < 5.
+int scatter_wavefronts(const uint32_t* pat)
+{
+    int per_bank[32] = {0};
+    int m = 0;
+    for (uint32_t l = 0; l < 32; ++l) {
+        uint32_t a = 0;
+        for (int r = 0; r < 5; ++r)
+            if ((l >> r) & 1u) a ^= pat[r];
+        m = std::max(m, ++per_bank[(a >> 2) & 31u]);
+    }
+    return m;
+}
+
 }  // namespace
+
+bool tc_direct_layout(TcOffsets& o, bool tma_ok, int conflict_slack, int* gbit1)
+{
+    if (o.nblocks != 2) return false;
+    const uint32_t gate0 = o.blk[0].jgate[31], gate1 = o.blk[1].jgate[31];
+    if (__builtin_popcount(gate0) != 5 || __builtin_popcount(gate1) != 5) return false;
+    std::vector<int> rows0, rows1;
+    for (int j = 0; j < 12; ++j) {
+        if (!((gate0 >> j) & 1u)) rows0.push_back(j);
+        if (!((gate1 >> j) & 1u)) rows1.push_back(j);
+    }
+    const bool v0 = o.blk[0].vec2 != 0;
+    const int width0 = v0 ? 16 : 8, inphase0 = v0 ? 3 : 4;
+    // per warp: block 0's row loads, 64 scattered stores, block 1's stores
+    const long ideal = 3 * 64;
+
+    struct Best {
+        long cost = -1;
+        uint32_t pad = 31;
+        uint32_t order[2][7] = {};
+        int g1[5] = {};
+    } best;
+    // the choice depends only on the geometry and the slack: remember it
+    static std::mutex mu;
+    static std::unordered_map<std::string, Best> memo;
+    std::string key(1, tma_ok ? 'T' : 'P');
+    key.append((const char*)&conflict_slack, sizeof(conflict_slack));
+    key.append((const char*)&o.run_bits, sizeof(o.run_bits));
+    key.append((const char*)o.blk[0].jgate, sizeof(o.blk[0].jgate));
+    key.append((const char*)&gate1, sizeof(gate1));
+    bool found = false;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        auto it = memo.find(key);
+        if (it != memo.end()) {
+            best = it->second;
+            found = true;
+        }
+    }
+    const uint32_t cands[] = {31, 11, 10, 9, 8, 7, 6, 5};
+    for (uint32_t pad : cands) {
+        if (found) break;
+        if (pad < 31 && tma_ok && best.cost >= 0 && best.cost <= conflict_slack * ideal) break;
+        // block 0: which 5 row bits are lanes, and which of them select the
+        // access phase (the rest vary inside a phase)
+        for (uint32_t lanes = 0; lanes < 128; ++lanes) {
+            if (__builtin_popcount(lanes) != 5) continue;
+            std::vector<int> S, W;
+            for (int r = 0; r < 7; ++r) ((lanes >> r) & 1u ? S : W).push_back(rows0[r]);
+            for (uint32_t sel = 0; sel < 32; ++sel) {
+                if (__builtin_popcount(sel) != 5 - inphase0) continue;
+                uint32_t order0[7];
+                int c = 0;
+                for (int i = 0; i < 5; ++i)
+                    if (!((sel >> i) & 1u)) order0[c++] = 1u << S[i];
+                for (int i = 0; i < 5; ++i)
+                    if ((sel >> i) & 1u) order0[c++] = 1u << S[i];
+                for (int w : W) order0[c++] = 1u << w;
+                const long load = (v0 ? 16 : 32) * (long)warp_wavefronts(order0, pad, width0);
+                if (best.cost >= 0 && load + 128 >= best.cost) continue;
+                // block 1's gate bits: block 0's lane bits first (they then
+                // select distinct banks through gate bits 0 and 1)
+                std::vector<int> GL, GO, RL, RO;
+                for (int i = 0; i < 5; ++i) {
+                    const int j = __builtin_ctz(order0[i]);
+                    ((gate1 >> j) & 1u ? GL : RL).push_back(j);
+                }
+                for (int j = 0; j < 12; ++j)
+                    if (((gate1 >> j) & 1u) && std::find(GL.begin(), GL.end(), j) == GL.end()) GO.push_back(j);
+                for (int j : rows1)
+                    if (std::find(RL.begin(), RL.end(), j) == RL.end()) RO.push_back(j);
+                int g1[5];
+                for (size_t k = 0; k < GL.size(); ++k) g1[k] = GL[k];
+                for (size_t k = 0; k < GO.size(); ++k) g1[GL.size() + k] = GO[k];
+                // block 1's row bits: block 0's row lanes at rows 0-2 (their
+                // bank bits in the operand layout), after the ones gate
+                // bits 2-4 already take; the other rows fill the free lane
+                // slots in every order for slots 3 and 4
+                const int a = (int)GL.size();
+                const int first = std::max(0, std::min(a - 2, 3 - (int)RL.size()));
+                int slot_of_rl[5];
+                for (size_t i = 0; i < RL.size(); ++i) slot_of_rl[i] = first + (int)i;
+                std::vector<int> freeslots;
+                for (int sl = 0; sl < 7; ++sl) {
+                    bool taken = false;
+                    for (size_t i = 0; i < RL.size(); ++i) taken = taken || slot_of_rl[i] == sl;
+                    if (!taken) freeslots.push_back(sl);
+                }
+                // RO fills freeslots (same count); try each ordered pair for
+                // the first two free slots at or above 3, the rest ascending
+                const int nro = (int)RO.size();
+                for (int p3 = 0; p3 < nro; ++p3)
+                    for (int p4 = 0; p4 < nro; ++p4) {
+                        if (p4 == p3) continue;
+                        uint32_t order1[7];
+                        for (size_t i = 0; i < RL.size(); ++i) order1[slot_of_rl[i]] = 1u << RL[i];
+                        std::vector<int> rest;
+                        for (int i = 0; i < nro; ++i)
+                            if (i != p3 && i != p4) rest.push_back(RO[i]);
+                        int ri = 0, hi_used = 0;
+                        for (int sl : freeslots) {
+                            if (sl >= 3 && hi_used == 0) {
+                                order1[sl] = 1u << RO[p3];
+                                ++hi_used;
+                            } else if (sl >= 3 && hi_used == 1) {
+                                order1[sl] = 1u << RO[p4];
+                                ++hi_used;
+                            } else {
+                                order1[sl] = 1u << rest[ri++];
+                            }
+                        }
+                        uint32_t pat[5];
+                        for (int i = 0; i < 5; ++i) pat[i] = direct_bit_offset(__builtin_ctz(order0[i]), g1, order1);
+                        const long scat = 64 * (long)scatter_wavefronts(pat);
+                        const bool v1 = g1[0] == 0;
+                        const long store = (v1 ? 16 : 32) * (long)warp_wavefronts(order1, pad, v1 ? 16 : 8);
+                        const long cost = load + scat + store;
+                        if (best.cost < 0 || cost < best.cost) {
+                            best.cost = cost;
+                            best.pad = pad;
+                            std::memcpy(best.order[0], order0, sizeof(order0));
+                            std::memcpy(best.order[1], order1, sizeof(order1));
+                            std::memcpy(best.g1, g1, sizeof(g1));
+                        }
+                    }
+            }
+        }
+        if (best.cost == ideal) break;
+    }
+    if (best.cost < 0) return false;
+    if (!found) {
+        std::lock_guard<std::mutex> lock(mu);
+        if (memo.size() > 4096) memo.clear();
+        memo.emplace(key, best);
+    }
+    // block 1 in its new gate order
+    TcBlockGeom& G1 = o.blk[1];
+    for (int g = 0; g < 32; ++g) {
+        uint32_t jc = 0;
+        for (int k = 0; k < 5; ++k)
+            if ((g >> k) & 1) jc |= 1u << best.g1[k];
+        G1.jgate[g] = jc;
+    }
+    G1.vec2 = G1.jgate[1] == 1u ? 1u : 0u;
+    apply_layout(o, best.pad, best.order);
+    for (int i = 0; i < 7; ++i)
+        o.scat_row[i] = direct_bit_offset(__builtin_ctz(best.order[0][i]), best.g1, best.order[1]);
+    for (int g = 0; g < 32; ++g) {
+        uint32_t a = 0;
+        for (int j = 0; j < 12; ++j)
+            if ((o.blk[0].jgate[g] >> j) & 1u) a ^= direct_bit_offset(j, best.g1, best.order[1]);
+        o.scat_gate[g] = a;
+    }
+    // both operand planes (2 x 16 KB) at 1024-byte aligned stage bases
+    o.stage_bytes = (o.stage_bytes + 1023u) & ~1023u;
+    o.direct = 1;
+    o.shuffle = 0;
+    std::memcpy(gbit1, best.g1, sizeof(best.g1));
+    return true;
+}
 
 void tc_choose_padding(TcOffsets& o, bool tma_ok, int conflict_slack)
 {
@@ -825,20 +1191,7 @@ void tc_choose_padding(TcOffsets& o, bool tma_ok, int conflict_slack)
         if (memo.size() > 4096) memo.clear();
         memo.emplace(key, ch);
     }
-    const uint32_t best_pad = ch.pad;
-    const auto& best_order = ch.order;
-    o.pad_shift = best_pad;
-    o.stage_bytes = kTileBytes + (best_pad < 31 ? 16u * (4096u >> best_pad) : 0u);
-    o.piece_bits = std::min(best_pad, o.run_bits);
-    o.npieces = 4096u >> o.piece_bits;
-    for (uint32_t b = 0; b < o.nblocks; ++b) {
-        TcBlockGeom& G = o.blk[b];
-        for (int r = 0; r < 7; ++r) {
-            G.jrow_bit[r] = best_order[b][r];
-            G.rowoff[r] = staged_offset(G.jrow_bit[r], best_pad);
-        }
-        for (int g = 0; g < 32; ++g) G.gateoff[g] = staged_offset(G.jgate[g], best_pad);
-    }
+    apply_layout(o, ch.pad, ch.order);
 }
 
 bool tc_shuffle_layout(TcBlockGeom& b0, TcBlockGeom& b1, int32_t* swap_lane, int* reg1)
@@ -1053,16 +1406,23 @@ cudaError_t launch_fused_tc(float2* amps, uint64_t ntiles, const IndexMap& tilem
             int v = 0;
             e = cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
             if (e != cudaSuccess) return e;
-            e = cudaFuncSetAttribute(k_fused_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+            e = cudaFuncSetAttribute(k_fused_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+            if (e != cudaSuccess) return e;
+            e = cudaFuncSetAttribute(k_fused_tc<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
             if (e != cudaSuccess) return e;
             optin[dev] = v;
         }
     }
     TcOffsets offs = offs_in;
     offs.wait_ns = wait_ns ? wait_ns : kTcDefaultWaitNs;
+    const uint32_t ng = offs.groups == 4 ? 4u : 2u;
     const uint32_t fixed = kAlignSlack + kOffB + offs.nblocks * kBImage;
+    // four groups hold four stages: at least one more for the copies;
+    // operands in shared memory need 1024-byte aligned stages
+    const uint32_t min_stages = ng == 4 ? 5u : 3u;
     if (offs.nblocks < 1 || offs.nblocks > 2 || offs.stage_bytes < kTileBytes ||
-        (uint32_t)optin[dev] < fixed + 3 * offs.stage_bytes)
+        ((ng == 4 || offs.direct) && offs.stage_bytes % 1024u) ||
+        (uint32_t)optin[dev] < fixed + min_stages * offs.stage_bytes)
         return cudaErrorInvalidConfiguration;
     offs.nstages = std::min(kMaxStages, ((uint32_t)optin[dev] - fixed) / offs.stage_bytes);
     const uint32_t smem = fixed + offs.nstages * offs.stage_bytes;
@@ -1095,8 +1455,12 @@ cudaError_t launch_fused_tc(float2* amps, uint64_t ntiles, const IndexMap& tilem
     uint64_t grid = (uint64_t)sm_count;
     if (grid > ntiles) grid = ntiles;
     if (grid == 0) return cudaSuccess;
-    k_fused_tc<<<(unsigned)grid, kTcThreads, smem, st>>>(amps, ntiles, tilemap, offs, tmap,
-                                                         (const uint4*)d_bimage, d_err);
+    if (ng == 4)
+        k_fused_tc<4><<<(unsigned)grid, TcShape<4>::kThreads, smem, st>>>(amps, ntiles, tilemap, offs, tmap,
+                                                                          (const uint4*)d_bimage, d_err);
+    else
+        k_fused_tc<2><<<(unsigned)grid, TcShape<2>::kThreads, smem, st>>>(amps, ntiles, tilemap, offs, tmap,
+                                                                          (const uint4*)d_bimage, d_err);
     return cudaGetLastError();
 }
 

@@ -121,10 +121,23 @@ struct TcOffsets {
     // order after the swaps.
     uint32_t shuffle;
     int32_t swap_lane[5];
-    uint32_t pad1_;
+    // Two-block passes whose second block reads its operands from shared
+    // memory (a plan's pair mode 3): the first block's write-back splits its
+    // results into hi/lo f16 pairs and stores them straight into the stage
+    // as the second block's A operand (K-major, SWIZZLE_128B, hi plane then
+    // lo plane), at byte (XOR over the thread's row bits i of scat_row[i])
+    // XOR scat_gate[g] for its output gate state g.  The second block's
+    // row and gate orders are the ones that layout implies.
+    uint32_t direct;
     uint64_t wait_ns;        // longest any wait may last (set by launch_fused_tc)
     uint64_t run_off[32];
     TcBlockGeom blk[2];
+    uint32_t scat_row[7];
+    uint32_t scat_gate[32];
+    // consumer groups of the kernel: 2 (0 means 2), or 4 with every A
+    // operand in shared memory (plan pair mode 4; stage_bytes a multiple of
+    // 1024)
+    uint32_t groups;
 };
 // A tile as a box of a rank-5 tensor map over the state: dimensions follow
 // the runs of tile / non-tile positions (tile runs split every 8 positions,
@@ -152,6 +165,21 @@ void tc_choose_padding(TcOffsets& offs, bool tma_ok, int conflict_slack = 2);
 // gate order after the swaps (jgate, vec2), its register bit k holding tile
 // bit reg1[k].  False if the blocks do not have five gate bits each.
 bool tc_shuffle_layout(TcBlockGeom& b0, TcBlockGeom& b1, int32_t* swap_lane, int* reg1);
+// Layout of a two-block pass in pair mode 3 (TcOffsets::direct): from block
+// 0's gate order and block 1's gate set, picks the padding (as
+// tc_choose_padding does, the same preference for one tensor-map copy) and
+// both blocks' row orders and block 1's gate order (gbit1[k] = tile bit of
+// its gate bit k) with the fewest predicted bank wavefronts over block 0's
+// reads, its scattered operand stores and block 1's write-back; sets
+// offs.direct, the scatter tables, block 1's jgate/vec2 and every staged
+// offset.  Returns false when the blocks do not have 5 gate bits each.
+bool tc_direct_layout(TcOffsets& offs, bool tma_ok, int conflict_slack, int* gbit1);
+// Byte offset of operand element (row r, K index k) in a K-major,
+// SWIZZLE_128B f16 matrix of 128-byte rows (8-row groups of 1024 B).
+inline uint32_t tc_sw128_offset(uint32_t r, uint32_t k)
+{
+    return (r >> 3) * 1024u + (r & 7u) * 128u + ((((k >> 3) ^ r) & 7u) << 4) + (k & 7u) * 2u;
+}
 // d_bimage: nblocks consecutive 16 KB f16 hi/lo images of the blocks' real
 // 64x64 embeddings in the kernel's swizzled layout; d_err: set to 1 if a
 // bounded wait expired.  wait_ns: longest any of the kernel's waits may

@@ -1,0 +1,149 @@
+// CPU check of the direct two-block tensor-core pass (fused_tc.cu, pair mode
+// 3): for random tile geometries, tc_direct_layout's scatter tables send
+// every output (row t, gate state g) of the first block, as the kernel
+// computes its offset (XOR of scat_row over t's bits, XOR scat_gate[g]), to
+// a distinct 4-byte word of the 16 KB operand plane, and that word is where
+// a K-major SWIZZLE_128B operand holds (row r2, K index 2 g2) of the second
+// block for the same tile coordinate.  Also checks the second block's gate
+// order, the staged offsets and the 1024-byte stage alignment.  Prints the
+// share of layouts whose predicted wavefronts are the minimum.  Exit status
+// 1 on any failure.
+#include <algorithm>
+#include <cstdio>
+#include <random>
+#include <vector>
+
+#include "../../q1tsim_gb300/csrc/common.cuh"
+#include "../../q1tsim_gb300/csrc/kernels.h"
+
+using namespace q1g;
+
+static uint32_t staged(uint32_t x, uint32_t pad) { return 8u * x + ((pad < 31 ? (x >> pad) : 0u) << 4); }
+
+static void default_geom(TcBlockGeom& G, const std::vector<int>& gate_bits)
+{
+    // gate bit k (LSB first) = tile bit gate_bits[k]; rows ascending
+    int r = 0;
+    for (int j = 0; j < 12; ++j)
+        if (std::find(gate_bits.begin(), gate_bits.end(), j) == gate_bits.end()) G.jrow_bit[r++] = 1u << j;
+    for (int g = 0; g < 32; ++g) {
+        uint32_t jc = 0;
+        for (int k = 0; k < 5; ++k)
+            if ((g >> k) & 1) jc |= 1u << gate_bits[k];
+        G.jgate[g] = jc;
+    }
+    G.vec2 = G.jgate[1] == 1u ? 1u : 0u;
+}
+
+int main()
+{
+    std::mt19937 rng(7);
+    int bad = 0, trials = 0, minimal = 0, padded = 0;
+    for (int trial = 0; trial < 1500; ++trial) {
+        std::vector<int> all(12);
+        for (int j = 0; j < 12; ++j) all[j] = j;
+        std::vector<int> g0, g1;
+        // block 1 overlaps block 0 on 0..4 tile bits; brick-like pairs
+        // (shifted windows) half of the time
+        if (trial % 2 == 0) {
+            const int lo0 = (int)(rng() % 8), shift = 1 + (int)(rng() % 4);
+            const int lo1 = std::max(0, std::min(7, lo0 + ((rng() & 1) ? shift : -shift)));
+            for (int k = 0; k < 5; ++k) {
+                g0.push_back(lo0 + k);
+                g1.push_back(lo1 + k);
+            }
+        } else {
+            std::shuffle(all.begin(), all.end(), rng);
+            g0.assign(all.begin(), all.begin() + 5);
+            std::shuffle(all.begin(), all.end(), rng);
+            g1.assign(all.begin(), all.begin() + 5);
+        }
+        std::shuffle(g0.begin(), g0.end(), rng);
+        std::shuffle(g1.begin(), g1.end(), rng);
+        if (g0 == g1) continue;
+        TcOffsets o{};
+        o.nblocks = 2;
+        o.run_bits = (uint32_t)(rng() % 13);
+        o.nruns = 1u << (12 - o.run_bits);
+        default_geom(o.blk[0], g0);
+        default_geom(o.blk[1], g1);
+        const uint32_t gate0 = o.blk[0].jgate[31], gate1 = o.blk[1].jgate[31];
+        uint32_t jgate0[32];
+        for (int g = 0; g < 32; ++g) jgate0[g] = o.blk[0].jgate[g];
+        int gbit1[5];
+        const bool tma_ok = (rng() % 3) != 0;
+        if (!tc_direct_layout(o, tma_ok, 2, gbit1)) {
+            ++bad;
+            std::printf("layout refused, trial %d\n", trial);
+            continue;
+        }
+        ++trials;
+        if (o.pad_shift < 31) ++padded;
+        // block 0 keeps its gate order; block 1 keeps its gate set, in the
+        // order gbit1
+        for (int g = 0; g < 32; ++g)
+            if (o.blk[0].jgate[g] != jgate0[g]) ++bad;
+        if (o.blk[1].jgate[31] != gate1 || o.direct != 1 || o.shuffle != 0) ++bad;
+        for (int k = 0; k < 5; ++k)
+            if (o.blk[1].jgate[1 << k] != (1u << gbit1[k])) ++bad;
+        if (o.blk[1].vec2 != (o.blk[1].jgate[1] == 1u ? 1u : 0u)) ++bad;
+        // row bits: each block's rows are the tile bits outside its gates
+        for (int b = 0; b < 2; ++b) {
+            uint32_t rows = 0;
+            for (int r = 0; r < 7; ++r) rows |= o.blk[b].jrow_bit[r];
+            if (rows != (0xFFFu & ~(b ? gate1 : gate0))) ++bad;
+        }
+        if (o.stage_bytes % 1024u || o.stage_bytes < 32768u) ++bad;
+        // staged offsets: every tile coordinate of each block inside the
+        // stage and in its own place
+        for (int b = 0; b < 2; ++b) {
+            const TcBlockGeom& G = o.blk[b];
+            for (int r = 0; r < 7; ++r)
+                if (G.rowoff[r] != staged(G.jrow_bit[r], o.pad_shift)) ++bad;
+            for (int g = 0; g < 32; ++g)
+                if (G.gateoff[g] != staged(G.jgate[g], o.pad_shift)) ++bad;
+        }
+        // the scatter
+        std::vector<int> seen(4096, 0);
+        for (uint32_t t = 0; t < 128; ++t) {
+            uint32_t rowpart = 0, xrow = 0;
+            for (int i = 0; i < 7; ++i)
+                if ((t >> i) & 1u) {
+                    rowpart ^= o.scat_row[i];
+                    xrow |= o.blk[0].jrow_bit[i];
+                }
+            for (int g = 0; g < 32; ++g) {
+                const uint32_t a = rowpart ^ o.scat_gate[g];
+                if (a >= 16384u || (a & 3u)) {
+                    ++bad;
+                    continue;
+                }
+                if (seen[a >> 2]++) ++bad;
+                const uint32_t x = xrow | o.blk[0].jgate[g];
+                uint32_t r2 = 0, g2 = 0;
+                for (int i = 0; i < 7; ++i)
+                    if (x & o.blk[1].jrow_bit[i]) r2 |= 1u << i;
+                for (int k = 0; k < 5; ++k)
+                    if (x & o.blk[1].jgate[1 << k]) g2 |= 1u << k;
+                if (a != tc_sw128_offset(r2, 2u * g2)) ++bad;
+            }
+        }
+        // predicted wavefronts: the minimum is 64 per warp for each of
+        // block 0's reads, the scatter and block 1's stores
+        bool at_min = true;
+        {
+            // scatter: lanes = row bits 0..4 of block 0
+            int per_bank[32] = {0}, m = 0;
+            for (uint32_t l = 0; l < 32; ++l) {
+                uint32_t a = 0;
+                for (int i = 0; i < 5; ++i)
+                    if ((l >> i) & 1u) a ^= o.scat_row[i];
+                m = std::max(m, ++per_bank[(a >> 2) & 31u]);
+            }
+            at_min = m == 1;
+        }
+        minimal += at_min;
+    }
+    std::printf("bad %d trials %d conflict-free scatter %d padded %d\n", bad, trials, minimal, padded);
+    return bad ? 1 : 0;
+}

@@ -627,15 +627,19 @@ def split_exact_amps(n):
     (15, [2, 7, 13]),
     (16, [0, 5, 10, 14, 15]),
 ])
-def test_tensor_core_block_exact_any_layout(n, qubits):
+@pytest.mark.parametrize("pairs", [1, 4])
+def test_tensor_core_block_exact_any_layout(n, qubits, pairs):
     """Permutation blocks through the tensor cores on every tile layout (gate
-    bits low or high, staged rows padded or not): hi + lo recover each
+    bits low or high, staged rows padded or not), with A in TMEM (two
+    consumer groups) or in shared memory (four): hi + lo recover each
     amplitude, so the result equals the oracle's exactly."""
     amps = split_exact_amps(n)
     P = cyclic_perm(len(qubits), 3)
     g = VectorState.from_amplitudes(amps, 1, "c64")
     g.profile(True)
-    g.apply_plan(Plan(n, [qubits], 5), P.ravel().view(np.float64))
+    plan = Plan(n, [qubits], 5)
+    plan.set_tc_tiling(pairs, 8, 2)
+    g.apply_plan(plan, P.ravel().view(np.float64))
     assert g.profile_report()["fused_tc_c64"]["launches"] == 1
     o = orc.OracleState.from_amplitudes(amps, 1)
     o.apply_gate(P, qubits)
@@ -675,6 +679,37 @@ def test_short_run_pair_goes_as_one_tensor_map_box(n, first, second):
     g = VectorState.from_amplitudes(amps, 1, "c64")
     g.profile(True)
     g.apply_plan(Plan(n, [b for b, _ in seq], 5), mats)
+    o = orc.OracleState.from_amplitudes(amps, 1)
+    for b, m in seq:
+        o.apply_gate(m, b)
+    out, ref = g.states()[:, 0], o.states()[:, 0]
+    assert np.array_equal(out, ref), float(np.max(np.abs(out - ref)))
+    assert g.profile_report()["fused_tc_c64"]["launches"] == 1
+
+
+@pytest.mark.parametrize("n,first,second", [
+    (14, [9, 10, 11, 12, 13], [7, 8, 9, 10, 11]),    # low positions, one run
+    (16, [3, 4, 5, 6, 7], [1, 2, 3, 4, 5]),          # high positions: brick pair
+    (22, [1, 2, 3, 4, 5], [5, 6, 7, 8, 9]),          # tile runs of 8 amplitudes
+    (20, [0, 1, 2, 3, 4], [3, 4, 5, 6, 7]),          # top position in the tile
+    (16, [0, 5, 10, 14, 15], [2, 3, 4, 5, 12]),      # scattered gate bits
+    (18, [13, 14, 15, 16, 17], [4, 5, 6, 7, 8]),     # disjoint blocks
+])
+@pytest.mark.parametrize("mode", [3, 4])
+def test_direct_pair_is_exact(n, first, second, mode):
+    """Pair modes 3 and 4: the first block's write-back stores the second
+    block's hi/lo operands in shared memory and its MMAs read them there
+    (mode 4: in the four-group kernel, whose first block's operands are in
+    shared memory too).  On permutation blocks and amplitudes that split
+    exactly, the state equals the oracle's bit for bit, in one pass."""
+    amps = split_exact_amps(n)
+    seq = [(first, cyclic_perm(5, 7)), (second, cyclic_perm(5, 11))]
+    mats = np.concatenate([m.ravel() for _, m in seq]).view(np.float64)
+    plan = Plan(n, [b for b, _ in seq], 5)
+    plan.set_tc_tiling(mode, 12, 2)
+    g = VectorState.from_amplitudes(amps, 1, "c64")
+    g.profile(True)
+    g.apply_plan(plan, mats)
     o = orc.OracleState.from_amplitudes(amps, 1)
     for b, m in seq:
         o.apply_gate(m, b)
@@ -989,11 +1024,13 @@ def test_autotuned_circuit_matches_oracle():
     assert set(autotune.TC_TILINGS) <= tilings
 
 
-@pytest.mark.parametrize("tiling", [(2, 5, 2), (1, 5, 2), (0, 5, 2), (2, 8, 2), (2, 5, 4), (2, 12, 64), (1, 12, 64)])
+@pytest.mark.parametrize("tiling", [(2, 5, 2), (1, 5, 2), (0, 5, 2), (2, 8, 2), (2, 5, 4), (2, 12, 64), (1, 12, 64),
+                                    (3, 5, 2), (3, 8, 2), (3, 12, 64), (4, 8, 2), (4, 12, 64)])
 def test_tc_tilings_match_oracle(tiling):
-    """Every tensor-core tiling (pairs through registers or through the
-    staged tile or none, pairs over more large pages, unpadded tiles kept at
-    more bank conflicts) gives the oracle's state."""
+    """Every tensor-core tiling (pairs through registers, through the staged
+    tile, as operands the first block stores for the second, or none; pairs
+    over more large pages; unpadded tiles kept at more bank conflicts) gives
+    the oracle's state."""
     rng = np.random.default_rng(31)
     n = 19
     gl = [random_gate(n, rng) for _ in range(80)]
@@ -1014,11 +1051,13 @@ def test_tc_tilings_match_oracle(tiling):
     assert 1 - abs(np.vdot(want, got)) ** 2 <= 1e-6
 
 
-def test_tensor_core_plan_with_many_tiles_per_sm_matches_oracle():
+@pytest.mark.parametrize("pairs", [1, 3, 4])
+def test_tensor_core_plan_with_many_tiles_per_sm_matches_oracle(pairs):
     """21 qubits: 512 tiles of 4096 amplitudes, so every SM's CTA takes
     several tiles and both consumer groups of the tensor-core kernel work
     (at 12-16 qubits a CTA has one tile at most).  A brick of U3/CX fused
-    into 5-qubit blocks, one- and two-block passes, against the oracle."""
+    into 5-qubit blocks, one- and two-block passes (the second block reading
+    the staged tile, or operands stored for it), against the oracle."""
     n = 21
     rng = np.random.default_rng(2101)
     gates = []
@@ -1034,10 +1073,44 @@ def test_tensor_core_plan_with_many_tiles_per_sm_matches_oracle():
     ref = o.states()[:, 0]
     mats = np.concatenate([np.ascontiguousarray(gt.matrix()).ravel() for gt, _ in gates]).view(np.float64)
     g = VectorState.from_amplitudes(amps, 1, "c64")
-    g.apply_plan(Plan(n, [b for _, b in gates], 5), mats)
+    plan = Plan(n, [b for _, b in gates], 5)
+    plan.set_tc_tiling(pairs, 8, 2)
+    g.apply_plan(plan, mats)
     out = g.states()[:, 0]
     assert np.max(np.abs(out - ref)) <= TOL64, float(np.max(np.abs(out - ref)))
     assert 1 - abs(np.vdot(ref, out)) ** 2 / np.linalg.norm(out) ** 2 <= 1e-9
+
+
+@pytest.mark.parametrize("pairs", [1, 3, 4])
+def test_tensor_core_stage_reuse_matches_complex128(pairs):
+    """24 qubits: 4096 tiles, about 27 per CTA, so each consumer group takes
+    several tiles and every shared-memory stage is reused many times, in
+    rings of 5 or 6 stages (padded pairs take 5).  A brick of U3/CX fused
+    into 5-qubit blocks (pairs of low and high positions among them) in
+    each pair mode, against the same circuit gate by gate in complex128 (whose
+    kernels the oracle pins)."""
+    n = 24
+    rng = np.random.default_rng(2402)
+    gates = []
+    for layer in range(8):
+        for q in range(n):
+            gates.append((G.U3(*rng.uniform(0, 2 * np.pi, 3)), [q]))
+        for q in range(layer % 2, n - 1, 2):
+            gates.append((G.CX(), [q, q + 1]))
+    bits = [b for _, b in gates]
+    mats = np.concatenate([np.ascontiguousarray(gt.matrix()).ravel() for gt, _ in gates]).view(np.float64)
+    ref = VectorState(n, 1, "c128")
+    ref.apply_plan(Plan(n, bits, 0), mats)
+    g = VectorState(n, 1, "c64")
+    plan = Plan(n, bits, 5)
+    plan.set_tc_tiling(pairs, 8, 2)
+    g.profile(True)
+    for _ in range(2):
+        g.reset_all()
+        g.apply_plan(plan, mats)
+    assert g.profile_report()["fused_tc_c64"]["launches"] > 0
+    acc = ref.compare(g)
+    assert acc["max_abs_diff"] <= 1e-6 and acc["infidelity"] <= 1e-9, acc
 
 
 def test_norm_correction_left_pending_until_needed():

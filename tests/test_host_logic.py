@@ -13,7 +13,8 @@
   permutation (tests/cpp/swap_run_check.cpp, same library).
 - fused_tc.cu: the row layouts and register/lane swaps of shuffled
   two-block tensor-core passes, replayed on tile coordinates
-  (tests/cpp/shuffle_check.cpp, same library).
+  (tests/cpp/shuffle_check.cpp, same library), and the scatter of direct
+  pairs into the second block's operand layout (tests/cpp/direct_check.cpp).
 - f16_host.h / fused_tc.cu: binary16 rounding against numpy's float16, the
   f16 image of a block read back through its swizzle, the operand scales and
   the row-norm bound of tensor-core blocks (tests/cpp/tc_image_check.cpp).
@@ -86,6 +87,11 @@ def test_tile_box_and_padding(gxx, tmp_path):
 
 def test_shuffled_pairs_redeal_the_rows(gxx, tmp_path):
     out = _run(_link_against_library(gxx, tmp_path, "shuffle_check"))
+    assert out.startswith("bad 0"), out
+
+
+def test_direct_pairs_scatter_into_the_operand_layout(gxx, tmp_path):
+    out = _run(_link_against_library(gxx, tmp_path, "direct_check"))
     assert out.startswith("bad 0"), out
 
 
