@@ -242,7 +242,7 @@ int q1g_plan_set_tensor_cores(q1g_plan* p, int enable);
  * most max_high_positions positions at or above 2 MB strides (default 8: at
  * most 256 large pages per tile); an unpadded tile, one tensor-map copy, is
  * kept while its shared-memory bank wavefronts stay within conflict_slack
- * times the minimum (default 2), else it is padded and copied in pieces.
+ * times the minimum (default 4), else it is padded and copied in pieces.
  * No counterpart in the reference. */
 int q1g_plan_set_tc_tiling(q1g_plan* p, int allow_pairs, int max_high_positions, int conflict_slack);
 

@@ -247,7 +247,7 @@ struct q1g_plan {
     // unpadded one-box tile may take.
     int tc_pairs = 4;
     int tc_max_high = 8;
-    int tc_slack = 2;
+    int tc_slack = 4;
     q1g::HostBuf hmats;            // pinned staging of dense matrices
     q1g::DevBuf dmats;
     cudaEvent_t staged = nullptr;  // last upload of hmats finished

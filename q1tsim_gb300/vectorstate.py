@@ -307,7 +307,7 @@ class Plan:
     # (pairs of blocks per pass: 0 none, 1 through the staged tile, 2 through
     # registers; tile positions at >= 2 MB strides a pair may have;
     # bank-conflict slack of an unpadded tile)
-    DEFAULT_TC_TILING = (4, 8, 2)
+    DEFAULT_TC_TILING = (4, 8, 4)
 
     def __init__(self, nr_bits, gate_bits, fusion_width=0, tensor_cores=True, diagonal=None, kinds=None):
         """kinds: per gate, KIND_DIAGONAL for gates whose matrix is always
@@ -340,7 +340,7 @@ class Plan:
     def handle(self):
         return self._h
 
-    def set_tc_tiling(self, allow_pairs=4, max_high_positions=8, conflict_slack=2):
+    def set_tc_tiling(self, allow_pairs=4, max_high_positions=8, conflict_slack=4):
         """Tiling of the tensor-core passes (q1g_plan_set_tc_tiling)."""
         check(_lib.load().q1g_plan_set_tc_tiling(self.handle, int(allow_pairs), int(max_high_positions),
                                                  int(conflict_slack)), "plan_set_tc_tiling")

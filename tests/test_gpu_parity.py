@@ -1025,7 +1025,7 @@ def test_autotuned_circuit_matches_oracle():
 
 
 @pytest.mark.parametrize("tiling", [(2, 5, 2), (1, 5, 2), (0, 5, 2), (2, 8, 2), (2, 5, 4), (2, 12, 64), (1, 12, 64),
-                                    (3, 5, 2), (3, 8, 2), (3, 12, 64), (4, 8, 2), (4, 12, 64)])
+                                    (3, 5, 2), (3, 8, 2), (3, 12, 64), (4, 8, 2), (4, 8, 4), (4, 12, 64)])
 def test_tc_tilings_match_oracle(tiling):
     """Every tensor-core tiling (pairs through registers, through the staged
     tile, as operands the first block stores for the second, or none; pairs
