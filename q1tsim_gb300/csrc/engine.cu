@@ -817,10 +817,22 @@ static TcPass lower_tc_pass(const std::vector<const std::vector<cd>*>& mats,
     // pair mode 4: the four-group kernel, every A operand in shared memory
     const bool quad = pair_mode == 4;
     auto finish = [&] {
-        if (quad) {
-            t.offs.groups = 4;
-            t.offs.stage_bytes = (t.offs.stage_bytes + 1023u) & ~1023u;
+        if (!quad) return;
+        t.offs.groups = 4;
+        t.offs.stage_bytes = (t.offs.stage_bytes + 1023u) & ~1023u;
+        // the first block's split is dealt to the threads by a map of its
+        // own, in a gate order that map chooses: its image in that order
+        int gbit0[5];
+        tc_split_map(t.offs, gbit0);
+        std::vector<int> q0(5);
+        for (int k = 0; k < 5; ++k) q0[4 - k] = nbits - 1 - T[gbit0[k]];
+        const auto m32 = embed_matrix(*mats[0], *bits[0], q0);
+        std::vector<double> md(2 * 32 * 32);
+        for (size_t e = 0; e < m32.size(); ++e) {
+            md[2 * e] = m32[e].real();
+            md[2 * e + 1] = m32[e].imag();
         }
+        build_tc_image(md.data(), t.images.data(), mats.size() == 1 ? kTcLastBScaleLog2 : 0);
     };
     int gbit1[5];
     if (mats.size() == 2 && (pair_mode == 3 || quad) && tc_direct_layout(t.offs, t.box.usable != 0, slack, gbit1)) {

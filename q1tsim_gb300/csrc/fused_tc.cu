@@ -547,6 +547,41 @@ __device__ __forceinline__ void issue_mma_ksteps(uint32_t tm, uint32_t bb, int k
         mma_f16_ts(tm + 192u, tm + 16u * ks + 8u, desc_sw128(bb + (uint32_t)ks * 32u), kIdescN64, 1u);
 }
 
+// The first block's tile dealt to the group's threads as the split map
+// says (TcOffsets::sp_*): 32 amplitudes at tb + sp_regoff[j], every load of
+// the group performed (the barrier), then each 16-byte chunk q of hi/lo
+// pairs stored at abase + (ta ^ sp_achunk[q]) in both planes.
+__device__ __forceinline__ void split_mapped(const uint8_t* raw, uint32_t tb, uint32_t abase, uint32_t ta,
+                                             const TcOffsets& o, uint32_t gbar)
+{
+    float2 x[32];
+    if (o.sp_vec2) {
+#pragma unroll
+        for (int m = 0; m < 16; ++m) {
+            const float4 p = *(const float4*)(raw + tb + o.sp_regoff[2 * m]);
+            x[2 * m] = make_float2(p.x, p.y);
+            x[2 * m + 1] = make_float2(p.z, p.w);
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) x[j] = *(const float2*)(raw + tb + o.sp_regoff[j]);
+    }
+    group_sync(gbar);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        uint32_t hi[4], lo[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) split_amp<true>(x[4 * q + e], o.ascale, hi[e], lo[e]);
+        const uint32_t a = abase + (ta ^ o.sp_achunk[q]);
+        asm volatile("st.shared.v4.u32 [%0], {%1, %2, %3, %4};" ::"r"(a), "r"(hi[0]), "r"(hi[1]), "r"(hi[2]),
+                     "r"(hi[3])
+                     : "memory");
+        asm volatile("st.shared.v4.u32 [%0], {%1, %2, %3, %4};" ::"r"(a + 16384u), "r"(lo[0]), "r"(lo[1]),
+                     "r"(lo[2]), "r"(lo[3])
+                     : "memory");
+    }
+}
+
 // The MMAs of K-steps k0 and k0+1 with A in shared memory at abase (hi
 // plane, then the lo plane 16 KB above, K-major SWIZZLE_128B): D_main at
 // TMEM column td, D_corr at td + 64.
@@ -725,13 +760,15 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, const __grid_constant__ Inde
         const uint32_t mbar = sbase + kOffMma + 8u * g;
         // row t of an A operand in shared memory (SWIZZLE_128B, 128 B rows)
         const uint32_t arow = (t >> 3) * 1024u + (t & 7u) * 128u;
-        uint32_t rowb0 = 0, rowb1 = 0, rowpart = 0;
+        uint32_t rowb0 = 0, rowb1 = 0, rowpart = 0, sp_tb = 0, sp_ta = 0;
 #pragma unroll
         for (int r = 0; r < 7; ++r)
             if ((t >> r) & 1u) {
                 rowb0 += offs.blk[0].rowoff[r];
                 rowb1 += offs.blk[1].rowoff[r];
                 rowpart ^= offs.scat_row[r];
+                sp_tb += offs.sp_thoff[r];
+                sp_ta ^= offs.sp_athr[r];
             }
         const bool direct = offs.direct != 0;
         uint32_t s = g, u = 0, mph = 0;     // tile i lives in stage i % nst
@@ -762,6 +799,19 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, const __grid_constant__ Inde
                     // the first block's write-back left this block's
                     // operands in the stage: make them visible to the
                     // tensor cores, then the MMAs
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                    group_sync(gbar);
+                    if (issuer) {
+                        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                        issue_mma_smem_ksteps(td, abase, bb, 0);
+                        issue_mma_smem_ksteps(td, abase, bb, 2);
+                        mma_commit(mbar);
+                    }
+                } else if (Sh::kSmemA && b == 0) {
+                    // the tile -> hi/lo operands over it in the stage, dealt
+                    // to the threads by the split map; then the 8 MMAs
+                    split_mapped(raw, sp_tb, abase, sp_ta, offs, gbar);
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
                     group_sync(gbar);
@@ -1129,6 +1179,171 @@ bool tc_direct_layout(TcOffsets& o, bool tma_ok, int conflict_slack, int* gbit1)
     o.shuffle = 0;
     std::memcpy(gbit1, best.g1, sizeof(best.g1));
     return true;
+}
+
+namespace {
+
+// Offset, in block 0's A operand, of tile bit j: gate bit k (from gate
+// order g0) at K index 2 * 2^k, row bit i (one-hot coordinates order0) at
+// row 2^i; linear over GF(2) like direct_bit_offset.
+uint32_t split_bit_offset(int j, const int* g0, const uint32_t* order0)
+{
+    for (int k = 0; k < 5; ++k)
+        if (g0[k] == j) return tc_sw128_offset(0, 2u << k);
+    for (int i = 0; i < 7; ++i)
+        if (order0[i] == (1u << j)) return tc_sw128_offset(1u << i, 0);
+    return 0;
+}
+
+// Wavefronts of one warp's 16-byte stores (quarter-warp phases of 8
+// lanes) whose lane bits 0-2 move the address by pat[0..2] (XOR).
+int sts128_wavefronts(const uint32_t* pat)
+{
+    int per_group[8] = {0};
+    int m = 0;
+    for (uint32_t l = 0; l < 8; ++l) {
+        uint32_t a = 0;
+        for (int r = 0; r < 3; ++r)
+            if ((l >> r) & 1u) a ^= pat[r];
+        m = std::max(m, ++per_group[(a >> 4) & 7u]);
+    }
+    return 4 * m;
+}
+
+}  // namespace
+
+void tc_split_map(TcOffsets& o, int* gbit0)
+{
+    TcBlockGeom& G = o.blk[0];
+    const uint32_t pad = o.pad_shift;
+    std::vector<int> gates;
+    for (int j = 0; j < 12; ++j)
+        if ((G.jgate[31] >> j) & 1u) gates.push_back(j);
+    // the last block's write-back reads rows (TMEM lanes) with the gate
+    // pairs adjacent when gate bit 0 is tile bit 0
+    auto wb_cost = [&](bool v2) {
+        return o.nblocks == 1 ? (v2 ? 16 : 32) * (long)warp_wavefronts(G.jrow_bit, pad, v2 ? 16 : 8) : 0L;
+    };
+    long best = -1;
+    int best_g[5] = {}, best_bits[12] = {};
+    // the choice depends only on the geometry: remember it
+    struct Choice {
+        int g[5];
+        int bits[12];
+    };
+    static std::mutex mu;
+    static std::unordered_map<std::string, Choice> memo;
+    std::string key(1, (char)o.nblocks);
+    key.append((const char*)&pad, sizeof(pad));
+    key.append((const char*)G.jrow_bit, sizeof(G.jrow_bit));
+    key.append((const char*)&G.jgate[31], sizeof(uint32_t));
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        auto it = memo.find(key);
+        if (it != memo.end()) {
+            best = 0;
+            std::memcpy(best_g, it->second.g, sizeof(best_g));
+            std::memcpy(best_bits, it->second.bits, sizeof(best_bits));
+        }
+    }
+    for (int ia = 0; ia < 5 && best < 0; ++ia)
+        for (int ib = ia + 1; ib < 5; ++ib) {
+            int g[5] = {gates[ia], gates[ib], 0, 0, 0};
+            int c = 2;
+            for (int k = 0; k < 5; ++k)
+                if (k != ia && k != ib) g[c++] = gates[k];
+            std::vector<int> rest;
+            for (int j = 0; j < 12; ++j)
+                if (j != g[0] && j != g[1]) rest.push_back(j);
+            const bool v2 = g[0] == 0;
+            const int width = v2 ? 16 : 8, nld = v2 ? 16 : 32;
+            const long wb = wb_cost(v2);
+            // lane bits 0-3 from the 10 other bits: which 4, and which of
+            // them is lane bit 3 (outside the 16-byte stores' phase)
+            for (uint32_t m4 = 0; m4 < 1024; ++m4) {
+                if (__builtin_popcount(m4) != 4) continue;
+                int P[4], n = 0, l4 = -1;
+                for (int r = 0; r < 10; ++r) {
+                    if ((m4 >> r) & 1u) P[n++] = rest[r];
+                    else if (l4 < 0) l4 = rest[r];
+                }
+                for (int h = 0; h < 4; ++h) {
+                    int lane[5], q = 0;
+                    for (int e = 0; e < 4; ++e)
+                        if (e != h) lane[q++] = P[e];
+                    lane[3] = P[h];
+                    lane[4] = l4;
+                    uint32_t ord[7];
+                    for (int e = 0; e < 5; ++e) ord[e] = 1u << lane[e];
+                    ord[5] = ord[6] = 0;
+                    const long ld = nld * (long)warp_wavefronts(ord, pad, width);
+                    uint32_t pat[3];
+                    for (int e = 0; e < 3; ++e) pat[e] = split_bit_offset(lane[e], g, G.jrow_bit);
+                    const long cost = ld + 16 * (long)sts128_wavefronts(pat) + wb;
+                    if (best < 0 || cost < best) {
+                        best = cost;
+                        std::memcpy(best_g, g, sizeof(g));
+                        // lanes 0-4, warps 5-6, registers 2-4: the rest ascending
+                        int bits[12], b = 0;
+                        for (int e = 0; e < 5; ++e) bits[b++] = lane[e];
+                        for (int j : rest) {
+                            bool used = false;
+                            for (int e = 0; e < 5; ++e) used = used || lane[e] == j;
+                            if (!used) bits[b++] = j;
+                        }
+                        std::memcpy(best_bits, bits, sizeof(bits));
+                    }
+                }
+            }
+        }
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        if (memo.size() > 4096) memo.clear();
+        Choice c;
+        std::memcpy(c.g, best_g, sizeof(best_g));
+        std::memcpy(c.bits, best_bits, sizeof(best_bits));
+        memo.emplace(key, c);
+    }
+    // bits 0-4 lanes, 5-6 warps, 7-9 registers 2-4 (10 of the 12 tile bits;
+    // gate bits 0-1 are registers 0-1)
+    for (int k = 0; k < 5; ++k) gbit0[k] = best_g[k];
+    for (int gi = 0; gi < 32; ++gi) {
+        uint32_t jc = 0;
+        for (int k = 0; k < 5; ++k)
+            if ((gi >> k) & 1) jc |= 1u << best_g[k];
+        G.jgate[gi] = jc;
+        G.gateoff[gi] = staged_offset(jc, pad);
+    }
+    G.vec2 = best_g[0] == 0 ? 1u : 0u;
+    o.sp_vec2 = G.vec2;
+    for (int i = 0; i < 7; ++i) {
+        o.sp_thoff[i] = staged_offset(1u << best_bits[i], pad);
+        o.sp_athr[i] = split_bit_offset(best_bits[i], best_g, G.jrow_bit);
+    }
+    const int reg[5] = {best_g[0], best_g[1], best_bits[7], best_bits[8], best_bits[9]};
+    for (int j = 0; j < 32; ++j) {
+        uint32_t x = 0;
+        for (int k = 0; k < 5; ++k)
+            if ((j >> k) & 1) x |= 1u << reg[k];
+        o.sp_regoff[j] = staged_offset(x, pad);
+    }
+    for (int q = 0; q < 8; ++q) {
+        uint32_t a = 0;
+        for (int k = 0; k < 3; ++k)
+            if ((q >> k) & 1) a ^= split_bit_offset(reg[2 + k], best_g, G.jrow_bit);
+        o.sp_achunk[q] = a;
+    }
+    if (o.direct) {
+        // the scatter table follows block 0's new gate order
+        int g1[5];
+        for (int k = 0; k < 5; ++k) g1[k] = __builtin_ctz(o.blk[1].jgate[1 << k]);
+        for (int gi = 0; gi < 32; ++gi) {
+            uint32_t a = 0;
+            for (int j = 0; j < 12; ++j)
+                if ((G.jgate[gi] >> j) & 1u) a ^= direct_bit_offset(j, g1, o.blk[1].jrow_bit);
+            o.scat_gate[gi] = a;
+        }
+    }
 }
 
 void tc_choose_padding(TcOffsets& o, bool tma_ok, int conflict_slack)

@@ -138,6 +138,19 @@ struct TcOffsets {
     // operand in shared memory (plan pair mode 4; stage_bytes a multiple of
     // 1024)
     uint32_t groups;
+    // Four groups: how the first block's split deals the tile to a group's
+    // 128 threads (tc_split_map).  Thread t (lane bits 0-4, warp bits 5-6
+    // of t) reads its 32 amplitudes at staged offset (sum over t's bits i of
+    // sp_thoff[i]) + sp_regoff[j] (register j: bits 0-1 are the block's gate
+    // bits 0-1, so that registers 4q..4q+3 fill one 16-byte operand chunk)
+    // and stores chunk q of each plane at (XOR over t's bits of sp_athr[i])
+    // XOR sp_achunk[q].  sp_vec2: registers 2m, 2m+1 are adjacent in the
+    // stage (16-byte loads).
+    uint32_t sp_vec2;
+    uint32_t sp_thoff[7];
+    uint32_t sp_athr[7];
+    uint32_t sp_achunk[8];
+    uint32_t sp_regoff[32];
 };
 // A tile as a box of a rank-5 tensor map over the state: dimensions follow
 // the runs of tile / non-tile positions (tile runs split every 8 positions,
@@ -174,6 +187,14 @@ bool tc_shuffle_layout(TcBlockGeom& b0, TcBlockGeom& b1, int32_t* swap_lane, int
 // offs.direct, the scatter tables, block 1's jgate/vec2 and every staged
 // offset.  Returns false when the blocks do not have 5 gate bits each.
 bool tc_direct_layout(TcOffsets& offs, bool tma_ok, int conflict_slack, int* gbit1);
+// Deal of the first block's tile to the threads of a four-group pass
+// (TcOffsets::sp_*), after its layout (padding, row orders, scatter tables)
+// is chosen: picks the block's gate bits 0-1 and the tile bits that vary
+// across a warp's lanes so that its loads and its 16-byte operand stores
+// take the fewest predicted bank wavefronts (the gate order is otherwise
+// ascending); updates block 0's jgate, vec2, gate offsets and, in a direct
+// pair, the scatter table.  gbit0[k]: tile bit of block 0's gate bit k.
+void tc_split_map(TcOffsets& offs, int* gbit0);
 // Byte offset of operand element (row r, K index k) in a K-major,
 // SWIZZLE_128B f16 matrix of 128-byte rows (8-row groups of 1024 B).
 inline uint32_t tc_sw128_offset(uint32_t r, uint32_t k)

@@ -5,9 +5,13 @@
 // a distinct 4-byte word of the 16 KB operand plane, and that word is where
 // a K-major SWIZZLE_128B operand holds (row r2, K index 2 g2) of the second
 // block for the same tile coordinate.  Also checks the second block's gate
-// order, the staged offsets and the 1024-byte stage alignment.  Prints the
-// share of layouts whose predicted wavefronts are the minimum.  Exit status
-// 1 on any failure.
+// order, the staged offsets and the 1024-byte stage alignment.  Then, for
+// the four-group kernel, tc_split_map's deal of the first block's tile
+// (single-block passes too): every (thread, register) reads a distinct tile
+// coordinate at its staged offset and stores it where the first block's A
+// operand holds (row, K index 2 g) in the block's new gate order, and the
+// scatter follows that order.  Prints how many layouts have a conflict-free
+// scatter.  Exit status 1 on any failure.
 #include <algorithm>
 #include <cstdio>
 #include <random>
@@ -33,6 +37,45 @@ static void default_geom(TcBlockGeom& G, const std::vector<int>& gate_bits)
         G.jgate[g] = jc;
     }
     G.vec2 = G.jgate[1] == 1u ? 1u : 0u;
+}
+
+// tc_split_map's deal against the geometry of block 0 (after the map).
+static int check_split(const TcOffsets& o)
+{
+    int bad = 0;
+    std::vector<int> inv(40000, -1);
+    for (uint32_t x = 0; x < 4096; ++x) inv[staged(x, o.pad_shift)] = (int)x;
+    std::vector<int> seen(4096, 0);
+    const TcBlockGeom& G = o.blk[0];
+    for (int g = 0; g < 32; ++g)
+        if (G.gateoff[g] != staged(G.jgate[g], o.pad_shift)) ++bad;
+    if (G.vec2 != (G.jgate[1] == 1u ? 1u : 0u) || o.sp_vec2 != G.vec2) ++bad;
+    for (uint32_t t = 0; t < 128; ++t) {
+        uint32_t tb = 0, ta = 0;
+        for (int i = 0; i < 7; ++i)
+            if ((t >> i) & 1u) {
+                tb += o.sp_thoff[i];
+                ta ^= o.sp_athr[i];
+            }
+        for (int j = 0; j < 32; ++j) {
+            const uint32_t off = tb + o.sp_regoff[j];
+            if (off >= inv.size() || inv[off] < 0) {
+                ++bad;
+                continue;
+            }
+            const uint32_t x = (uint32_t)inv[off];
+            if (seen[x]++) ++bad;
+            if (o.sp_vec2 && (j & 1) == 0 && o.sp_regoff[j + 1] != o.sp_regoff[j] + 8u) ++bad;
+            uint32_t r = 0, gi = 0;
+            for (int i = 0; i < 7; ++i)
+                if (x & G.jrow_bit[i]) r |= 1u << i;
+            for (int k = 0; k < 5; ++k)
+                if (x & G.jgate[1 << k]) gi |= 1u << k;
+            const uint32_t a = (ta ^ o.sp_achunk[j >> 2]) + 4u * (uint32_t)(j & 3);
+            if (a != tc_sw128_offset(r, 2u * gi) || a >= 16384u) ++bad;
+        }
+    }
+    return bad;
 }
 
 int main()
@@ -79,8 +122,8 @@ int main()
         }
         ++trials;
         if (o.pad_shift < 31) ++padded;
-        // block 0 keeps its gate order; block 1 keeps its gate set, in the
-        // order gbit1
+        // the direct layout keeps block 0's gate order; block 1 keeps its
+        // gate set, in the order gbit1
         for (int g = 0; g < 32; ++g)
             if (o.blk[0].jgate[g] != jgate0[g]) ++bad;
         if (o.blk[1].jgate[31] != gate1 || o.direct != 1 || o.shuffle != 0) ++bad;
@@ -103,6 +146,14 @@ int main()
             for (int g = 0; g < 32; ++g)
                 if (G.gateoff[g] != staged(G.jgate[g], o.pad_shift)) ++bad;
         }
+        // the four-group kernel deals block 0's tile by a split map in a
+        // gate order of its own; the checks below use that order
+        int gbit0[5];
+        tc_split_map(o, gbit0);
+        bad += check_split(o);
+        for (int k = 0; k < 5; ++k)
+            if (o.blk[0].jgate[1 << k] != (1u << gbit0[k])) ++bad;
+        if (o.blk[0].jgate[31] != gate0) ++bad;
         // the scatter
         std::vector<int> seen(4096, 0);
         for (uint32_t t = 0; t < 128; ++t) {
@@ -144,6 +195,27 @@ int main()
         }
         minimal += at_min;
     }
-    std::printf("bad %d trials %d conflict-free scatter %d padded %d\n", bad, trials, minimal, padded);
+    // single-block passes of the four-group kernel
+    int singles = 0;
+    for (int trial = 0; trial < 600; ++trial) {
+        std::vector<int> all(12);
+        for (int j = 0; j < 12; ++j) all[j] = j;
+        std::shuffle(all.begin(), all.end(), rng);
+        std::vector<int> g0(all.begin(), all.begin() + 5);
+        TcOffsets o{};
+        o.nblocks = 1;
+        o.run_bits = (uint32_t)(rng() % 13);
+        o.nruns = 1u << (12 - o.run_bits);
+        default_geom(o.blk[0], g0);
+        const uint32_t gate0 = o.blk[0].jgate[31];
+        tc_choose_padding(o, (rng() % 3) != 0, 2 + (int)(rng() % 3));
+        int gbit0[5];
+        tc_split_map(o, gbit0);
+        bad += check_split(o);
+        if (o.blk[0].jgate[31] != gate0) ++bad;
+        ++singles;
+    }
+    std::printf("bad %d trials %d conflict-free scatter %d padded %d singles %d\n", bad, trials, minimal, padded,
+                singles);
     return bad ? 1 : 0;
 }
