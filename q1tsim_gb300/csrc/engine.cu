@@ -555,10 +555,11 @@ void q1g_state::measure_all(const size_t* cbits, size_t ncbits, uint64_t* res, s
         double* d_stmp = d_tot + ncols;
         double* d_u = d_stmp + scan_tmp;
         double* d_spc = d_u + nshots;
-        uscratch.ensure((2 * nshots + 64) * sizeof(uint64_t));
+        uscratch.ensure((2 * nshots + 64 + nshots / 2 + 1) * sizeof(uint64_t));
         uint64_t* d_out = uscratch.as<uint64_t>();
         uint64_t* d_word = d_out + nshots;
         uint64_t* d_cpos = d_word + nshots;
+        uint32_t* d_chunk = reinterpret_cast<uint32_t*>(d_cpos + 64);   // each shot's chunk
         h2d(d_cpos, cbit_of_pos.data(), 64 * sizeof(uint64_t), "upload cbits");
         launch("chunk_sums", double(ncols * N * bsz()), [&] {
             return launch_chunk_sums_dense(amps.p, prec, ncols * N, chunk, d_sums, stream);
@@ -603,6 +604,7 @@ void q1g_state::measure_all(const size_t* cbits, size_t ncbits, uint64_t* res, s
             a.word = d_word + off;
             a.nbits = nbits;
             a.d_cbit_of_pos = d_cpos;
+            a.chunk_of = d_chunk + off;
             launch("sample", double(counts[c] * chunk * bsz()), [&] { return launch_sample(a, stream); });
             off += counts[c];
         }

@@ -300,6 +300,10 @@ struct SampleArgs {
     uint64_t* word;         // per run
     int nbits;
     const uint64_t* d_cbit_of_pos;  // classical bit mask for each bit position
+    // nruns device words for each shot's chunk: with it the shots' chunks
+    // come from one merge of the sorted targets with the prefix (a
+    // separate launch) instead of a search per shot; nullptr: the search
+    uint32_t* chunk_of;
 };
 cudaError_t launch_sample(const SampleArgs& a, cudaStream_t st);
 // ---- batch.cu: many circuits in one persistent launch (complex64)

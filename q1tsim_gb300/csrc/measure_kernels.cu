@@ -7,6 +7,8 @@
 // are FP64 with a fixed reduction order, so repeated runs give identical
 // results.
 #include "common.cuh"
+#include <algorithm>
+
 #include "kernels.h"
 #include "sampling.cuh"
 
@@ -199,7 +201,7 @@ k_chunk_sums_dense(const T* __restrict__ a, uint64_t nchunks, uint64_t chunk, do
     for (uint64_t c = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; c < nchunks; c += warps) {
         R p[8];
         group_probs(a, c * chunk, chunk, lane, p);
-        const double s = warp_sum((double)group_sum(p));
+        const double s = chunk_total(group_sum(p), lane);
         if (lane == 0) out[c] = s;
     }
 }
@@ -208,12 +210,69 @@ template <typename T>
 __global__ void __launch_bounds__(256)
 k_sample(SampleArgs s)
 {
-    const uint64_t r = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-    if (r >= s.nruns) return;
-    uint64_t idx;
-    if (sample_one((const T*)s.amps, s.chunk, s.excl, s.nchunks, *s.total, s.u[r], threadIdx.x & 31, &idx)) {
-        s.outcome[r] = idx;
-        s.word[r] = outcome_word(idx, s.nbits, s.d_cbit_of_pos);
+    // one warp per shot, warps looping over the shots (a few blocks per SM
+    // rather than one short-lived block per eight shots)
+    const uint64_t nwarps = (uint64_t(gridDim.x) * blockDim.x) >> 5;
+    for (uint64_t r = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; r < s.nruns; r += nwarps) {
+        uint64_t idx;
+        if (sample_one((const T*)s.amps, s.chunk, s.excl, s.nchunks, *s.total, s.u[r], threadIdx.x & 31, &idx)) {
+            s.outcome[r] = idx;
+            s.word[r] = outcome_word(idx, s.nbits, s.d_cbit_of_pos);
+        }
+    }
+}
+
+// The chunk of every shot of a column: the largest c with excl[c] <=
+// target(u[r]), for sorted u, found by one merge of the targets with the
+// chunk prefix (excl first on ties).  The merge is cut into spans of
+// kMergeSpan steps (merge path): thread t finds where its span starts by a
+// binary search on its diagonal and walks it, so that every thread does the
+// same work whatever the distribution of the shots over the chunks.
+constexpr uint64_t kMergeSpan = 32;
+
+__global__ void k_locate_chunks(const double* __restrict__ excl, uint64_t nchunks, const double* __restrict__ u,
+                                const double* total_p, uint64_t nruns, uint32_t* __restrict__ chunk_of)
+{
+    const uint64_t d0 = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) * kMergeSpan;
+    const uint64_t len = nchunks + nruns;
+    if (d0 >= len) return;
+    const double total = *total_p;
+    // largest i in [max(0, d0 - nruns), min(d0, nchunks)] whose first i
+    // prefixes all precede the first d0 - i targets
+    uint64_t lo = d0 > nruns ? d0 - nruns : 0, hi = d0 < nchunks ? d0 : nchunks;
+    while (lo < hi) {
+        const uint64_t i = (lo + hi + 1) >> 1;     // candidate: excl[i-1] precedes target[d0-i]
+        const uint64_t j = d0 - i;
+        if (j >= nruns || excl[i - 1] <= shot_target(u[j], total)) lo = i;
+        else hi = i - 1;
+    }
+    uint64_t i = lo, j = d0 - lo;
+    const uint64_t end = d0 + kMergeSpan < len ? d0 + kMergeSpan : len;
+    double tj = j < nruns ? shot_target(u[j], total) : 0.0;
+    for (uint64_t d = d0; d < end; ++d) {
+        if (j < nruns && (i >= nchunks || excl[i] > tj)) {
+            chunk_of[j] = (uint32_t)(i - 1);   // excl[0] = 0 precedes every target
+            ++j;
+            if (j < nruns) tj = shot_target(u[j], total);
+        } else {
+            ++i;
+        }
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_sample_located(SampleArgs s, const uint32_t* __restrict__ chunk_of)
+{
+    const uint64_t nwarps = (uint64_t(gridDim.x) * blockDim.x) >> 5;
+    const double total = *s.total;
+    for (uint64_t r = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; r < s.nruns; r += nwarps) {
+        uint64_t idx;
+        const double target = shot_target(s.u[r], total);
+        if (sample_in_chunk((const T*)s.amps, s.chunk, s.excl, chunk_of[r], target, threadIdx.x & 31, &idx)) {
+            s.outcome[r] = idx;
+            s.word[r] = outcome_word(idx, s.nbits, s.d_cbit_of_pos);
+        }
     }
 }
 
@@ -417,8 +476,20 @@ cudaError_t launch_scale_columns(void* amps, int prec, uint64_t col_len, uint64_
 cudaError_t launch_sample(const SampleArgs& a, cudaStream_t st)
 {
     if (a.nruns == 0) return cudaSuccess;
-    const uint64_t threads = a.nruns * 32;
-    const unsigned grid = (unsigned)((threads + 255) / 256);
+    // 8 warps per block, 8 blocks per SM (64 warps): every SM full, each
+    // warp taking every nwarps-th shot
+    const uint64_t blocks = (a.nruns + 7) / 8;
+    const unsigned grid = (unsigned)std::min<uint64_t>(blocks, 152ull * 8);
+    if (a.chunk_of && a.nchunks < (uint64_t(1) << 32)) {
+        const uint64_t spans = (a.nchunks + a.nruns + kMergeSpan - 1) / kMergeSpan;
+        k_locate_chunks<<<(unsigned)((spans + 255) / 256), 256, 0, st>>>(a.excl, a.nchunks, a.u, a.total, a.nruns,
+                                                                          a.chunk_of);
+        if (a.prec == kC128)
+            k_sample_located<double2><<<grid, 256, 0, st>>>(a, a.chunk_of);
+        else
+            k_sample_located<float2><<<grid, 256, 0, st>>>(a, a.chunk_of);
+        return cudaGetLastError();
+    }
     if (a.prec == kC128)
         k_sample<double2><<<grid, 256, 0, st>>>(a);
     else

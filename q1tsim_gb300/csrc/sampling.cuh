@@ -5,8 +5,9 @@
 // Outcome probabilities are summed hierarchically, with the same arithmetic
 // in the reduction and in the search so the two agree: p_i = |a_i|^2 in the
 // state's precision, groups of 8 consecutive p_i summed sequentially in that
-// precision, chunks of 32 groups (256 amplitudes) summed in FP64, and an FP64
-// exclusive prefix over chunks.  A shot finds its chunk by a 32-ary warp
+// precision, chunks of 32 groups (256 amplitudes) summed in the state's
+// precision too (FP64 for complex128), and an FP64 exclusive prefix over
+// chunks.  A shot finds its chunk by a 32-ary warp
 // search on that prefix, its group by an FP64 warp scan of the chunk's 32
 // group sums, and its amplitude by a sequential scan of the group.
 #pragma once
@@ -81,27 +82,64 @@ __device__ __forceinline__ R group_sum(const R p[8])
     return s;
 }
 
+// Inclusive prefix of v over the warp's lanes, in v's precision: the order
+// in which the sampler adds a chunk's 32 group sums.
+template <typename R>
+__device__ __forceinline__ R warp_incl_scan(R v, int lane)
+{
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const R y = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += y;
+    }
+    return v;
+}
+
+// A chunk's total from its lanes' group sums (all lanes get it).
+// complex64: in FP32, in the sampler's scan order, so that the total is the
+// value the sampler's scan reaches at lane 31 (an FP64 warp reduction costs
+// 16 cycles of an SM's FP64 pipe per instruction; a chunk holds about 2^-22
+// of the mass at 30 qubits, so FP32 leaves it good to about 1e-14).
+// complex128: in FP64.
+__device__ __forceinline__ double chunk_total(float gs, int lane)
+{
+    return (double)__shfl_sync(0xffffffffu, warp_incl_scan(gs, lane), 31);
+}
+__device__ __forceinline__ double chunk_total(double gs, int) { return warp_sum(gs); }
+
 // Chunk sum of one warp's chunk (all lanes get it).
 template <typename T>
 __device__ __forceinline__ double chunk_sum(const T* a, uint64_t i0, uint64_t chunk, int lane)
 {
     typename ProbT<T>::R p[8];
     group_probs(a, i0, chunk, lane, p);
-    return warp_sum((double)group_sum(p));
+    return chunk_total(group_sum(p), lane);
 }
 
 // One shot, executed by a whole warp: the basis index whose inclusive
 // probability prefix first exceeds u * total.  Returns true on the lane that
 // holds the result in *idx.
+// The shot's target u * total, kept strictly inside the mass if rounding
+// pushed it onto the total (u < 1): the shot then lands on the last nonzero
+// amplitude.
+__device__ __forceinline__ double shot_target(double u, double total)
+{
+    const double target = u * total;
+    return target < total ? target : nextafter(total, 0.0);
+}
+
+// One shot whose chunk lo is known (the largest chunk c with excl[c] <=
+// target), executed by a whole warp.  Returns true on the lane that holds
+// the result in *idx.
+template <typename T>
+__device__ bool sample_in_chunk(const T* a, uint64_t chunk, const double* excl, uint64_t lo, double target,
+                                int lane, uint64_t* idx);
+
 template <typename T>
 __device__ bool sample_one(const T* a, uint64_t chunk, const double* excl, uint64_t nchunks, double total,
                            double u, int lane, uint64_t* idx)
 {
-    using R = typename ProbT<T>::R;
-    double target = u * total;
-    // u < 1, but keep the target strictly inside the mass if rounding pushed
-    // it onto the total: the shot then lands on the last nonzero amplitude.
-    if (!(target < total)) target = nextafter(total, 0.0);
+    const double target = shot_target(u, total);
     // Largest chunk c with excl[c] <= target (excl is non-decreasing and
     // excl[0] = 0).  The warp searches 32-ary: lane j probes lo + j * step,
     // and the last lane whose prefix is <= target narrows [lo, hi) to one
@@ -115,27 +153,35 @@ __device__ bool sample_one(const T* a, uint64_t chunk, const double* excl, uint6
         lo += (uint64_t)(31 - __clz(ok)) * step;    // lane 0 always qualifies
         hi = min(hi, lo + step);
     }
+    return sample_in_chunk(a, chunk, excl, lo, target, lane, idx);
+}
+
+template <typename T>
+__device__ bool sample_in_chunk(const T* a, uint64_t chunk, const double* excl, uint64_t lo, double target,
+                                int lane, uint64_t* idx)
+{
+    using R = typename ProbT<T>::R;
     const uint64_t i0 = lo * chunk;
     const double tl = target - excl[lo];
     R p[8];
     group_probs(a, i0, chunk, lane, p);
-    const double gs = (double)group_sum(p);
-    double incl = gs;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const double y = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += y;
-    }
-    const unsigned hit = __ballot_sync(0xffffffffu, gs > 0.0 && incl > tl);
-    const unsigned nz = __ballot_sync(0xffffffffu, gs > 0.0);
+    // the chunk's group sums scanned in the state's precision (the chunk
+    // sums add them in the same order, chunk_total)
+    // and the target's offset into the chunk compared in that precision too
+    // (it is at most the chunk's mass)
+    const R gs = group_sum(p);
+    const R incl = warp_incl_scan(gs, lane);
+    const R tlr = (R)tl;
+    const unsigned hit = __ballot_sync(0xffffffffu, gs > R(0) && incl > tlr);
+    const unsigned nz = __ballot_sync(0xffffffffu, gs > R(0));
     int owner;
-    double local;
+    R local;
     if (hit) {
         owner = __ffs(hit) - 1;
-        local = tl - (incl - gs);
+        local = tlr - (incl - gs);
     } else {
         owner = nz ? 31 - __clz(nz) : 0;
-        local = INFINITY;   // past the end: take the group's last nonzero amplitude
+        local = R(INFINITY);   // past the end: take the group's last nonzero amplitude
     }
     if (lane != owner) return false;
     int e_pick = -1, e_last = 0;
@@ -145,7 +191,7 @@ __device__ bool sample_one(const T* a, uint64_t chunk, const double* excl, uint6
         run = padd(run, p[e]);
         if (p[e] > R(0)) {
             e_last = e;
-            if (e_pick < 0 && (double)run > local) e_pick = e;
+            if (e_pick < 0 && run > local) e_pick = e;
         }
     }
     if (e_pick < 0) e_pick = e_last;
