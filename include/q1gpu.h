@@ -238,7 +238,8 @@ int q1g_plan_set_tensor_cores(q1g_plan* p, int enable);
  * write-back stores them as the second block's f16 operands in shared
  * memory, which its MMAs read directly; 4, the default: the same in a
  * kernel with four consumer groups, every pass's operands in shared
- * memory); a pair's tile may hold at
+ * memory; 5: as 4, and three consecutive blocks share a pass where their
+ * tile has runs of at least 64 bytes); a pair's tile may hold at
  * most max_high_positions positions at or above 2 MB strides (default 8: at
  * most 256 large pages per tile); an unpadded tile, one tensor-map copy, is
  * kept while its shared-memory bank wavefronts stay within conflict_slack

@@ -19,10 +19,10 @@ from .vectorstate import Plan, VectorState
 DEFAULT_TILING = Plan.DEFAULT_TC_TILING
 # tensor-core tilings tried beside the default (four consumer groups, pairs
 # whose second block reads operands the first stored) at the widest fusion
-# width: two groups with pairs through the staged tile, through registers
-# (warp shuffles) or through stored operands; no pairs; pairs over fewer
-# large pages; a tighter conflict slack
-TC_TILINGS = (DEFAULT_TILING, (1, 8, 2), (2, 8, 2), (3, 8, 2), (0, 8, 2), (4, 5, 4), (4, 8, 2))
+# width: three blocks per pass; two groups with pairs through the staged
+# tile, through registers (warp shuffles) or through stored operands; no
+# pairs; pairs over fewer large pages; a tighter conflict slack
+TC_TILINGS = (DEFAULT_TILING, (5, 8, 4), (1, 8, 2), (2, 8, 2), (3, 8, 2), (0, 8, 2), (4, 5, 4), (4, 8, 2))
 
 # (fusion width, dense complex64 blocks on tensor cores, tiling)
 CANDIDATES_C64 = tuple((5, True, t) for t in TC_TILINGS) + (

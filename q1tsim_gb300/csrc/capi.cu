@@ -399,7 +399,7 @@ int q1g_plan_create(size_t nr_bits, size_t ngates, const size_t* ks, const size_
         }
         if (fusion_width > 0) {
             p->blocks = fuse(p->gate_bits, (int)nr_bits, fusion_width);
-            order_blocks_for_tc_pairs(p->blocks, (int)nr_bits, p->tc_max_high);
+            order_blocks_for_tc_pairs(p->blocks, (int)nr_bits, p->tc_max_high, p->tc_pairs == 5 ? 3 : 2);
         } else {
             for (size_t g = 0; g < ngates; ++g) {
                 FusedBlock b;
@@ -438,7 +438,7 @@ int q1g_plan_set_gate_kinds(q1g_plan* p, const unsigned char* kinds, size_t ngat
         p->kinds.assign(kinds, kinds + ngates);
         if (p->width > 0) {
             p->blocks = fuse_runs(p->gate_bits, p->kinds, p->nbits, p->width);
-            order_blocks_for_tc_pairs(p->blocks, p->nbits, p->tc_max_high);
+            order_blocks_for_tc_pairs(p->blocks, p->nbits, p->tc_max_high, p->tc_pairs == 5 ? 3 : 2);
         }
         p->prefix_known = false;
         p->prefix_plan.reset();
@@ -503,11 +503,15 @@ int q1g_plan_set_tc_tiling(q1g_plan* p, int allow_pairs, int max_high_positions,
             throw Error(Q1G_ERR_INVALID_ARGUMENT, "max_high_positions must be in 0..12");
         if (conflict_slack < 1 || conflict_slack > 64)
             throw Error(Q1G_ERR_INVALID_ARGUMENT, "conflict_slack must be in 1..64");
-        if (allow_pairs < 0 || allow_pairs > 4)
-            throw Error(Q1G_ERR_INVALID_ARGUMENT, "allow_pairs must be in 0..4", (uint64_t)allow_pairs);
+        if (allow_pairs < 0 || allow_pairs > 5)
+            throw Error(Q1G_ERR_INVALID_ARGUMENT, "allow_pairs must be in 0..5", (uint64_t)allow_pairs);
+        // the block order is made for the passes' size (three blocks in mode
+        // 5): reorder the blocks when that changes
+        const bool regroup = (allow_pairs == 5) != (p->tc_pairs == 5);
         p->tc_pairs = allow_pairs;
         p->tc_max_high = max_high_positions;
         p->tc_slack = conflict_slack;
+        if (regroup) order_blocks_for_tc_pairs(p->blocks, p->nbits, p->tc_max_high, p->tc_pairs == 5 ? 3 : 2);
         // the compact prefix plan copies the tiling when it is made
         p->prefix_known = false;
         p->prefix_plan.reset();

@@ -289,7 +289,7 @@ void q1g_state::apply_unary_all(const double* mat)
             p->gate_bits.push_back({q});
         }
         p->blocks = fuse(p->gate_bits, nbits, width);
-        order_blocks_for_tc_pairs(p->blocks, nbits, p->tc_max_high);
+        order_blocks_for_tc_pairs(p->blocks, nbits, p->tc_max_high, p->tc_pairs == 5 ? 3 : 2);
         unary_plan = std::move(p);
     }
     std::vector<double> mats(8 * (size_t)nbits);
@@ -746,6 +746,9 @@ constexpr int kMinTcRunBits = 7;
 // default: at most 256 large pages per tile; a tile over 512 ran 2.4x
 // slower, one over 256 as fast as any).
 constexpr int kHighPosition = 18;
+// Shortest contiguous run (as a power of two of amplitudes) of a three-block
+// pass's tile: 8 amplitudes, 64 bytes.
+constexpr int kMinTripleRunBits = 3;
 
 static TcPass lower_tc_pass(const std::vector<const std::vector<cd>*>& mats,
                             const std::vector<const std::vector<int>*>& bits, int nbits, uint64_t ncols, int slack,
@@ -816,8 +819,9 @@ static TcPass lower_tc_pass(const std::vector<const std::vector<cd>*>& mats,
         }
         build_tc_image(md.data(), t.images.data() + kTcImageHalves, kTcLastBScaleLog2);
     }
-    // pair mode 4: the four-group kernel, every A operand in shared memory
-    const bool quad = pair_mode == 4;
+    // pair modes 4 and 5: the four-group kernel, every A operand in shared
+    // memory (5: three blocks per pass where they fit)
+    const bool quad = pair_mode >= 4;
     auto finish = [&] {
         if (!quad) return;
         t.offs.groups = 4;
@@ -836,6 +840,36 @@ static TcPass lower_tc_pass(const std::vector<const std::vector<cd>*>& mats,
         }
         build_tc_image(md.data(), t.images.data(), mats.size() == 1 ? kTcLastBScaleLog2 : 0);
     };
+    auto rebuild_image = [&](size_t bi, const int* gb) {
+        // block bi in the gate order a layout chose: matrix index bit k =
+        // tile bit gb[k]
+        std::vector<int> qk(5);
+        for (int k = 0; k < 5; ++k) qk[4 - k] = nbits - 1 - T[gb[k]];
+        const auto m32 = embed_matrix(*mats[bi], *bits[bi], qk);
+        std::vector<double> md(2 * 32 * 32);
+        for (size_t e = 0; e < m32.size(); ++e) {
+            md[2 * e] = m32[e].real();
+            md[2 * e + 1] = m32[e].imag();
+        }
+        build_tc_image(md.data(), t.images.data() + bi * kTcImageHalves,
+                       bi + 1 == mats.size() ? kTcLastBScaleLog2 : 0);
+    };
+    int gbits[kTcMaxBlocks][5];
+    // store boxes for the last block's write-back (an unpadded one-box tile)
+    std::vector<TcStoreBox> stores;
+    if (quad && mats.size() >= 2 && t.box.usable)
+        stores = tc_store_boxes(T.data(), nbits, ncols, t.offs.blk[mats.size() - 1].jgate[31]);
+    int store = -1;
+    if (quad && mats.size() >= 2 &&
+        tc_chain_layout(t.offs, t.box.usable != 0, slack, gbits, &t.cost, &t.ideal, &stores, &store)) {
+        if (t.offs.st_box) t.sbox = stores[(size_t)store].box;
+        // the later blocks read the operands the previous block's
+        // write-back scattered, in the gate orders the layout chose
+        for (size_t bi = 1; bi < mats.size(); ++bi) rebuild_image(bi, gbits[bi]);
+        finish();
+        return t;
+    }
+    if (mats.size() > 2) throw Error(Q1G_ERR_INVALID_ARGUMENT, "a three-block pass needs the four-group kernel");
     int gbit1[5];
     if (mats.size() == 2 && (pair_mode == 3 || quad) && tc_direct_layout(t.offs, t.box.usable != 0, slack, gbit1)) {
         // the second block reads the operands the first block's write-back
@@ -858,28 +892,30 @@ static TcPass lower_tc_pass(const std::vector<const std::vector<cd>*>& mats,
     return t;
 }
 
-// Whether blocks on qubits qa and qb could share a tensor-core pass: their
+// Whether blocks on these qubit sets could share a tensor-core pass: their
 // positions fit one 12-position tile, at most max_high of its positions lie
 // at 2 MB strides or more, and the tile has runs of >= 128 amplitudes or is
 // one tensor-map box (the rule plan_run applies, before any padding choice).
-static bool tc_pairable(const std::vector<int>& qa, const std::vector<int>& qb, int nbits, int max_high)
+static bool tc_pairable(const std::vector<const std::vector<int>*>& qs, int nbits, int max_high)
 {
-    std::vector<int> u = qa;
-    for (int q : qb)
-        if (std::find(u.begin(), u.end(), q) == u.end()) u.push_back(q);
+    std::vector<int> u;
+    for (auto* q : qs)
+        for (int x : *q)
+            if (std::find(u.begin(), u.end(), x) == u.end()) u.push_back(x);
     if (u.size() > 12 || nbits < 12) return false;
-    const auto T = tile_positions({&qa, &qb}, nbits);
+    const auto T = tile_positions(qs, nbits);
     int high = 0;
     for (int p : T) high += p >= kHighPosition;
     return high <= max_high && (tile_run_bits(T) >= kMinTcRunBits || tc_tile_box(T.data(), nbits, 1).usable);
 }
 
-void order_blocks_for_tc_pairs(std::vector<FusedBlock>& blocks, int nbits, int max_high)
+void order_blocks_for_tc_pairs(std::vector<FusedBlock>& blocks, int nbits, int max_high, int group)
 {
     // Blocks on disjoint qubits commute.  Take the earliest block whose
     // predecessors (the last earlier block on each of its qubits) are all
-    // taken, then, if one is ready, the earliest ready block that can share
-    // its tensor-core pass, so that plan_run finds them next to each other.
+    // taken, then, while the pass has room (group blocks), the earliest
+    // ready block that can share its tensor-core pass, so that plan_run
+    // finds them next to each other.
     const int m = (int)blocks.size();
     if (m < 3 || nbits < 12) return;
     auto candidate = [&](int i) {
@@ -911,11 +947,23 @@ void order_blocks_for_tc_pairs(std::vector<FusedBlock>& blocks, int nbits, int m
         const int a = *ready.begin();
         take(a);
         if (!candidate(a)) continue;
-        for (int b : ready)
-            if (candidate(b) && tc_pairable(blocks[a].qubits, blocks[b].qubits, nbits, max_high)) {
-                take(b);
-                break;
+        std::vector<const std::vector<int>*> pass = {&blocks[a].qubits};
+        while ((int)pass.size() < group) {
+            int next = -1;
+            for (int b : ready) {
+                if (!candidate(b)) continue;
+                pass.push_back(&blocks[b].qubits);
+                const bool ok = tc_pairable(pass, nbits, max_high);
+                pass.pop_back();
+                if (ok) {
+                    next = b;
+                    break;
+                }
             }
+            if (next < 0) break;
+            pass.push_back(&blocks[next].qubits);
+            take(next);
+        }
     }
     std::vector<FusedBlock> out;
     out.reserve(m);
@@ -1178,13 +1226,17 @@ void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n, bool subs
     // shape: a circuit run again builds no images (about 50 us per block on
     // the host, which small states do not hide behind their passes).
     auto lower_tc_cached = [&](size_t i, int nblk) -> TcPass {
-        if (p->tc_memo.size() != 2 * nb) p->tc_memo.assign(2 * nb, TcPassMemo{});
-        TcPassMemo& e = p->tc_memo[2 * i + (size_t)(nblk - 1)];
+        if (p->tc_memo.size() != kTcMaxBlocks * nb) p->tc_memo.assign(kTcMaxBlocks * nb, TcPassMemo{});
+        TcPassMemo& e = p->tc_memo[kTcMaxBlocks * i + (size_t)(nblk - 1)];
         const int variant = 8 * p->tc_slack + p->tc_pairs;
         bool hit = e.nblocks == nblk && e.nbits == s->nbits && e.ncols == s->ncols && e.slack == variant;
         for (int j = 0; hit && j < nblk; ++j) hit = e.bits[j] == bbits[i + j] && e.mats[j] == bmats[i + j];
         if (!hit) {
-            if (nblk == 2) {
+            if (nblk == 3) {
+                e.pass = lower_tc_pass({&bmats[i], &bmats[i + 1], &bmats[i + 2]},
+                                       {&bbits[i], &bbits[i + 1], &bbits[i + 2]}, s->nbits, s->ncols, p->tc_slack,
+                                       p->tc_pairs);
+            } else if (nblk == 2) {
                 e.pass = lower_tc_pass({&bmats[i], &bmats[i + 1]}, {&bbits[i], &bbits[i + 1]}, s->nbits, s->ncols,
                                        p->tc_slack, p->tc_pairs);
                 if ((e.pass.offs.shuffle || e.pass.offs.direct) && e.pass.offs.pad_shift < 31) {
@@ -1198,7 +1250,7 @@ void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n, bool subs
                 }
             } else
                 e.pass = lower_tc_pass({&bmats[i]}, {&bbits[i]}, s->nbits, s->ncols, p->tc_slack,
-                                       p->tc_pairs == 4 ? 4 : 1);
+                                       p->tc_pairs >= 4 ? 4 : 1);
             e.nblocks = nblk;
             e.slack = variant;
             e.nbits = s->nbits;
@@ -1257,24 +1309,54 @@ void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n, bool subs
         const GateOp& op = ops[i];
         if (op.kind == GateOp::Noop) continue;
         if (eligible(i)) {
-            // two consecutive blocks share a pass when their qubits fit one
-            // 12-position tile with runs of >= 128 amplitudes
+            // consecutive blocks share a pass when their qubits fit one
+            // 12-position tile with runs of >= 128 amplitudes or as one
+            // tensor-map box: up to three in the four-group kernel's direct
+            // chain in pair mode 5, else two
             TcPass t;
-            bool paired = false;
-            if (p->tc_pairs && i + 1 < nb && eligible(i + 1) &&
-                union_size(positions_of(bbits[i], s->nbits), positions_of(bbits[i + 1], s->nbits)) <= 12) {
-                const auto T2 = tile_positions({&bbits[i], &bbits[i + 1]}, s->nbits);
+            int group = 1;
+            // -1: blocks i .. i+k-1 do not fit one tile; else its run bits
+            auto fits = [&](int k) {
+                std::vector<const std::vector<int>*> bs;
+                std::vector<int> u;
+                for (int j = 0; j < k; ++j) {
+                    bs.push_back(&bbits[i + j]);
+                    for (int q : positions_of(bbits[i + j], s->nbits))
+                        if (std::find(u.begin(), u.end(), q) == u.end()) u.push_back(q);
+                }
+                if (u.size() > 12) return -1;
+                const auto Tk = tile_positions(bs, s->nbits);
                 int high = 0;
-                for (int p : T2) high += p >= kHighPosition;
-                const int L2 = tile_run_bits(T2);
-                if (high <= p->tc_max_high &&
-                    (L2 >= kMinTcRunBits || tc_tile_box(T2.data(), s->nbits, s->ncols).usable)) {
-                    t = lower_tc_cached(i, 2);
-                    // short runs only as one unpadded tensor-map copy
-                    paired = L2 >= kMinTcRunBits || t.offs.pad_shift >= 31;
+                for (int q : Tk) high += q >= kHighPosition;
+                const int L = tile_run_bits(Tk);
+                if (high > p->tc_max_high) return -1;
+                if (L < kMinTcRunBits && !tc_tile_box(Tk.data(), s->nbits, s->ncols).usable) return -1;
+                return L;
+            };
+            if (p->tc_pairs == 5 && i + 2 < nb && eligible(i + 1) && eligible(i + 2)) {
+                const int L3 = fits(3);
+                if (L3 >= 0) {
+                    t = lower_tc_cached(i, 3);
+                    // short runs only as one unpadded tensor-map copy; a
+                    // third block only where the tile's runs are at least
+                    // 64 bytes (a copy of 16- or 32-byte runs wastes DRAM
+                    // sectors: such passes ran at 19-46 % of DRAM rate) and
+                    // the layout keeps the bank wavefronts within twice the
+                    // minimum (a conflicted write-back costs more than the
+                    // saved pass)
+                    if ((L3 >= kMinTcRunBits || t.offs.pad_shift >= 31) && L3 >= kMinTripleRunBits &&
+                        t.cost <= 2 * t.ideal)
+                        group = 3;
                 }
             }
-            if (!paired) t = lower_tc_cached(i, 1);
+            if (group == 1 && p->tc_pairs && i + 1 < nb && eligible(i + 1)) {
+                const int L2 = fits(2);
+                if (L2 >= 0) {
+                    t = lower_tc_cached(i, 2);
+                    if (L2 >= kMinTcRunBits || t.offs.pad_shift >= 31) group = 2;
+                }
+            }
+            if (group == 1) t = lower_tc_cached(i, 1);
             begin();
             if (!any_tc) {
                 s->errbuf.ensure(sizeof(int));
@@ -1286,9 +1368,10 @@ void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n, bool subs
             const uint64_t total = s->total();
             s->launch("fused_tc_c64", 2.0 * total * s->bsz(), [&] {
                 return launch_fused_tc(s->amps.as<float2>(), total >> 12, t.tilemap, t.offs, t.box, img,
-                                       s->errbuf.as<int>(), s->sm_count(), s->stream, s->tc_wait_ns);
+                                       s->errbuf.as<int>(), s->sm_count(), s->stream, s->tc_wait_ns,
+                                       t.offs.st_box ? &t.sbox : nullptr);
             });
-            if (paired) ++i;   // the next block rode in this pass
+            i += (size_t)(group - 1);   // the next blocks rode in this pass
         } else if (op.kind == GateOp::Dense &&
                    dense_tiled_applies(s->prec, s->nbits, op.t, op.map, s->fp64_exact)) {
             begin();

@@ -206,6 +206,8 @@ struct TcPass {
     TcOffsets offs{};
     TcTileBox box{};                // the tile as a tensor-map box
     std::vector<uint16_t> images;   // nblocks x kTcImageHalves f16
+    long cost = 0, ideal = 0;       // the layout's predicted bank wavefronts per warp (chain layouts)
+    TcTileBox sbox{};               // the storers' box when offs.st_box
 };
 // A pass's lowering kept by its plan, with what it was made from.
 struct TcPassMemo {
@@ -213,8 +215,8 @@ struct TcPassMemo {
     int nbits = -1;
     int slack = 0;          // 8 x conflict slack + pair mode the lowering was made for
     uint64_t ncols = 0;
-    std::vector<int> bits[2];
-    std::vector<std::complex<double>> mats[2];
+    std::vector<int> bits[kTcMaxBlocks];
+    std::vector<std::complex<double>> mats[kTcMaxBlocks];
     TcPass pass;
 };
 }  // namespace q1g
@@ -236,13 +238,14 @@ struct q1g_plan {
     size_t prefix_len = 0;
     uint64_t prefix_mask = 0;
     std::unique_ptr<q1g_plan> prefix_plan;
-    std::vector<q1g::TcPassMemo> tc_memo;   // by 2 * first block + block count - 1 (plan_run)
+    std::vector<q1g::TcPassMemo> tc_memo;   // by 3 * first block + block count - 1 (plan_run)
     // Tensor-core tiling (q1g_plan_set_tc_tiling, tuned by autotune.py):
     // whether two blocks may share a pass (0 no; 1 the second block reads
     // the first's results from the staged tile; 2 from registers, by warp
     // shuffles; 3 as operands the first block's write-back stored in the
     // stage, with no split of its own; 4 the same in the four-group kernel,
-    // whose single-block passes also keep A in shared memory), how many tile positions a pair's tile may have at or above
+    // whose single-block passes also keep A in shared memory; 5 as 4 with up
+    // to three blocks per pass), how many tile positions a pair's tile may have at or above
     // 2 MB strides, and how many times the minimum bank wavefronts an
     // unpadded one-box tile may take.
     int tc_pairs = 4;
@@ -258,9 +261,9 @@ struct q1g_plan {
 namespace q1g {
 void plan_run(q1g_plan* p, q1g_state* s, const double* mats, size_t n, bool subspace_prefix = true);
 // Reorders a plan's blocks (blocks on disjoint qubits commute) so that blocks
-// that can share a tensor-core pass follow each other; max_high as
-// q1g_plan::tc_max_high.
-void order_blocks_for_tc_pairs(std::vector<FusedBlock>& blocks, int nbits, int max_high);
+// that can share a tensor-core pass follow each other, up to `group` of them
+// (3 in pair mode 4, else 2); max_high as q1g_plan::tc_max_high.
+void order_blocks_for_tc_pairs(std::vector<FusedBlock>& blocks, int nbits, int max_high, int group);
 // noalloc.cu: the sampler whose scratch is a fixed device array.
 void sample_shots_noalloc(const void* d_amps, int precision, size_t nr_bits, const double* d_sorted_uniforms,
                           size_t nshots, uint64_t* d_outcomes, uint64_t* d_words, const size_t* cbits,

@@ -60,6 +60,7 @@
 
 #include <cstring>
 #include <algorithm>
+#include <functional>
 #include <map>
 #include <mutex>
 #include <set>
@@ -463,10 +464,10 @@ __device__ __forceinline__ void writeback_row(uint8_t* raw, uint32_t rowb, const
     }
 }
 
-// The first block's results of a direct pair (TcOffsets::direct): each
-// output amplitude, still scaled, split into hi/lo f16 pairs and stored as
-// the second block's A operand -- hi plane at abase, lo plane 16 KB above --
-// at offset rowpart ^ scat_gate[g].
+// A block's results in a direct pass (TcOffsets::direct): each output
+// amplitude, still scaled, split into hi/lo f16 pairs and stored as the
+// next block's A operand -- hi plane at abase, lo plane 16 KB above -- at
+// offset rowpart ^ scat_gate[g].
 __device__ __forceinline__ void writeback_scatter(uint32_t abase, uint32_t rowpart, const uint32_t* scat_gate,
                                                   uint32_t td)
 {
@@ -622,7 +623,7 @@ template <int NG>
 __global__ void __launch_bounds__(TcShape<NG>::kThreads, 1)
 k_fused_tc(float2* __restrict__ a, uint64_t ntiles, const __grid_constant__ IndexMap tilemap,
            const __grid_constant__ TcOffsets offs, const __grid_constant__ CUtensorMap tmap,
-           const uint4* __restrict__ bimage, int* __restrict__ err)
+           const __grid_constant__ CUtensorMap tmap_st, const uint4* __restrict__ bimage, int* __restrict__ err)
 {
     using Sh = TcShape<NG>;
     extern __shared__ uint8_t smem_raw[];
@@ -725,8 +726,16 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, const __grid_constant__ Inde
             if (offs.use_tma) {
                 if (lane == 0) {
                     int c[5];
-                    tile_coords(tile, offs, c);
-                    tma_store_5d(&tmap, c, st);
+                    if (offs.st_box) {
+                        // the last block wrote the store box's layout
+#pragma unroll
+                        for (int d = 0; d < 5; ++d)
+                            c[d] = (int)((uint32_t)(tile >> offs.st_tshift[d]) & offs.st_tmask[d]);
+                        tma_store_5d(&tmap_st, c, st);
+                    } else {
+                        tile_coords(tile, offs, c);
+                        tma_store_5d(&tmap, c, st);
+                    }
                 }
             } else {
                 const uint64_t base = expand_index(tile, tilemap);
@@ -760,13 +769,15 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, const __grid_constant__ Inde
         const uint32_t mbar = sbase + kOffMma + 8u * g;
         // row t of an A operand in shared memory (SWIZZLE_128B, 128 B rows)
         const uint32_t arow = (t >> 3) * 1024u + (t & 7u) * 128u;
-        uint32_t rowb0 = 0, rowb1 = 0, rowpart = 0, sp_tb = 0, sp_ta = 0;
+        uint32_t rowb0 = 0, rowb1 = 0, rowb2 = 0, rowpart0 = 0, rowpart1 = 0, sp_tb = 0, sp_ta = 0;
 #pragma unroll
         for (int r = 0; r < 7; ++r)
             if ((t >> r) & 1u) {
                 rowb0 += offs.blk[0].rowoff[r];
                 rowb1 += offs.blk[1].rowoff[r];
-                rowpart ^= offs.scat_row[r];
+                rowb2 += offs.blk[2].rowoff[r];
+                rowpart0 ^= offs.scat_row[0][r];
+                rowpart1 ^= offs.scat_row[1][r];
                 sp_tb += offs.sp_thoff[r];
                 sp_ta ^= offs.sp_athr[r];
             }
@@ -787,10 +798,10 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, const __grid_constant__ Inde
             const bool shuf = !Sh::kSmemA && offs.shuffle != 0;
             float2 x[32];
 #pragma unroll
-            for (int b = 0; b < 2; ++b) {
+            for (int b = 0; b < kTcMaxBlocks; ++b) {
                 if ((uint32_t)b >= nblocks) break;
                 const TcBlockGeom& G = offs.blk[b];
-                const uint32_t rowb = b ? rowb1 : rowb0;
+                const uint32_t rowb = b == 0 ? rowb0 : (b == 1 ? rowb1 : rowb2);
                 // the previous block's results are all staged (or, shuffled,
                 // already in this thread's registers)
                 if (b > 0 && !shuf && !direct) group_sync(gbar);
@@ -888,7 +899,7 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, const __grid_constant__ Inde
                     writeback_regs(td, x);
                     swap_reg_lane_bits(x, offs.swap_lane, (uint32_t)lane);
                 } else if (direct) {
-                    writeback_scatter(abase, rowpart, offs.scat_gate, td);
+                    writeback_scatter(abase, b == 0 ? rowpart0 : rowpart1, offs.scat_gate[b < 1 ? 0 : 1], td);
                 } else {
                     writeback_row<false>(raw, rowb, G, td, offs.unscale);
                 }
@@ -946,6 +957,33 @@ int warp_wavefronts(const uint32_t* order, uint32_t pad, int width)
     return total;
 }
 
+// warp_wavefronts for a layout that puts tile bit j at element bit sbit[j]
+// (unpadded): 8-byte or 16-byte accesses, lanes = rows with row bit r at
+// tile coordinate order[r].
+int warp_wavefronts_map(const uint32_t* order, const int* sbit, int width)
+{
+    const uint32_t lanes_per_phase = width == 16 ? 8 : 16;
+    const uint32_t wpl = (uint32_t)width / 4;
+    int total = 0;
+    for (uint32_t ph = 0; ph < 32 / lanes_per_phase; ++ph) {
+        uint32_t words[64];
+        uint32_t nw = 0;
+        for (uint32_t l = ph * lanes_per_phase; l < (ph + 1) * lanes_per_phase; ++l) {
+            uint32_t e = 0;
+            for (int r = 0; r < 5; ++r)
+                if ((l >> r) & 1u) e |= 1u << sbit[__builtin_ctz(order[r])];
+            for (uint32_t w = 0; w < wpl; ++w) words[nw++] = 2 * e + w;
+        }
+        std::sort(words, words + nw);
+        int per_bank[32] = {0};
+        int m = 0;
+        for (uint32_t i = 0; i < nw; ++i)
+            if (i == 0 || words[i] != words[i - 1]) m = std::max(m, ++per_bank[words[i] % 32]);
+        total += m;
+    }
+    return total;
+}
+
 // The order of a block's 7 row bits (which tile coordinates the low lane
 // bits select) with the fewest wavefronts under padding `pad`.  Rows are
 // independent in the GEMM, so any order is correct; only the row bits that
@@ -974,7 +1012,7 @@ int best_row_order(const TcBlockGeom& G, uint32_t pad, uint32_t* order)
 }
 
 // Sets the padding fields and both blocks' row orders and staged offsets.
-void apply_layout(TcOffsets& o, uint32_t pad, const uint32_t (&order)[2][7])
+void apply_layout(TcOffsets& o, uint32_t pad, const uint32_t (&order)[kTcMaxBlocks][7])
 {
     o.pad_shift = pad;
     o.stage_bytes = kTileBytes + (pad < 31 ? 16u * (4096u >> pad) : 0u);
@@ -1039,7 +1077,7 @@ bool tc_direct_layout(TcOffsets& o, bool tma_ok, int conflict_slack, int* gbit1)
     struct Best {
         long cost = -1;
         uint32_t pad = 31;
-        uint32_t order[2][7] = {};
+        uint32_t order[kTcMaxBlocks][7] = {};
         int g1[5] = {};
     } best;
     // the choice depends only on the geometry and the slack: remember it
@@ -1166,12 +1204,12 @@ bool tc_direct_layout(TcOffsets& o, bool tma_ok, int conflict_slack, int* gbit1)
     G1.vec2 = G1.jgate[1] == 1u ? 1u : 0u;
     apply_layout(o, best.pad, best.order);
     for (int i = 0; i < 7; ++i)
-        o.scat_row[i] = direct_bit_offset(__builtin_ctz(best.order[0][i]), best.g1, best.order[1]);
+        o.scat_row[0][i] = direct_bit_offset(__builtin_ctz(best.order[0][i]), best.g1, best.order[1]);
     for (int g = 0; g < 32; ++g) {
         uint32_t a = 0;
         for (int j = 0; j < 12; ++j)
             if ((o.blk[0].jgate[g] >> j) & 1u) a ^= direct_bit_offset(j, best.g1, best.order[1]);
-        o.scat_gate[g] = a;
+        o.scat_gate[0][g] = a;
     }
     // both operand planes (2 x 16 KB) at 1024-byte aligned stage bases
     o.stage_bytes = (o.stage_bytes + 1023u) & ~1023u;
@@ -1341,9 +1379,238 @@ void tc_split_map(TcOffsets& o, int* gbit0)
             uint32_t a = 0;
             for (int j = 0; j < 12; ++j)
                 if ((G.jgate[gi] >> j) & 1u) a ^= direct_bit_offset(j, g1, o.blk[1].jrow_bit);
-            o.scat_gate[gi] = a;
+            o.scat_gate[0][gi] = a;
         }
     }
+}
+
+bool tc_chain_layout(TcOffsets& o, bool tma_ok, int conflict_slack, int (*gbits)[5], long* cost_out,
+                     long* ideal_out, const std::vector<TcStoreBox>* stores, int* store_out)
+{
+    if (stores && stores->empty()) stores = nullptr;
+    const int nb = (int)o.nblocks;
+    if (nb < 2 || nb > kTcMaxBlocks) return false;
+    uint32_t gate[kTcMaxBlocks];
+    std::vector<int> rows[kTcMaxBlocks];
+    for (int b = 0; b < nb; ++b) {
+        gate[b] = o.blk[b].jgate[31];
+        if (__builtin_popcount(gate[b]) != 5) return false;
+        for (int j = 0; j < 12; ++j)
+            if (!((gate[b] >> j) & 1u)) rows[b].push_back(j);
+    }
+    // per warp: 64 scattered 4-byte stores per transition, the last block's
+    // write-back (32 8-byte or 16 16-byte stores)
+    const long ideal = 64L * nb;
+    struct Best {
+        long cost = -1;
+        uint32_t pad = 31;
+        uint32_t order[kTcMaxBlocks][7] = {};
+        int g[kTcMaxBlocks][5] = {};
+        int store = -1;
+    } best;
+    static std::mutex mu;
+    static std::unordered_map<std::string, Best> memo;
+    std::string key(1, tma_ok ? 'T' : 'P');
+    key.append((const char*)&conflict_slack, sizeof(conflict_slack));
+    key.append((const char*)&o.run_bits, sizeof(o.run_bits));
+    key.append((const char*)gate, sizeof(uint32_t) * nb);
+    if (stores) {
+        // the store boxes follow from the tile's runs and the last gates
+        for (const auto& sb : *stores) key.append((const char*)sb.sbit, sizeof(sb.sbit));
+    }
+    bool found = false;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        auto it = memo.find(key);
+        if (it != memo.end()) {
+            best = it->second;
+            found = true;
+        }
+    }
+    uint32_t order[kTcMaxBlocks][7];
+    int g[kTcMaxBlocks][5];
+    uint32_t pad = 31;
+    // transition k -> k+1 from block k's lanes (order[k][0..4]); cost so far
+    std::function<void(int, long)> step = [&](int k, long cost) {
+        int lanes[5];
+        for (int i = 0; i < 5; ++i) lanes[i] = __builtin_ctz(order[k][i]);
+        const uint32_t gn = gate[k + 1];
+        std::vector<int> GL, RL, GO, RO;
+        for (int i = 0; i < 5; ++i) ((gn >> lanes[i]) & 1u ? GL : RL).push_back(lanes[i]);
+        std::sort(GL.begin(), GL.end());
+        std::sort(RL.begin(), RL.end());
+        for (int j = 0; j < 12; ++j)
+            if (((gn >> j) & 1u) && std::find(GL.begin(), GL.end(), j) == GL.end()) GO.push_back(j);
+        for (int j : rows[k + 1])
+            if (std::find(RL.begin(), RL.end(), j) == RL.end()) RO.push_back(j);
+        int* gk = g[k + 1];
+        for (size_t i = 0; i < GL.size(); ++i) gk[i] = GL[i];
+        for (size_t i = 0; i < GO.size(); ++i) gk[GL.size() + i] = GO[i];
+        // the lanes that are rows of block k+1 take its row bits (a-2)..2,
+        // after the ones its gate bits 2-4 already take (a conflict-free
+        // scatter when a >= 2)
+        const int a = (int)GL.size();
+        const int first = std::max(0, std::min(a - 2, 3 - (int)RL.size()));
+        bool taken[7] = {};
+        for (size_t i = 0; i < RL.size(); ++i) taken[first + i] = true;
+        std::vector<int> FL, FW;
+        for (int sl = 0; sl < 7; ++sl)
+            if (!taken[sl]) (sl < 5 ? FL : FW).push_back(sl);
+        const bool last = k + 2 == nb;
+        const int nro = (int)RO.size(), nfl = (int)FL.size();
+        auto fill = [&](const std::vector<int>& lane_bits, int at4) {
+            // lane_bits into the free lane slots (at4: the one for slot 4,
+            // -1 if none), the rest of RO into the warp slots, ascending
+            uint32_t* ok1 = order[k + 1];
+            for (size_t i = 0; i < RL.size(); ++i) ok1[first + i] = 1u << RL[i];
+            size_t li = 0;
+            for (int sl : FL) {
+                if (sl == 4 && at4 >= 0) ok1[sl] = 1u << at4;
+                else {
+                    while (li < lane_bits.size() && lane_bits[li] == at4) ++li;
+                    ok1[sl] = 1u << lane_bits[li++];
+                }
+            }
+            size_t wi = 0;
+            for (int j : RO)
+                if (std::find(lane_bits.begin(), lane_bits.end(), j) == lane_bits.end()) ok1[FW[wi++]] = 1u << j;
+        };
+        auto scatter_cost = [&]() {
+            uint32_t pat[5];
+            for (int i = 0; i < 5; ++i) pat[i] = direct_bit_offset(lanes[i], gk, order[k + 1]);
+            return 64L * scatter_wavefronts(pat);
+        };
+        if (last) {
+            // every choice of the lane rows, and of the one in slot 4 (it
+            // selects the write-back's phase)
+            const bool v2 = gk[0] == 0;
+            const int width = v2 ? 16 : 8, nwb = v2 ? 16 : 32;
+            const bool slot4_free = std::find(FL.begin(), FL.end(), 4) != FL.end();
+            for (uint32_t m = 0; m < (1u << nro); ++m) {
+                if (__builtin_popcount(m) != nfl) continue;
+                std::vector<int> lb;
+                for (int i = 0; i < nro; ++i)
+                    if ((m >> i) & 1u) lb.push_back(RO[i]);
+                const size_t n4 = slot4_free ? lb.size() : 1;
+                for (size_t c4 = 0; c4 < n4; ++c4) {
+                    fill(lb, slot4_free ? lb[c4] : -1);
+                    // the write-back in the load layout, or (unpadded) in
+                    // the best store box
+                    long wb = -1;
+                    int si = -1;
+                    if (stores && pad >= 31) {
+                        for (size_t c = 0; c < stores->size(); ++c) {
+                            const long w = nwb * (long)warp_wavefronts_map(order[k + 1], (*stores)[c].sbit, width);
+                            if (wb < 0 || w < wb) {
+                                wb = w;
+                                si = (int)c;
+                            }
+                        }
+                    } else {
+                        wb = nwb * (long)warp_wavefronts(order[k + 1], pad, width);
+                    }
+                    const long total = cost + scatter_cost() + wb;
+                    if (best.cost < 0 || total < best.cost) {
+                        best.cost = total;
+                        best.pad = pad;
+                        std::memcpy(best.order, order, sizeof(order));
+                        std::memcpy(best.g, g, sizeof(g));
+                        best.store = si;
+                    }
+                }
+            }
+        } else {
+            // a middle block's lane rows: the next block's gate bits first
+            // (its scatter then has gate lanes), or simply the lowest
+            std::vector<int> pref = RO;
+            std::stable_sort(pref.begin(), pref.end(), [&](int x, int y) {
+                return ((gate[k + 2] >> x) & 1u) > ((gate[k + 2] >> y) & 1u);
+            });
+            for (int variant = 0; variant < 2; ++variant) {
+                std::vector<int> lb(variant == 0 ? pref.begin() : RO.begin(),
+                                    (variant == 0 ? pref.begin() : RO.begin()) + nfl);
+                std::sort(lb.begin(), lb.end());
+                fill(lb, -1);
+                const long c = cost + scatter_cost();
+                if (best.cost >= 0 && c + 64L * (nb - k - 1) >= best.cost) continue;
+                step(k + 1, c);
+            }
+        }
+    };
+    const uint32_t cands[] = {31, 11, 10, 9, 8, 7, 6, 5};
+    for (uint32_t pc : cands) {
+        if (found) break;
+        if (pc < 31 && tma_ok && best.cost >= 0 && best.cost <= conflict_slack * ideal) break;
+        pad = pc;
+        for (uint32_t lm = 0; lm < 128; ++lm) {
+            if (__builtin_popcount(lm) != 5) continue;
+            int c = 0;
+            for (int r = 0; r < 7; ++r)
+                if ((lm >> r) & 1u) order[0][c++] = 1u << rows[0][r];
+            for (int r = 0; r < 7; ++r)
+                if (!((lm >> r) & 1u)) order[0][c++] = 1u << rows[0][r];
+            step(0, 0);
+            if (best.cost == ideal) break;
+        }
+        if (best.cost == ideal) break;
+    }
+    if (best.cost < 0) return false;
+    if (!found) {
+        std::lock_guard<std::mutex> lock(mu);
+        if (memo.size() > 4096) memo.clear();
+        memo.emplace(key, best);
+    }
+    if (cost_out) *cost_out = best.cost;
+    if (ideal_out) *ideal_out = ideal;
+    // later blocks in their new gate orders
+    for (int b = 1; b < nb; ++b) {
+        TcBlockGeom& G = o.blk[b];
+        for (int gi = 0; gi < 32; ++gi) {
+            uint32_t jc = 0;
+            for (int k = 0; k < 5; ++k)
+                if ((gi >> k) & 1) jc |= 1u << best.g[b][k];
+            G.jgate[gi] = jc;
+        }
+        G.vec2 = G.jgate[1] == 1u ? 1u : 0u;
+        for (int k = 0; k < 5; ++k) gbits[b][k] = best.g[b][k];
+    }
+    apply_layout(o, best.pad, best.order);
+    for (int k = 0; k + 1 < nb; ++k) {
+        for (int i = 0; i < 7; ++i)
+            o.scat_row[k][i] = direct_bit_offset(__builtin_ctz(best.order[k][i]), best.g[k + 1], best.order[k + 1]);
+        for (int gi = 0; gi < 32; ++gi) {
+            uint32_t a = 0;
+            for (int j = 0; j < 12; ++j)
+                if ((o.blk[k].jgate[gi] >> j) & 1u) a ^= direct_bit_offset(j, best.g[k + 1], best.order[k + 1]);
+            o.scat_gate[k][gi] = a;
+        }
+    }
+    o.stage_bytes = (o.stage_bytes + 1023u) & ~1023u;
+    o.direct = 1;
+    o.shuffle = 0;
+    o.st_box = 0;
+    if (store_out) *store_out = best.store;
+    if (stores && best.store >= 0) {
+        // the last block writes the chosen store box's layout
+        const TcStoreBox& sb = (*stores)[best.store];
+        TcBlockGeom& L = o.blk[nb - 1];
+        auto off = [&](uint32_t x) {
+            uint32_t a = 0;
+            for (int j = 0; j < 12; ++j)
+                if ((x >> j) & 1u) a += 8u << sb.sbit[j];
+            return a;
+        };
+        for (int r = 0; r < 7; ++r) L.rowoff[r] = off(L.jrow_bit[r]);
+        for (int gi = 0; gi < 32; ++gi) L.gateoff[gi] = off(L.jgate[gi]);
+        if (best.store > 0) {
+            o.st_box = 1;
+            for (int d = 0; d < 5; ++d) {
+                o.st_tshift[d] = sb.box.tshift[d];
+                o.st_tmask[d] = sb.box.tmask[d];
+            }
+        }
+    }
+    return true;
 }
 
 void tc_choose_padding(TcOffsets& o, bool tma_ok, int conflict_slack)
@@ -1352,7 +1619,7 @@ void tc_choose_padding(TcOffsets& o, bool tma_ok, int conflict_slack)
     // repeats from run to run of a plan: remember it.
     struct Choice {
         uint32_t pad;
-        uint32_t order[2][7];
+        uint32_t order[kTcMaxBlocks][7];
     };
     static std::mutex mu;
     static std::unordered_map<std::string, Choice> memo;
@@ -1386,7 +1653,7 @@ void tc_choose_padding(TcOffsets& o, bool tma_ok, int conflict_slack)
         for (uint32_t pad : cands) {
             if (pad < 31 && tma_ok && best >= 0 && best <= conflict_slack * ideal) break;   // keep the tensor-map copy
             long cost = 0;
-            uint32_t order[2][7] = {};
+            uint32_t order[kTcMaxBlocks][7] = {};
             for (uint32_t b = 0; b < o.nblocks; ++b) {
                 if (o.shuffle) {
                     std::memcpy(order[b], o.blk[b].jrow_bit, sizeof(order[b]));
@@ -1584,6 +1851,115 @@ TcTileBox tc_tile_box(const int* tile_pos, int nbits, uint64_t ncols)
     return b;
 }
 
+std::vector<TcStoreBox> tc_store_boxes(const int* tile_pos, int nbits, uint64_t ncols, uint32_t gates)
+{
+    std::vector<TcStoreBox> out;
+    {
+        TcStoreBox id{};
+        id.box = tc_tile_box(tile_pos, nbits, ncols);
+        if (!id.box.usable) return out;
+        for (int j = 0; j < 12; ++j) id.sbit[j] = j;
+        out.push_back(id);
+    }
+    // runs of consecutive tile positions, as tile-bit ranges
+    std::vector<std::pair<int, int>> runs;   // (first tile bit, length)
+    for (int j = 0; j < 12;) {
+        int k = j + 1;
+        while (k < 12 && tile_pos[k] == tile_pos[k - 1] + 1) ++k;
+        runs.push_back({j, k - j});
+        j = k;
+    }
+    // the gap dimensions (box 1) in position order, as tc_tile_box makes them
+    std::vector<char> in_tile(nbits, 0);
+    for (int j = 0; j < 12; ++j) in_tile[tile_pos[j]] = 1;
+    struct Dim {
+        uint64_t gdim, gstride;
+        uint32_t box, tshift, tmask;
+    };
+    std::vector<Dim> gaps;
+    {
+        uint32_t below = 0;
+        bool top_outside = false;
+        for (int p = 0; p < nbits;) {
+            int q = p;
+            while (q < nbits && in_tile[q] == in_tile[p]) ++q;
+            if (!in_tile[p]) {
+                gaps.push_back({uint64_t(1) << (q - p), uint64_t(8) << p, 1u, below,
+                                (uint32_t)((uint64_t(1) << (q - p)) - 1)});
+                below += (uint32_t)(q - p);
+            }
+            top_outside = !in_tile[p];
+            p = q;
+        }
+        if (ncols > 1) {
+            if (top_outside) {
+                gaps.back().gdim *= ncols;
+                gaps.back().tmask = 0xFFFFFFFFu;
+            } else {
+                gaps.push_back({ncols, uint64_t(8) << nbits, 1u, below, 0xFFFFFFFFu});
+            }
+        }
+    }
+    // dimension 0 is the stores' contiguous run in memory: at least 8
+    // amplitudes (64 bytes) or the whole first run, so that no store box
+    // writes shorter runs than the tile has
+    const int s_max = std::min(8, runs[0].second);
+    for (int s0 = std::min(3, runs[0].second); s0 <= s_max; ++s0) {
+        // the other tile bits cut into pieces of one role (row or gate of
+        // the last block), within a run, of at most 8 bits; rows first
+        std::vector<std::pair<int, int>> rowp, gatep;
+        for (size_t r = 0; r < runs.size(); ++r) {
+            int j = r == 0 ? s0 : runs[r].first;
+            const int end = runs[r].first + runs[r].second;
+            while (j < end) {
+                const bool g = (gates >> j) & 1u;
+                int k = j + 1;
+                while (k < end && (((gates >> k) & 1u) != 0) == g && k - j < 8) ++k;
+                (g ? gatep : rowp).push_back({j, k - j});
+                j = k;
+            }
+        }
+        std::vector<std::pair<int, int>> pieces = {{0, s0}};
+        pieces.insert(pieces.end(), rowp.begin(), rowp.end());
+        pieces.insert(pieces.end(), gatep.begin(), gatep.end());
+        if (pieces.size() + gaps.size() > 5) continue;
+        TcStoreBox c{};
+        int nd = 0, acc = 0;
+        for (auto& pc : pieces) {
+            c.box.gdim[nd] = c.box.box[nd] = 1u << pc.second;
+            c.box.gstride[nd] = uint64_t(8) << tile_pos[pc.first];
+            c.box.tshift[nd] = 0;
+            c.box.tmask[nd] = 0;
+            for (int e = 0; e < pc.second; ++e) c.sbit[pc.first + e] = acc + e;
+            acc += pc.second;
+            ++nd;
+        }
+        for (auto& g : gaps) {
+            c.box.gdim[nd] = g.gdim;
+            c.box.gstride[nd] = g.gstride;
+            c.box.box[nd] = g.box;
+            c.box.tshift[nd] = g.tshift;
+            c.box.tmask[nd] = g.tmask;
+            ++nd;
+        }
+        bool ok = true;
+        for (int d = 0; d < nd; ++d) ok = ok && c.box.gdim[d] <= (uint64_t(1) << 32);
+        if (!ok) continue;
+        for (int d = nd; d < 5; ++d) {
+            c.box.gdim[d] = 1;
+            c.box.gstride[d] = c.box.gstride[d - 1] * c.box.gdim[d - 1];
+            c.box.box[d] = 1;
+            c.box.tshift[d] = 0;
+            c.box.tmask[d] = 0;
+        }
+        c.box.usable = 1;
+        bool same = true;
+        for (int j = 0; j < 12; ++j) same = same && c.sbit[j] == j;
+        if (!same) out.push_back(c);
+    }
+    return out;
+}
+
 namespace {
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
@@ -1607,7 +1983,7 @@ EncodeTiledFn encode_tiled()
 
 cudaError_t launch_fused_tc(float2* amps, uint64_t ntiles, const IndexMap& tilemap, const TcOffsets& offs_in,
                             const TcTileBox& box, const void* d_bimage, int* d_err, int sm_count,
-                            cudaStream_t st, uint64_t wait_ns)
+                            cudaStream_t st, uint64_t wait_ns, const TcTileBox* store_box)
 {
     static std::mutex mu;
     static int optin[64] = {0};
@@ -1635,35 +2011,42 @@ cudaError_t launch_fused_tc(float2* amps, uint64_t ntiles, const IndexMap& tilem
     // four groups hold four stages: at least one more for the copies;
     // operands in shared memory need 1024-byte aligned stages
     const uint32_t min_stages = ng == 4 ? 5u : 3u;
-    if (offs.nblocks < 1 || offs.nblocks > 2 || offs.stage_bytes < kTileBytes ||
+    // three blocks only as a direct chain of the four-group kernel
+    if (offs.nblocks < 1 || offs.nblocks > (ng == 4 && offs.direct ? 3u : 2u) || offs.stage_bytes < kTileBytes ||
         ((ng == 4 || offs.direct) && offs.stage_bytes % 1024u) ||
         (uint32_t)optin[dev] < fixed + min_stages * offs.stage_bytes)
         return cudaErrorInvalidConfiguration;
     offs.nstages = std::min(kMaxStages, ((uint32_t)optin[dev] - fixed) / offs.stage_bytes);
     const uint32_t smem = fixed + offs.nstages * offs.stage_bytes;
     // unpadded tiles: one tensor-map box per tile
-    CUtensorMap tmap;
+    CUtensorMap tmap, tmap_st;
     std::memset(&tmap, 0, sizeof(tmap));
+    std::memset(&tmap_st, 0, sizeof(tmap_st));
     offs.use_tma = 0;
     EncodeTiledFn enc = encode_tiled();
-    if (offs.pad_shift >= 31 && box.usable && enc) {
+    auto encode = [&](CUtensorMap* m, const TcTileBox& b) {
         cuuint64_t gdim[5], gstride[4];
         cuuint32_t bdim[5], estride[5] = {1, 1, 1, 1, 1};
         for (int d = 0; d < 5; ++d) {
-            gdim[d] = box.gdim[d];
-            bdim[d] = box.box[d];
-            if (d > 0) gstride[d - 1] = box.gstride[d];
+            gdim[d] = b.gdim[d];
+            bdim[d] = b.box[d];
+            if (d > 0) gstride[d - 1] = b.gstride[d];
         }
-        if (enc(&tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 5, amps, gdim, gstride, bdim, estride,
-                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS) {
-            offs.use_tma = 1;
-            for (int d = 0; d < 5; ++d) {
-                offs.tshift[d] = box.tshift[d];
-                offs.tmask[d] = box.tmask[d];
-            }
+        return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 5, amps, gdim, gstride, bdim, estride,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+    };
+    if (offs.pad_shift >= 31 && box.usable && enc && encode(&tmap, box)) {
+        offs.use_tma = 1;
+        for (int d = 0; d < 5; ++d) {
+            offs.tshift[d] = box.tshift[d];
+            offs.tmask[d] = box.tmask[d];
         }
     }
+    // the last block's write-back follows the store box: without it (or
+    // its map) the pass cannot run
+    if (offs.st_box && (!offs.use_tma || !store_box || !store_box->usable || !encode(&tmap_st, *store_box)))
+        return cudaErrorInvalidConfiguration;
     // the piece path has a table of 32 runs: a tile of more runs must go as
     // one tensor-map box
     if (!offs.use_tma && (offs.nruns > 32 || offs.npieces > 4096u >> 5)) return cudaErrorInvalidConfiguration;
@@ -1671,10 +2054,10 @@ cudaError_t launch_fused_tc(float2* amps, uint64_t ntiles, const IndexMap& tilem
     if (grid > ntiles) grid = ntiles;
     if (grid == 0) return cudaSuccess;
     if (ng == 4)
-        k_fused_tc<4><<<(unsigned)grid, TcShape<4>::kThreads, smem, st>>>(amps, ntiles, tilemap, offs, tmap,
+        k_fused_tc<4><<<(unsigned)grid, TcShape<4>::kThreads, smem, st>>>(amps, ntiles, tilemap, offs, tmap, tmap_st,
                                                                           (const uint4*)d_bimage, d_err);
     else
-        k_fused_tc<2><<<(unsigned)grid, TcShape<2>::kThreads, smem, st>>>(amps, ntiles, tilemap, offs, tmap,
+        k_fused_tc<2><<<(unsigned)grid, TcShape<2>::kThreads, smem, st>>>(amps, ntiles, tilemap, offs, tmap, tmap_st,
                                                                           (const uint4*)d_bimage, d_err);
     return cudaGetLastError();
 }

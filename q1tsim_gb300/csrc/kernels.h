@@ -2,6 +2,8 @@
 #pragma once
 
 #include <cuda_runtime.h>
+
+#include <vector>
 #include <stdint.h>
 
 #include <complex>
@@ -89,6 +91,9 @@ cudaError_t launch_dense_tiled(void* amps, int prec, uint64_t total, int nbits, 
 // that are a multiple of 32 amplitudes apart onto different banks; it is
 // chosen per pass by tc_choose_padding.  Tiles are copied in npieces pieces
 // of 2^piece_bits amplitudes (contiguous in both memories).
+// Blocks one tensor-core pass may apply in turn (three only in the
+// four-group kernel's direct chain).
+constexpr int kTcMaxBlocks = 3;
 struct TcBlockGeom {
     uint32_t jrow_bit[7];    // tile coordinate of row bit r (any order: rows are independent)
     uint32_t vec2;           // 1 if gate bit 0 is tile bit 0 (gate pairs adjacent)
@@ -121,19 +126,19 @@ struct TcOffsets {
     // order after the swaps.
     uint32_t shuffle;
     int32_t swap_lane[5];
-    // Two-block passes whose second block reads its operands from shared
-    // memory (a plan's pair mode 3): the first block's write-back splits its
-    // results into hi/lo f16 pairs and stores them straight into the stage
-    // as the second block's A operand (K-major, SWIZZLE_128B, hi plane then
-    // lo plane), at byte (XOR over the thread's row bits i of scat_row[i])
-    // XOR scat_gate[g] for its output gate state g.  The second block's
-    // row and gate orders are the ones that layout implies.
+    // Passes whose later blocks read their operands from shared memory (a
+    // plan's pair modes 3 and 4): block b's write-back splits its results
+    // into hi/lo f16 pairs and stores them straight into the stage as block
+    // b+1's A operand (K-major, SWIZZLE_128B, hi plane then lo plane), at
+    // byte (XOR over the thread's row bits i of scat_row[b][i]) XOR
+    // scat_gate[b][g] for its output gate state g.  Block b+1's row and gate
+    // orders are the ones that layout implies.
     uint32_t direct;
     uint64_t wait_ns;        // longest any wait may last (set by launch_fused_tc)
     uint64_t run_off[32];
-    TcBlockGeom blk[2];
-    uint32_t scat_row[7];
-    uint32_t scat_gate[32];
+    TcBlockGeom blk[kTcMaxBlocks];
+    uint32_t scat_row[kTcMaxBlocks - 1][7];
+    uint32_t scat_gate[kTcMaxBlocks - 1][32];
     // consumer groups of the kernel: 2 (0 means 2), or 4 with every A
     // operand in shared memory (plan pair mode 4; stage_bytes a multiple of
     // 1024)
@@ -146,6 +151,12 @@ struct TcOffsets {
     // and stores chunk q of each plane at (XOR over t's bits of sp_athr[i])
     // XOR sp_achunk[q].  sp_vec2: registers 2m, 2m+1 are adjacent in the
     // stage (16-byte loads).
+    // 1: the storers copy the tile with a second tensor map (TcStoreBox), the
+    // last block's staged offsets following its layout; coordinates as
+    // tshift / tmask
+    uint32_t st_box;
+    uint32_t st_tshift[5];
+    uint32_t st_tmask[5];
     uint32_t sp_vec2;
     uint32_t sp_thoff[7];
     uint32_t sp_athr[7];
@@ -165,6 +176,19 @@ struct TcTileBox {
     uint32_t tmask[5];
 };
 TcTileBox tc_tile_box(const int* tile_pos /* 12, ascending */, int nbits, uint64_t ncols);
+// A second box of the same tile for the stores: the tile's positions cut into
+// dimensions of at most 8 positions in another order (dimension 0, which
+// starts at position 0, first), so that in shared memory the tile bits lie
+// in another order: tile bit j at element bit sbit[j].  Only the last
+// block's write-back writes this layout, and only the storers read it.
+struct TcStoreBox {
+    TcTileBox box;
+    int sbit[12];
+};
+// Store boxes for a tile whose last block has gate bits `gates` (tile bits):
+// the identity order first, then orders that put that block's row bits in
+// the low shared-memory bits (usable boxes only).
+std::vector<TcStoreBox> tc_store_boxes(const int* tile_pos, int nbits, uint64_t ncols, uint32_t gates);
 // Picks pad_shift (and piece_bits, npieces, stage_bytes, the blocks' staged
 // offsets) that minimise shared-memory bank conflicts of the per-row reads.
 // With tma_ok (the tile is one tensor-map box) an unpadded tile is kept when
@@ -187,6 +211,21 @@ bool tc_shuffle_layout(TcBlockGeom& b0, TcBlockGeom& b1, int32_t* swap_lane, int
 // offs.direct, the scatter tables, block 1's jgate/vec2 and every staged
 // offset.  Returns false when the blocks do not have 5 gate bits each.
 bool tc_direct_layout(TcOffsets& offs, bool tma_ok, int conflict_slack, int* gbit1);
+// Layout of a direct pass of the four-group kernel (2 or 3 blocks; the first
+// block's split is dealt by tc_split_map, so its reads do not constrain its
+// row order): picks the padding as tc_direct_layout does, block 0's row
+// order and, for each later block, its gate order (gbits[b][k] = tile bit of
+// its gate bit k) and row order, with the fewest predicted bank wavefronts
+// over the scatters from block to block and the last block's write-back;
+// sets offs.direct, the scatter tables, the later blocks' jgate/vec2 and
+// every staged offset; *cost / *ideal: the chosen layout's predicted
+// wavefronts per warp and their minimum.  With `stores` (an unpadded tile
+// that is one box), the last block's write-back is evaluated in each store
+// box and *store is the chosen one's index (its staged offsets are set from
+// that box's sbit; -1: the load layout).  False when a block does not have
+// 5 gate bits.
+bool tc_chain_layout(TcOffsets& offs, bool tma_ok, int conflict_slack, int (*gbits)[5], long* cost = nullptr,
+                     long* ideal = nullptr, const std::vector<TcStoreBox>* stores = nullptr, int* store = nullptr);
 // Deal of the first block's tile to the threads of a four-group pass
 // (TcOffsets::sp_*), after its layout (padding, row orders, scatter tables)
 // is chosen: picks the block's gate bits 0-1 and the tile bits that vary
@@ -205,11 +244,12 @@ inline uint32_t tc_sw128_offset(uint32_t r, uint32_t k)
 // 64x64 embeddings in the kernel's swizzled layout; d_err: set to 1 if a
 // bounded wait expired.  wait_ns: longest any of the kernel's waits may
 // last before it gives up (0: the default, 60 s).
-// box: the tile as a tensor-map box (used for unpadded passes when usable).
+// box: the tile as a tensor-map box (used for unpadded passes when usable);
+// store_box: the storers' box when offs.st_box.
 constexpr uint64_t kTcDefaultWaitNs = 60000000000ull;
 cudaError_t launch_fused_tc(float2* amps, uint64_t ntiles, const IndexMap& tilemap, const TcOffsets& offs,
                             const TcTileBox& box, const void* d_bimage, int* d_err, int sm_count,
-                            cudaStream_t st, uint64_t wait_ns = 0);
+                            cudaStream_t st, uint64_t wait_ns = 0, const TcTileBox* store_box = nullptr);
 // Host: the 16 KB image (8192 f16) for the 32x32 complex matrix m
 // (row-major (re, im)), entries times 2^scale_log2: kTcLastBScaleLog2 for
 // the last block of a pass, 0 for the one before (whose output stays scaled).

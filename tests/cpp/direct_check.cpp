@@ -78,6 +78,41 @@ static int check_split(const TcOffsets& o)
     return bad;
 }
 
+// Transition k of a direct pass: block k's output (thread t, gate g) lands
+// on a distinct word of block k+1's operand plane, where that operand holds
+// (row, K = 2 gate) of block k+1 for the same tile coordinate.
+static int check_scatter(const TcOffsets& o, int k)
+{
+    int bad = 0;
+    std::vector<int> seen(4096, 0);
+    const TcBlockGeom& A = o.blk[k];
+    const TcBlockGeom& B = o.blk[k + 1];
+    for (uint32_t t = 0; t < 128; ++t) {
+        uint32_t rowpart = 0, xrow = 0;
+        for (int i = 0; i < 7; ++i)
+            if ((t >> i) & 1u) {
+                rowpart ^= o.scat_row[k][i];
+                xrow |= A.jrow_bit[i];
+            }
+        for (int g = 0; g < 32; ++g) {
+            const uint32_t a = rowpart ^ o.scat_gate[k][g];
+            if (a >= 16384u || (a & 3u)) {
+                ++bad;
+                continue;
+            }
+            if (seen[a >> 2]++) ++bad;
+            const uint32_t x = xrow | A.jgate[g];
+            uint32_t r2 = 0, g2 = 0;
+            for (int i = 0; i < 7; ++i)
+                if (x & B.jrow_bit[i]) r2 |= 1u << i;
+            for (int q = 0; q < 5; ++q)
+                if (x & B.jgate[1 << q]) g2 |= 1u << q;
+            if (a != tc_sw128_offset(r2, 2u * g2)) ++bad;
+        }
+    }
+    return bad;
+}
+
 int main()
 {
     std::mt19937 rng(7);
@@ -160,11 +195,11 @@ int main()
             uint32_t rowpart = 0, xrow = 0;
             for (int i = 0; i < 7; ++i)
                 if ((t >> i) & 1u) {
-                    rowpart ^= o.scat_row[i];
+                    rowpart ^= o.scat_row[0][i];
                     xrow |= o.blk[0].jrow_bit[i];
                 }
             for (int g = 0; g < 32; ++g) {
-                const uint32_t a = rowpart ^ o.scat_gate[g];
+                const uint32_t a = rowpart ^ o.scat_gate[0][g];
                 if (a >= 16384u || (a & 3u)) {
                     ++bad;
                     continue;
@@ -188,7 +223,7 @@ int main()
             for (uint32_t l = 0; l < 32; ++l) {
                 uint32_t a = 0;
                 for (int i = 0; i < 5; ++i)
-                    if ((l >> i) & 1u) a ^= o.scat_row[i];
+                    if ((l >> i) & 1u) a ^= o.scat_row[0][i];
                 m = std::max(m, ++per_bank[(a >> 2) & 31u]);
             }
             at_min = m == 1;
@@ -215,7 +250,178 @@ int main()
         if (o.blk[0].jgate[31] != gate0) ++bad;
         ++singles;
     }
-    std::printf("bad %d trials %d conflict-free scatter %d padded %d singles %d\n", bad, trials, minimal, padded,
-                singles);
+    // chained layouts of the four-group kernel: pairs and triples
+    int chains = 0, chain_free = 0;
+    for (int trial = 0; trial < 900; ++trial) {
+        const int nb = 2 + trial % 2;
+        std::vector<std::vector<int>> gs(nb);
+        if (trial % 3 != 2) {
+            // brick-like windows of five, each shifted from the previous
+            int lo = (int)(rng() % 4);
+            for (int b = 0; b < nb; ++b) {
+                for (int k = 0; k < 5; ++k) gs[b].push_back(std::min(11, lo + k) - (lo + 4 > 11 ? lo + 4 - 11 : 0));
+                lo = std::max(0, std::min(7, lo + 1 + (int)(rng() % 3)));
+            }
+        } else {
+            for (int b = 0; b < nb; ++b) {
+                std::vector<int> all(12);
+                for (int j = 0; j < 12; ++j) all[j] = j;
+                std::shuffle(all.begin(), all.end(), rng);
+                gs[b].assign(all.begin(), all.begin() + 5);
+            }
+        }
+        TcOffsets o{};
+        o.nblocks = (uint32_t)nb;
+        o.run_bits = (uint32_t)(rng() % 13);
+        o.nruns = 1u << (12 - o.run_bits);
+        for (int b = 0; b < nb; ++b) {
+            std::shuffle(gs[b].begin(), gs[b].end(), rng);
+            default_geom(o.blk[b], gs[b]);
+        }
+        uint32_t gates[3];
+        for (int b = 0; b < nb; ++b) gates[b] = o.blk[b].jgate[31];
+        int gbits[kTcMaxBlocks][5];
+        if (!tc_chain_layout(o, (rng() % 3) != 0, 4, gbits)) {
+            ++bad;
+            continue;
+        }
+        int gbit0[5];
+        tc_split_map(o, gbit0);
+        ++chains;
+        if (o.direct != 1 || o.stage_bytes % 1024u) ++bad;
+        for (int b = 0; b < nb; ++b) {
+            if (o.blk[b].jgate[31] != gates[b]) ++bad;
+            uint32_t rows = 0;
+            for (int r = 0; r < 7; ++r) rows |= o.blk[b].jrow_bit[r];
+            if (rows != (0xFFFu & ~gates[b])) ++bad;
+            if (b > 0)
+                for (int k = 0; k < 5; ++k)
+                    if (o.blk[b].jgate[1 << k] != (1u << gbits[b][k])) ++bad;
+            for (int r = 0; r < 7; ++r)
+                if (o.blk[b].rowoff[r] != staged(o.blk[b].jrow_bit[r], o.pad_shift)) ++bad;
+            for (int g = 0; g < 32; ++g)
+                if (o.blk[b].gateoff[g] != staged(o.blk[b].jgate[g], o.pad_shift)) ++bad;
+        }
+        bad += check_split(o);
+        bool free = true;
+        for (int k = 0; k + 1 < nb; ++k) {
+            bad += check_scatter(o, k);
+            int per_bank[32] = {0}, m = 0;
+            for (uint32_t l = 0; l < 32; ++l) {
+                uint32_t a = 0;
+                for (int i = 0; i < 5; ++i)
+                    if ((l >> i) & 1u) a ^= o.scat_row[k][i];
+                m = std::max(m, ++per_bank[(a >> 2) & 31u]);
+            }
+            free = free && m == 1;
+        }
+        chain_free += free;
+    }
+    // store boxes: every element of the box, in the box's own order, is the
+    // amplitude its tile coordinate denotes, and shared-memory element
+    // index = sum of 2^sbit over the coordinate's bits; a chain layout with
+    // store boxes puts the last block's offsets in the chosen box's layout
+    int boxes = 0, stored = 0;
+    for (int trial = 0; trial < 600; ++trial) {
+        const int nbits = 12 + (int)(rng() % 18);
+        std::vector<int> T;
+        const int nb = 2 + trial % 2;
+        std::vector<std::vector<int>> gs(nb);
+        int lo = (int)(rng() % (nbits - 11));
+        for (int b = 0; b < nb; ++b) {
+            for (int k = 0; k < 5; ++k) gs[b].push_back(lo + k);
+            lo = std::min(nbits - 5, lo + 1 + (int)(rng() % 3));
+        }
+        for (auto& gb : gs)
+            for (int p : gb)
+                if (std::find(T.begin(), T.end(), p) == T.end()) T.push_back(p);
+        if (T.size() > 12) continue;
+        for (int p = 0; (int)T.size() < 12; ++p)
+            if (std::find(T.begin(), T.end(), p) == T.end()) T.push_back(p);
+        std::sort(T.begin(), T.end());
+        auto tb = [&](int p) { return (int)(std::find(T.begin(), T.end(), p) - T.begin()); };
+        uint32_t lastg = 0;
+        for (int p : gs[nb - 1]) lastg |= 1u << tb(p);
+        const uint64_t ncols = 1;
+        const auto cands = tc_store_boxes(T.data(), nbits, ncols, lastg);
+        IndexMap tm{};
+        tm.nz = 12;
+        for (int j = 0; j < 12; ++j) tm.zpos[j] = T[j];
+        const uint64_t ntiles = (ncols << nbits) >> 12;
+        for (const auto& c : cands) {
+            ++boxes;
+            std::vector<int> seen(12, 0);
+            for (int j = 0; j < 12; ++j)
+                if (c.sbit[j] < 0 || c.sbit[j] > 11 || seen[c.sbit[j]]++) ++bad;
+            uint64_t elems = 1;
+            for (int d = 0; d < 5; ++d) elems *= c.box.box[d];
+            if (elems != 4096 || c.box.tmask[0] != 0 || c.box.gstride[0] != 8) ++bad;
+            for (int k = 0; k < 3; ++k) {
+                const uint64_t t = k == 0 ? 0 : (k == 1 ? ntiles - 1 : rng() % ntiles);
+                const uint64_t base = expand_index(t, tm);
+                uint64_t e = 0;
+                for (uint64_t e4 = 0; e4 < c.box.box[4]; ++e4)
+                    for (uint64_t e3 = 0; e3 < c.box.box[3]; ++e3)
+                        for (uint64_t e2 = 0; e2 < c.box.box[2]; ++e2)
+                            for (uint64_t e1 = 0; e1 < c.box.box[1]; ++e1)
+                                for (uint64_t e0 = 0; e0 < c.box.box[0]; ++e0, ++e) {
+                                    const uint64_t co[5] = {e0, e1, e2, e3, e4};
+                                    uint64_t off = 0;
+                                    for (int d = 0; d < 5; ++d) {
+                                        const uint64_t cd = ((uint32_t)(t >> c.box.tshift[d]) & c.box.tmask[d]) + co[d];
+                                        off += cd * (d ? c.box.gstride[d] / 8 : 1);
+                                    }
+                                    // tile coordinate of shared-memory element e
+                                    uint32_t x = 0;
+                                    for (int j = 0; j < 12; ++j)
+                                        if ((e >> c.sbit[j]) & 1u) x |= 1u << j;
+                                    uint64_t want = base;
+                                    for (int j = 0; j < 12; ++j)
+                                        if ((x >> j) & 1u) want |= uint64_t(1) << T[j];
+                                    if (off != want) ++bad;
+                                }
+            }
+        }
+        // a chain layout over these blocks with the store boxes
+        TcOffsets o{};
+        o.nblocks = (uint32_t)nb;
+        int L = 0;
+        while (L < 12 && T[L] == L) ++L;
+        o.run_bits = (uint32_t)L;
+        o.nruns = 1u << (12 - L);
+        for (int b = 0; b < nb; ++b) {
+            std::vector<int> gbits;
+            for (int p : gs[b]) gbits.push_back(tb(p));
+            default_geom(o.blk[b], gbits);
+        }
+        int gbs[kTcMaxBlocks][5], si = -1;
+        long cost = 0, ideal = 0;
+        if (!tc_chain_layout(o, true, 4, gbs, &cost, &ideal, &cands, &si)) {
+            ++bad;
+            continue;
+        }
+        if (si >= 0 && o.pad_shift >= 31) {
+            ++stored;
+            const auto& c = cands[(size_t)si];
+            const TcBlockGeom& Lb = o.blk[nb - 1];
+            for (uint32_t t = 0; t < 128; ++t)
+                for (int g = 0; g < 32; ++g) {
+                    uint32_t x = Lb.jgate[g], off = Lb.gateoff[g];
+                    for (int i = 0; i < 7; ++i)
+                        if ((t >> i) & 1u) {
+                            x |= Lb.jrow_bit[i];
+                            off += Lb.rowoff[i];
+                        }
+                    uint32_t e = 0;
+                    for (int j = 0; j < 12; ++j)
+                        if ((x >> j) & 1u) e |= 1u << c.sbit[j];
+                    if (off != 8u * e) ++bad;
+                }
+            if ((si > 0) != (o.st_box != 0)) ++bad;
+        }
+    }
+    std::printf("bad %d trials %d conflict-free scatter %d padded %d singles %d chains %d conflict-free chains %d "
+                "store boxes %d chains with a store box %d\n",
+                bad, trials, minimal, padded, singles, chains, chain_free, boxes, stored);
     return bad ? 1 : 0;
 }

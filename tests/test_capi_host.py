@@ -48,7 +48,7 @@ def test_null_arguments_are_errors_not_crashes(lib):
     p = Plan(3, [[0]], fusion_width=2)
     p.set_tc_tiling(0, 8, 4)
     assert p.tc_tiling == (0, 8, 4)
-    for bad in ((2, 13, 2), (2, 5, 0), (2, -1, 2), (5, 5, 2), (-1, 5, 2)):
+    for bad in ((2, 13, 2), (2, 5, 0), (2, -1, 2), (6, 5, 2), (-1, 5, 2)):
         with pytest.raises(_lib.InvalidArgument):
             p.set_tc_tiling(*bad)
 

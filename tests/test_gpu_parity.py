@@ -683,23 +683,27 @@ def test_tensor_core_block_exact_any_layout(n, qubits, pairs):
     assert np.array_equal(out, ref), float(np.max(np.abs(out - ref)))
 
 
-def test_two_blocks_share_one_tensor_core_pass():
+@pytest.mark.parametrize("pairs,launches", [(1, 2), (4, 2), (5, 1)])
+def test_two_blocks_share_one_tensor_core_pass(pairs, launches):
     """Consecutive blocks whose qubits fit one 12-position tile run in one
-    pass over the state; results stay exact."""
+    pass over the state: two per pass, up to three in the four-group
+    kernel's direct chain in pair mode 5; results stay exact."""
     n = 14
     amps = split_exact_amps(n)
     seq = [([0, 1, 2], cyclic_perm(3, 1)), ([11, 12, 13], cyclic_perm(3, 5)), ([5, 6, 7], cyclic_perm(3, 2))]
     mats = np.concatenate([m.ravel() for _, m in seq]).view(np.float64)
     g = VectorState.from_amplitudes(amps, 1, "c64")
     g.profile(True)
-    g.apply_plan(Plan(n, [b for b, _ in seq], 3), mats)
+    plan = Plan(n, [b for b, _ in seq], 3)
+    plan.set_tc_tiling(pairs, 8, 4)
+    g.apply_plan(plan, mats)
     o = orc.OracleState.from_amplitudes(amps, 1)
     for b, m in seq:
         o.apply_gate(m, b)
     out, ref = g.states()[:, 0], o.states()[:, 0]
     assert np.array_equal(out, ref), float(np.max(np.abs(out - ref)))
     rep = g.profile_report()
-    assert rep["fused_tc_c64"]["launches"] == 2, rep
+    assert rep["fused_tc_c64"]["launches"] == launches, rep
 
 
 @pytest.mark.parametrize("n,first,second", [
@@ -743,6 +747,33 @@ def test_direct_pair_is_exact(n, first, second, mode):
     mats = np.concatenate([m.ravel() for _, m in seq]).view(np.float64)
     plan = Plan(n, [b for b, _ in seq], 5)
     plan.set_tc_tiling(mode, 12, 2)
+    g = VectorState.from_amplitudes(amps, 1, "c64")
+    g.profile(True)
+    g.apply_plan(plan, mats)
+    o = orc.OracleState.from_amplitudes(amps, 1)
+    for b, m in seq:
+        o.apply_gate(m, b)
+    out, ref = g.states()[:, 0], o.states()[:, 0]
+    assert np.array_equal(out, ref), float(np.max(np.abs(out - ref)))
+    assert g.profile_report()["fused_tc_c64"]["launches"] == 1
+
+
+@pytest.mark.parametrize("n,blocks", [
+    (16, [[9, 10, 11, 12, 13], [7, 8, 9, 10, 11], [5, 6, 7, 8, 9]]),      # brick windows, one run
+    (20, [[3, 4, 5, 6, 7], [1, 2, 3, 4, 5], [0, 1, 2, 3, 4]]),           # high positions
+    (22, [[0, 1, 2, 3, 4], [2, 3, 4, 5, 6], [4, 5, 6, 7, 8]]),            # top positions, runs of 8
+    (20, [[0, 4, 8, 2, 6], [1, 3, 5, 7, 8], [2, 4, 6, 7, 5]]),           # scattered gate bits, one box
+])
+def test_direct_triple_is_exact(n, blocks):
+    """Three blocks in one pass of the four-group kernel (pair mode 5):
+    block b's write-back stores block b+1's operands in the stage.  On permutation
+    blocks and amplitudes that split exactly, the state equals the oracle's
+    bit for bit, in one launch."""
+    amps = split_exact_amps(n)
+    seq = [(b, cyclic_perm(5, 3 + 4 * k)) for k, b in enumerate(blocks)]
+    mats = np.concatenate([m.ravel() for _, m in seq]).view(np.float64)
+    plan = Plan(n, [b for b, _ in seq], 5)
+    plan.set_tc_tiling(5, 12, 4)
     g = VectorState.from_amplitudes(amps, 1, "c64")
     g.profile(True)
     g.apply_plan(plan, mats)
@@ -1061,7 +1092,8 @@ def test_autotuned_circuit_matches_oracle():
 
 
 @pytest.mark.parametrize("tiling", [(2, 5, 2), (1, 5, 2), (0, 5, 2), (2, 8, 2), (2, 5, 4), (2, 12, 64), (1, 12, 64),
-                                    (3, 5, 2), (3, 8, 2), (3, 12, 64), (4, 8, 2), (4, 8, 4), (4, 12, 64)])
+                                    (3, 5, 2), (3, 8, 2), (3, 12, 64), (4, 8, 2), (4, 8, 4), (4, 12, 64),
+                                    (5, 8, 4), (5, 12, 64)])
 def test_tc_tilings_match_oracle(tiling):
     """Every tensor-core tiling (pairs through registers, through the staged
     tile, as operands the first block stores for the second, or none; pairs
