@@ -971,14 +971,6 @@ void order_blocks_for_tc_pairs(std::vector<FusedBlock>& blocks, int nbits, int m
     blocks.swap(out);
 }
 
-static size_t union_size(const std::vector<int>& a, const std::vector<int>& b)
-{
-    std::vector<int> u = a;
-    for (int x : b)
-        if (std::find(u.begin(), u.end(), x) == u.end()) u.push_back(x);
-    return u.size();
-}
-
 // A swap-run block (fuse_runs): every gate must be the swap permutation;
 // one permutation pass (swap_run.cu), or the swaps one by one when the
 // state has fewer than 10 qubits.
