@@ -227,6 +227,16 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t* v)
         : "r"(taddr));
 }
 
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t* v)
+{
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+        : "r"(taddr));
+}
+
 __device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t* v)
 {
     asm volatile(
@@ -459,6 +469,80 @@ __device__ __forceinline__ void writeback_row(uint8_t* raw, uint32_t rowb, const
 #pragma unroll
             for (int j = 0; j < 16; ++j)
                 *(float2*)(raw + rowb + G.gateoff[16 * hh + j]) =
+                    make_float2(__uint_as_float(dm[2 * j]), __uint_as_float(dm[2 * j + 1]));
+        }
+    }
+}
+
+// The last block's write-back with lane-permuted stores (TcOffsets::wb_xor):
+// at step j of half hh the thread stores its output gate state j ^ wx,
+// moved into place by register butterflies, at staged byte rowx ^
+// gateoff[16 hh + j], rowx = row offset ^ gateoff[wx].  The layout is
+// linear (unpadded), so that is the state's own offset.  wx < 16; bit 0
+// clear where 16-byte stores keep gate pairs together.  Every butterfly
+// runs, selecting by the lane's bit: branches around the unused ones
+// measured slower.
+__device__ __forceinline__ void writeback_row_xor(uint8_t* raw, uint32_t rowx, const TcBlockGeom& G, uint32_t td,
+                                                  float unscale, uint32_t wx)
+{
+#pragma unroll
+    for (int hh = 0; hh < 2; ++hh) {
+        // D_corr in two loads of 16 columns: fewer registers live at once
+        uint32_t dm[32], dc[16];
+        tmem_ld32(td + 32u * hh, dm);
+        tmem_ld16(td + 64u + 32u * hh, dc);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+            dm[j] = __float_as_uint(__fmaf_rn(__uint_as_float(dc[j]), kLoUnscale, __uint_as_float(dm[j])) * unscale);
+        tmem_ld16(td + 80u + 32u * hh, dc);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+            dm[16 + j] =
+                __float_as_uint(__fmaf_rn(__uint_as_float(dc[j]), kLoUnscale, __uint_as_float(dm[16 + j])) * unscale);
+        if (G.vec2) {
+            // 8 chunks of two gate states (4 words); chunk m <- chunk m ^ (wx >> 1)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const bool p = (wx >> (k + 1)) & 1u;
+#pragma unroll
+                for (int m = 0; m < 8; ++m) {
+                    if (m & (1 << k)) continue;
+                    const int m1 = m | (1 << k);
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        const uint32_t v0 = dm[4 * m + e], v1 = dm[4 * m1 + e];
+                        dm[4 * m + e] = p ? v1 : v0;
+                        dm[4 * m1 + e] = p ? v0 : v1;
+                    }
+                }
+            }
+#pragma unroll
+            for (int m = 0; m < 8; ++m)
+                *(float4*)(raw + (rowx ^ G.gateoff[16 * hh + 2 * m])) =
+                    make_float4(__uint_as_float(dm[4 * m]), __uint_as_float(dm[4 * m + 1]),
+                                __uint_as_float(dm[4 * m + 2]), __uint_as_float(dm[4 * m + 3]));
+        } else {
+            // 16 gate states (2 words); state j <- state j ^ wx
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const bool p = (wx >> k) & 1u;
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    if (j & (1 << k)) continue;
+                    const int j1 = j | (1 << k);
+#pragma unroll
+                    for (int e = 0; e < 2; ++e) {
+                        const uint32_t v0 = dm[2 * j + e], v1 = dm[2 * j1 + e];
+                        dm[2 * j + e] = p ? v1 : v0;
+                        dm[2 * j1 + e] = p ? v0 : v1;
+                    }
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < 16; ++j)
+                *(float2*)(raw + (rowx ^ G.gateoff[16 * hh + j])) =
                     make_float2(__uint_as_float(dm[2 * j]), __uint_as_float(dm[2 * j + 1]));
         }
     }
@@ -894,7 +978,20 @@ k_fused_tc(float2* __restrict__ a, uint64_t ntiles, const __grid_constant__ Inde
                 ++mph;
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 if ((uint32_t)b + 1 == nblocks) {
-                    writeback_row<true>(raw, rowb, G, td, offs.unscale);
+                    if ((offs.wb_xor[0] | offs.wb_xor[1] | offs.wb_xor[2] | offs.wb_xor[3] | offs.wb_xor[4]) != 0) {
+                        // the store permutation of this lane
+                        uint32_t wx = 0;
+#pragma unroll
+                        for (int r = 0; r < 5; ++r)
+                            if ((lane >> r) & 1) wx ^= offs.wb_xor[r];
+                        uint32_t rowx = rowb;
+#pragma unroll
+                        for (int k = 0; k < 4; ++k)
+                            if ((wx >> k) & 1u) rowx ^= G.gateoff[1 << k];
+                        writeback_row_xor(raw, rowx, G, td, offs.unscale, wx);
+                    } else {
+                        writeback_row<true>(raw, rowb, G, td, offs.unscale);
+                    }
                 } else if (shuf) {
                     writeback_regs(td, x);
                     swap_reg_lane_bits(x, offs.swap_lane, (uint32_t)lane);
@@ -982,6 +1079,95 @@ int warp_wavefronts_map(const uint32_t* order, const int* sbit, int width)
         total += m;
     }
     return total;
+}
+
+// Wavefronts of one phase of lane addresses a(l) = XOR over the lane's bits
+// r < nbits of vec[r] (byte offsets), `width` bytes per lane.
+static int phase_wavefronts(const uint32_t* vec, int nbits, int width)
+{
+    const uint32_t wpl = (uint32_t)width / 4;
+    uint32_t words[64];
+    uint32_t nw = 0;
+    for (uint32_t l = 0; l < (1u << nbits); ++l) {
+        uint32_t x = 0;
+        for (int r = 0; r < nbits; ++r)
+            if ((l >> r) & 1u) x ^= vec[r];
+        for (uint32_t w = 0; w < wpl; ++w) words[nw++] = x / 4 + w;
+    }
+    std::sort(words, words + nw);
+    int per_bank[32] = {0};
+    int m = 0;
+    for (uint32_t i = 0; i < nw; ++i)
+        if (i == 0 || words[i] != words[i - 1]) m = std::max(m, ++per_bank[words[i] % 32]);
+    return m;
+}
+
+// warp_wavefronts of the last block's write-back in a linear layout (tile
+// bit j at element bit sbit[j], or at j when sbit is null) when the stores
+// may be permuted per lane (TcOffsets::wb_xor): lane bit r XORs the stored
+// gate state by phi[r].  Lane l then stores at its row's offset XOR the
+// gate offset of phi(l) (plus the step's, common to all lanes), so each
+// phase lane bit r may add any gate offset of gate bits 1-3 (16-byte
+// stores) or 0-3 to its row offset.  Lane bits are taken in order, each
+// given the first permutation that raises the rank of the phase's bank
+// slots (address bits 4-6 for 16-byte, 3-6 for 8-byte stores), none if
+// its row offset does already; the result is kept when it beats no
+// permutation.  gk[i]: tile bit of gate bit i; phi out (zero: none);
+// plain_out: the wavefronts without a permutation.
+// The lane-permuted write-back's register butterflies (4, or 3 with 16-byte
+// stores; all run once any lane permutes), each in wavefront units of one
+// warp: 64 selects a row, measured at about 12 shared-memory wavefronts'
+// worth of pass time (30-qubit brick passes: the four butterflies cost
+// 13 % of a conflict-free pass, a 4x conflicted 16-byte write-back 48 %).
+constexpr long kWbButterflyCost = 12;
+
+int warp_wavefronts_xor(const uint32_t* order, const int* sbit, const int* gk, int width, uint32_t* phi,
+                        int* plain_out)
+{
+    auto off = [&](int j) { return 8u << (sbit ? sbit[j] : j); };
+    const int nl = width == 16 ? 3 : 4;                 // lane bits of a phase
+    const uint32_t lo = width == 16 ? 4u : 3u, slots = width == 16 ? 7u : 15u;
+    const uint32_t gmin = width == 16 ? 1u : 0u;        // lowest gate bit permuted
+    uint32_t row[5], best[5] = {0, 0, 0, 0, 0};
+    for (int r = 0; r < 5; ++r) row[r] = off(__builtin_ctz(order[r]));
+    auto gate_off = [&](uint32_t ph) {
+        uint32_t a = 0;
+        for (int i = 0; i < 4; ++i)
+            if ((ph >> i) & 1u) a ^= off(gk[i]);
+        return a;
+    };
+    const int plain = (32 / (1 << nl)) * phase_wavefronts(row, nl, width);
+    // greedy rank: basis of the chosen slot vectors, by leading bit
+    uint32_t basis[4] = {0, 0, 0, 0};
+    auto reduce = [&](uint32_t v) {
+        for (int b = 3; b >= 0; --b)
+            if (((v >> b) & 1u) && basis[b]) v ^= basis[b];
+        return v;
+    };
+    auto insert = [&](uint32_t v) {
+        v = reduce(v);
+        if (!v) return false;
+        basis[31 - __builtin_clz(v)] = v;
+        return true;
+    };
+    uint32_t vec[5];
+    for (int r = 0; r < nl; ++r) {
+        uint32_t pick = 0;
+        for (uint32_t ph = 0; ph < 16; ++ph) {
+            if (ph & ((1u << gmin) - 1u)) continue;
+            if (reduce(((row[r] ^ gate_off(ph)) >> lo) & slots)) {
+                pick = ph;
+                break;
+            }
+        }
+        best[r] = pick;
+        vec[r] = row[r] ^ gate_off(pick);
+        insert((vec[r] >> lo) & slots);
+    }
+    const int permuted = (32 / (1 << nl)) * phase_wavefronts(vec, nl, width);
+    for (int r = 0; r < 5; ++r) phi[r] = permuted < plain ? best[r] : 0u;
+    if (plain_out) *plain_out = plain;
+    return std::min(plain, permuted);
 }
 
 // The order of a block's 7 row bits (which tile coordinates the low lane
@@ -1407,6 +1593,7 @@ bool tc_chain_layout(TcOffsets& o, bool tma_ok, int conflict_slack, int (*gbits)
         uint32_t order[kTcMaxBlocks][7] = {};
         int g[kTcMaxBlocks][5] = {};
         int store = -1;
+        uint32_t wxor[5] = {};
     } best;
     static std::mutex mu;
     static std::unordered_map<std::string, Best> memo;
@@ -1496,16 +1683,30 @@ bool tc_chain_layout(TcOffsets& o, bool tma_ok, int conflict_slack, int (*gbits)
                     fill(lb, slot4_free ? lb[c4] : -1);
                     // the write-back in the load layout, or (unpadded) in
                     // the best store box
+                    // (lane-permuted stores where the layout is linear)
                     long wb = -1;
                     int si = -1;
+                    uint32_t wx[5] = {0, 0, 0, 0, 0};
+                    auto permuted = [&](const int* sbit, uint32_t* ph) {
+                        int plain = 0;
+                        const long w = nwb * (long)warp_wavefronts_xor(order[k + 1], sbit, gk, width, ph, &plain) +
+                                       kWbButterflyCost * (width == 16 ? 3 : 4);
+                        if (w < nwb * (long)plain) return w;
+                        for (int r = 0; r < 5; ++r) ph[r] = 0;
+                        return nwb * (long)plain;
+                    };
                     if (stores && pad >= 31) {
                         for (size_t c = 0; c < stores->size(); ++c) {
-                            const long w = nwb * (long)warp_wavefronts_map(order[k + 1], (*stores)[c].sbit, width);
+                            uint32_t ph[5];
+                            const long w = permuted((*stores)[c].sbit, ph);
                             if (wb < 0 || w < wb) {
                                 wb = w;
                                 si = (int)c;
+                                std::memcpy(wx, ph, sizeof(wx));
                             }
                         }
+                    } else if (pad >= 31) {
+                        wb = permuted(nullptr, wx);
                     } else {
                         wb = nwb * (long)warp_wavefronts(order[k + 1], pad, width);
                     }
@@ -1516,6 +1717,7 @@ bool tc_chain_layout(TcOffsets& o, bool tma_ok, int conflict_slack, int (*gbits)
                         std::memcpy(best.order, order, sizeof(order));
                         std::memcpy(best.g, g, sizeof(g));
                         best.store = si;
+                        std::memcpy(best.wxor, wx, sizeof(wx));
                     }
                 }
             }
@@ -1589,6 +1791,7 @@ bool tc_chain_layout(TcOffsets& o, bool tma_ok, int conflict_slack, int (*gbits)
     o.direct = 1;
     o.shuffle = 0;
     o.st_box = 0;
+    for (int r = 0; r < 5; ++r) o.wb_xor[r] = best.wxor[r];
     if (store_out) *store_out = best.store;
     if (stores && best.store >= 0) {
         // the last block writes the chosen store box's layout

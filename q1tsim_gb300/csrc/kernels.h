@@ -162,6 +162,13 @@ struct TcOffsets {
     uint32_t sp_athr[7];
     uint32_t sp_achunk[8];
     uint32_t sp_regoff[32];
+    // The last block's write-back with lane-permuted stores (a linear,
+    // unpadded layout only; all zero otherwise): a thread whose lane has
+    // bits r stores, at step j of each half row, its output gate state
+    // j ^ wx, wx = XOR over its lane bits r of wb_xor[r] (gate bits 0-3;
+    // 1-3 where the block stores 16 bytes per step).  Rows whose staged
+    // offsets share banks then store to different banks at every step.
+    uint32_t wb_xor[5];
 };
 // A tile as a box of a rank-5 tensor map over the state: dimensions follow
 // the runs of tile / non-tile positions (tile runs split every 8 positions,

@@ -113,6 +113,54 @@ static int check_scatter(const TcOffsets& o, int k)
     return bad;
 }
 
+// The last block's lane-permuted write-back (TcOffsets::wb_xor), as the
+// kernel computes it: thread t with lane permutation wx stores, at step j of
+// half hh, its output gate state 16 hh + (j ^ wx) at staged byte
+// (row offset ^ gateoff of wx) ^ gateoff[16 hh + j] (pairs of gate states
+// per 16-byte store where vec2).  That must be the state's own staged
+// offset, every (row, state) once; the permutation is zero unless the
+// layout is unpadded, and keeps 16-byte pairs together.
+static int check_wb_xor(const TcOffsets& o, bool* used)
+{
+    const TcBlockGeom& L = o.blk[o.nblocks - 1];
+    uint32_t any = 0;
+    for (int r = 0; r < 5; ++r) any |= o.wb_xor[r];
+    *used = any != 0;
+    if (!any) return 0;
+    int bad = 0;
+    if (o.pad_shift < 31) ++bad;
+    for (int r = 0; r < 5; ++r)
+        if (o.wb_xor[r] >= 16u || (L.vec2 && (o.wb_xor[r] & 1u))) ++bad;
+    std::vector<int> seen(4096, 0);
+    for (uint32_t t = 0; t < 128; ++t) {
+        uint32_t rowb = 0, wx = 0;
+        for (int i = 0; i < 7; ++i)
+            if ((t >> i) & 1u) rowb += L.rowoff[i];
+        for (int r = 0; r < 5; ++r)
+            if ((t >> r) & 1u) wx ^= o.wb_xor[r];
+        uint32_t rowx = rowb;
+        for (int k = 0; k < 4; ++k)
+            if ((wx >> k) & 1u) rowx ^= L.gateoff[1 << k];
+        for (int hh = 0; hh < 2; ++hh)
+            for (int j = 0; j < 16; ++j) {
+                const uint32_t gs = 16u * hh + ((uint32_t)j ^ wx);   // the state stored at step j
+                uint32_t addr;
+                if (L.vec2) {
+                    // step j / 2 stores the pair (2m, 2m+1), m = j / 2
+                    addr = (rowx ^ L.gateoff[16 * hh + (j & ~1)]) + 8u * (uint32_t)(j & 1);
+                } else {
+                    addr = rowx ^ L.gateoff[16 * hh + j];
+                }
+                if (addr != rowb + L.gateoff[gs] || (addr & 7u) || addr / 8u >= 4096u) {
+                    ++bad;
+                    continue;
+                }
+                if (seen[addr / 8u]++) ++bad;
+            }
+    }
+    return bad;
+}
+
 int main()
 {
     std::mt19937 rng(7);
@@ -251,7 +299,7 @@ int main()
         ++singles;
     }
     // chained layouts of the four-group kernel: pairs and triples
-    int chains = 0, chain_free = 0;
+    int chains = 0, chain_free = 0, wb_permuted = 0;
     for (int trial = 0; trial < 900; ++trial) {
         const int nb = 2 + trial % 2;
         std::vector<std::vector<int>> gs(nb);
@@ -303,6 +351,9 @@ int main()
                 if (o.blk[b].gateoff[g] != staged(o.blk[b].jgate[g], o.pad_shift)) ++bad;
         }
         bad += check_split(o);
+        bool permuted = false;
+        bad += check_wb_xor(o, &permuted);
+        wb_permuted += permuted;
         bool free = true;
         for (int k = 0; k + 1 < nb; ++k) {
             bad += check_scatter(o, k);
@@ -400,6 +451,9 @@ int main()
             ++bad;
             continue;
         }
+        bool permuted = false;
+        bad += check_wb_xor(o, &permuted);
+        wb_permuted += permuted;
         if (si >= 0 && o.pad_shift >= 31) {
             ++stored;
             const auto& c = cands[(size_t)si];
@@ -421,7 +475,7 @@ int main()
         }
     }
     std::printf("bad %d trials %d conflict-free scatter %d padded %d singles %d chains %d conflict-free chains %d "
-                "store boxes %d chains with a store box %d\n",
-                bad, trials, minimal, padded, singles, chains, chain_free, boxes, stored);
+                "store boxes %d chains with a store box %d permuted write-backs %d\n",
+                bad, trials, minimal, padded, singles, chains, chain_free, boxes, stored, wb_permuted);
     return bad ? 1 : 0;
 }

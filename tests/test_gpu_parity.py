@@ -734,6 +734,8 @@ def test_short_run_pair_goes_as_one_tensor_map_box(n, first, second):
     (20, [0, 1, 2, 3, 4], [3, 4, 5, 6, 7]),          # top position in the tile
     (16, [0, 5, 10, 14, 15], [2, 3, 4, 5, 12]),      # scattered gate bits
     (18, [13, 14, 15, 16, 17], [4, 5, 6, 7, 8]),     # disjoint blocks
+    (14, [4, 5, 6, 7, 8], [9, 10, 11, 12, 13]),      # second block on the lowest positions: 16-byte stores permuted per lane
+    (16, [6, 7, 8, 9, 10], [3, 11, 12, 13, 14]),     # 8-byte stores permuted per lane
 ])
 @pytest.mark.parametrize("mode", [3, 4])
 def test_direct_pair_is_exact(n, first, second, mode):
@@ -763,6 +765,7 @@ def test_direct_pair_is_exact(n, first, second, mode):
     (20, [[3, 4, 5, 6, 7], [1, 2, 3, 4, 5], [0, 1, 2, 3, 4]]),           # high positions
     (22, [[0, 1, 2, 3, 4], [2, 3, 4, 5, 6], [4, 5, 6, 7, 8]]),            # top positions, runs of 8
     (20, [[0, 4, 8, 2, 6], [1, 3, 5, 7, 8], [2, 4, 6, 7, 5]]),           # scattered gate bits, one box
+    (16, [[6, 7, 8, 9, 10], [8, 9, 10, 11, 12], [11, 12, 13, 14, 15]]),   # last block on the lowest positions
 ])
 def test_direct_triple_is_exact(n, blocks):
     """Three blocks in one pass of the four-group kernel (pair mode 5):
