@@ -326,10 +326,10 @@ int q1g_state_set_wait_limit(q1g_state* s, double seconds);
  * (cudaGetSymbolAddress).  With CUDA's lazy module loading that lookup is what
  * loads the array onto the device, so the first call does take device memory;
  * every GPU keeps the array until the process exits.  Make that first call
- * (nshots = 0 is enough) before handing device memory to a pool, and before
- * any stream capture.  All calls share the one array and it keeps the last
- * call's contents (every call rewrites what it reads), so calls that overlap
- * on the GPU race; serialise them (one stream).  The call is asynchronous on
+ * (nshots = 0 is enough) before handing device memory to a pool.  All calls
+ * share the one array and it keeps the last call's contents (every call
+ * rewrites what it reads), so calls that overlap on the GPU race; serialise
+ * them (one stream).  The call is asynchronous on
  * cuda_stream (NULL: the legacy default stream) and calls no cudaMalloc,
  * cudaFree or other allocating routine. */
 int q1g_sample_shots_noalloc(const void* d_amps, int precision, size_t nr_bits,
