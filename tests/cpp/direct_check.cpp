@@ -10,8 +10,11 @@
 // (single-block passes too): every (thread, register) reads a distinct tile
 // coordinate at its staged offset and stores it where the first block's A
 // operand holds (row, K index 2 g) in the block's new gate order, and the
-// scatter follows that order.  Prints how many layouts have a conflict-free
-// scatter.  Exit status 1 on any failure.
+// scatter follows that order.  For chain layouts whose last block stores
+// lane-permuted (TcOffsets::wb_xor), every (row, gate state) lands once at
+// its own staged offset, and the brick circuit's pair on the lowest
+// positions takes that form at the modelled cost.  Prints how many layouts
+// have a conflict-free scatter.  Exit status 1 on any failure.
 #include <algorithm>
 #include <cstdio>
 #include <random>
@@ -472,6 +475,31 @@ int main()
                     if (off != 8u * e) ++bad;
                 }
             if ((si > 0) != (o.st_box != 0)) ++bad;
+        }
+    }
+    // The brick circuit's pair whose last block is the tile's lowest five
+    // positions (one contiguous tile: 12 positions from 0): every row of
+    // that block starts on the same bank, so row-per-thread 16-byte stores
+    // take 4x the minimum wavefronts.  The chain layout stores them
+    // lane-permuted instead: the scatter and the write-back at the minimum
+    // (64 wavefronts per warp each) plus the three butterflies of 16-byte
+    // stores, unpadded.
+    {
+        TcOffsets o{};
+        o.nblocks = 2;
+        o.run_bits = 12;
+        o.nruns = 1;
+        default_geom(o.blk[0], {3, 4, 5, 6, 7});
+        default_geom(o.blk[1], {0, 1, 2, 3, 4});
+        int gbs[kTcMaxBlocks][5];
+        long cost = 0, ideal = 0;
+        bool permuted = false;
+        if (!tc_chain_layout(o, true, 4, gbs, &cost, &ideal, nullptr, nullptr)) {
+            ++bad;
+        } else {
+            bad += check_wb_xor(o, &permuted);
+            if (!permuted || o.pad_shift < 31 || ideal != 128 || cost != 128 + 3 * 12) ++bad;
+            std::printf("lowest-positions pair: cost %ld of minimum %ld, permuted %d\n", cost, ideal, (int)permuted);
         }
     }
     std::printf("bad %d trials %d conflict-free scatter %d padded %d singles %d chains %d conflict-free chains %d "

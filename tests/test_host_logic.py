@@ -92,7 +92,8 @@ def test_shuffled_pairs_redeal_the_rows(gxx, tmp_path):
 
 def test_direct_pairs_scatter_into_the_operand_layout(gxx, tmp_path):
     out = _run(_link_against_library(gxx, tmp_path, "direct_check"))
-    assert out.startswith("bad 0"), out
+    assert out.splitlines()[-1].startswith("bad 0"), out
+    assert "lowest-positions pair: cost 164 of minimum 128, permuted 1" in out, out
 
 
 def test_batch_warp_tiles(gxx, tmp_path):
