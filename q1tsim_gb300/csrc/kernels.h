@@ -143,6 +143,12 @@ struct TcOffsets {
     // operand in shared memory (plan pair mode 4; stage_bytes a multiple of
     // 1024)
     uint32_t groups;
+    // 1: the storers copy the tile with a second tensor map (TcStoreBox), the
+    // last block's staged offsets following its layout; coordinates as
+    // tshift / tmask
+    uint32_t st_box;
+    uint32_t st_tshift[5];
+    uint32_t st_tmask[5];
     // Four groups: how the first block's split deals the tile to a group's
     // 128 threads (tc_split_map).  Thread t (lane bits 0-4, warp bits 5-6
     // of t) reads its 32 amplitudes at staged offset (sum over t's bits i of
@@ -151,12 +157,6 @@ struct TcOffsets {
     // and stores chunk q of each plane at (XOR over t's bits of sp_athr[i])
     // XOR sp_achunk[q].  sp_vec2: registers 2m, 2m+1 are adjacent in the
     // stage (16-byte loads).
-    // 1: the storers copy the tile with a second tensor map (TcStoreBox), the
-    // last block's staged offsets following its layout; coordinates as
-    // tshift / tmask
-    uint32_t st_box;
-    uint32_t st_tshift[5];
-    uint32_t st_tmask[5];
     uint32_t sp_vec2;
     uint32_t sp_thoff[7];
     uint32_t sp_athr[7];
