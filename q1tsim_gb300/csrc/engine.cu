@@ -621,44 +621,33 @@ void q1g_state::measure_all(const size_t* cbits, size_t ncbits, uint64_t* res, s
     if (!collapse) return;
     // one basis column per distinct (column, outcome), in order: outcomes are
     // sorted within a column, so a column's distinct outcomes are its runs of
-    // equal ones.  A first pass writes the words and counts the runs (about
-    // 10^6 at 30 qubits and 10^6 shots, two for a GHZ state), a second fills
-    // basis/counts sized to that count; their capacity carries over between
-    // runs.
+    // equal ones (about 10^6 at 30 qubits and 10^6 shots, two for a GHZ
+    // state).  One pass writes the words and appends the runs to
+    // basis/counts, whose capacity (up to one entry per shot) carries over
+    // between runs: no second pass, and no zero fill of a resize.
     const uint64_t* h_word = sparse ? nullptr : h_outc + nshots;
     const std::vector<uint64_t> runs(counts.begin(), counts.end());
-    uint64_t m = 0, off = 0;
+    basis.clear();
+    counts.clear();
+    basis.reserve(nshots);
+    counts.reserve(nshots);
+    uint64_t off = 0;
     for (uint64_t c = 0; c < runs.size(); ++c) {
         const uint64_t end = off + runs[c];
         for (uint64_t r = off; r < end; ++r) {
             if (h_word) res[r] = (res[r] & mask) | h_word[r];
-            m += (r == off || h_outc[r] != h_outc[r - 1]) ? 1 : 0;
-        }
-        off = end;
-    }
-    basis.clear();
-    counts.clear();
-    basis.resize(m);
-    counts.resize(m);
-    uint64_t* bp = basis.data();
-    uint64_t* cp = counts.data();
-    uint64_t k = 0;
-    off = 0;
-    for (uint64_t c = 0; c < runs.size(); ++c) {
-        const uint64_t end = off + runs[c];
-        for (uint64_t r = off; r < end; ++r) {
             if (r == off || h_outc[r] != h_outc[r - 1]) {
-                bp[k] = h_outc[r];
-                cp[k] = 0;
-                ++k;
+                basis.push_back(h_outc[r]);
+                counts.push_back(1);
+            } else {
+                ++counts.back();
             }
-            ++cp[k - 1];
         }
         off = end;
     }
     sparse = true;
     norm_pending = false;
-    ncols = m;
+    ncols = basis.size();
     norms.assign(ncols, 1.0);
 }
 
