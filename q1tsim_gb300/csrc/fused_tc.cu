@@ -1102,6 +1102,13 @@ static int phase_wavefronts(const uint32_t* vec, int nbits, int width)
     return m;
 }
 
+// The lane-permuted write-back's register butterflies (4, or 3 with 16-byte
+// stores; all run once any lane permutes), each in wavefront units of one
+// warp: 64 selects a row, measured at about 12 shared-memory wavefronts'
+// worth of pass time (30-qubit brick passes: the four butterflies cost
+// 13 % of a conflict-free pass, a 4x conflicted 16-byte write-back 48 %).
+constexpr long kWbButterflyCost = 12;
+
 // warp_wavefronts of the last block's write-back in a linear layout (tile
 // bit j at element bit sbit[j], or at j when sbit is null) when the stores
 // may be permuted per lane (TcOffsets::wb_xor): lane bit r XORs the stored
@@ -1114,13 +1121,6 @@ static int phase_wavefronts(const uint32_t* vec, int nbits, int width)
 // its row offset does already; the result is kept when it beats no
 // permutation.  gk[i]: tile bit of gate bit i; phi out (zero: none);
 // plain_out: the wavefronts without a permutation.
-// The lane-permuted write-back's register butterflies (4, or 3 with 16-byte
-// stores; all run once any lane permutes), each in wavefront units of one
-// warp: 64 selects a row, measured at about 12 shared-memory wavefronts'
-// worth of pass time (30-qubit brick passes: the four butterflies cost
-// 13 % of a conflict-free pass, a 4x conflicted 16-byte write-back 48 %).
-constexpr long kWbButterflyCost = 12;
-
 int warp_wavefronts_xor(const uint32_t* order, const int* sbit, const int* gk, int width, uint32_t* phi,
                         int* plain_out)
 {
