@@ -1470,7 +1470,8 @@ void tc_split_map(TcOffsets& o, int* gbit0)
             std::memcpy(best_bits, it->second.bits, sizeof(best_bits));
         }
     }
-    for (int ia = 0; ia < 5 && best < 0; ++ia)
+    const bool known = best >= 0;
+    for (int ia = 0; ia < 5 && !known; ++ia)
         for (int ib = ia + 1; ib < 5; ++ib) {
             int g[5] = {gates[ia], gates[ib], 0, 0, 0};
             int c = 2;
