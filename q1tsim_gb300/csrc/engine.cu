@@ -623,14 +623,16 @@ void q1g_state::measure_all(const size_t* cbits, size_t ncbits, uint64_t* res, s
     // sorted within a column, so a column's distinct outcomes are its runs of
     // equal ones (about 10^6 at 30 qubits and 10^6 shots, two for a GHZ
     // state).  One pass writes the words and appends the runs to
-    // basis/counts, whose capacity (up to one entry per shot) carries over
-    // between runs: no second pass, and no zero fill of a resize.
+    // basis/counts, whose capacity carries over between runs: no second
+    // pass, and no zero fill of a resize.  The reservation is capped (2^20
+    // entries, 8 MB each): many shots of few outcomes keep no large buffer,
+    // and more distinct outcomes grow the vectors as they come.
     const uint64_t* h_word = sparse ? nullptr : h_outc + nshots;
     const std::vector<uint64_t> runs(counts.begin(), counts.end());
     basis.clear();
     counts.clear();
-    basis.reserve(nshots);
-    counts.reserve(nshots);
+    basis.reserve(std::min<uint64_t>(nshots, uint64_t(1) << 20));
+    counts.reserve(std::min<uint64_t>(nshots, uint64_t(1) << 20));
     uint64_t off = 0;
     for (uint64_t c = 0; c < runs.size(); ++c) {
         const uint64_t end = off + runs[c];
