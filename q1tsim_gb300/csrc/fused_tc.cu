@@ -1054,33 +1054,6 @@ int warp_wavefronts(const uint32_t* order, uint32_t pad, int width)
     return total;
 }
 
-// warp_wavefronts for a layout that puts tile bit j at element bit sbit[j]
-// (unpadded): 8-byte or 16-byte accesses, lanes = rows with row bit r at
-// tile coordinate order[r].
-int warp_wavefronts_map(const uint32_t* order, const int* sbit, int width)
-{
-    const uint32_t lanes_per_phase = width == 16 ? 8 : 16;
-    const uint32_t wpl = (uint32_t)width / 4;
-    int total = 0;
-    for (uint32_t ph = 0; ph < 32 / lanes_per_phase; ++ph) {
-        uint32_t words[64];
-        uint32_t nw = 0;
-        for (uint32_t l = ph * lanes_per_phase; l < (ph + 1) * lanes_per_phase; ++l) {
-            uint32_t e = 0;
-            for (int r = 0; r < 5; ++r)
-                if ((l >> r) & 1u) e |= 1u << sbit[__builtin_ctz(order[r])];
-            for (uint32_t w = 0; w < wpl; ++w) words[nw++] = 2 * e + w;
-        }
-        std::sort(words, words + nw);
-        int per_bank[32] = {0};
-        int m = 0;
-        for (uint32_t i = 0; i < nw; ++i)
-            if (i == 0 || words[i] != words[i - 1]) m = std::max(m, ++per_bank[words[i] % 32]);
-        total += m;
-    }
-    return total;
-}
-
 // Wavefronts of one phase of lane addresses a(l) = XOR over the lane's bits
 // r < nbits of vec[r] (byte offsets), `width` bytes per lane.
 static int phase_wavefronts(const uint32_t* vec, int nbits, int width)
