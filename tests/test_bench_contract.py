@@ -1,7 +1,8 @@
-"""The bench's reference arm keeps the JSON contract on the CPU: one line
+"""The bench's JSON contract on the CPU. The reference arm prints one line
 with the metric, its unit and direction, `impl: reference`, a cpu_baseline
 describing the run and an e2e object without host-device bytes; ranks other
-than 0 of a multi-process launch exit 0 without work or output."""
+than 0 of a multi-process launch exit 0 without work or output. The clock
+record and the DRAM-traffic lookup the GPU arm adds parse as intended."""
 import json
 import os
 import subprocess
@@ -38,3 +39,30 @@ def test_reference_arm_other_ranks_exit_quietly():
                        env=_env(RANK="1", WORLD_SIZE="2", LOCAL_RANK="1"), cwd=ROOT)
     assert r.returncode == 0, r.stderr[-2000:]
     assert r.stdout.strip() == ""
+
+
+def _bench():
+    sys.path.insert(0, ROOT)
+    import bench
+    return bench
+
+
+def test_clock_summary_reads_median_and_reasons():
+    """nvidia-smi lines (clocks.sm, clocks.max.sm, power, active mask, then the
+    four reasons) become the JSON line's clocks object; unparsable lines are
+    skipped."""
+    s = _bench().ClockSampler(0)
+    s.lines = ["2070, 2070, 910.2, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active",
+               "2055, 2070, 1399.8, 0x0000000000000004, Not Active, Not Active, Not Active, Active",
+               "[N/A], 2070, 0, 0x0, Not Active, Not Active, Not Active, Not Active",
+               "2040, 2070, 1400.0, 0x0000000000000004, Not Active, Not Active, Not Active, Active",
+               "garbage"]
+    assert s.summary() == {"sm_mhz": 2055.0, "sm_max_mhz": 2070.0, "reasons": ["sw_power_cap"], "samples": 3}
+
+
+def test_dram_traffic_table_lookup():
+    b = _bench()
+    assert b.dram_traffic("fused_tc_c64", 30) == 16313143296.0
+    assert b.dram_traffic("fused_tc_c64", 26) == 1019571456.0
+    assert b.dram_traffic("fused_tc_c64", 17) is None
+    assert b.dram_traffic("no_such_kernel", 30) is None
