@@ -165,6 +165,22 @@ def main():
     ccrz = np.eye(8, dtype=complex)
     ccrz[6, 6], ccrz[7, 7] = -i, i
     mat_case("CCRZ", [math.pi], ccrz.tolist(), "src/gates/controlled.rs:599-609")
+    t4 = polar(1.0, math.pi / 4)
+    mat_case("H", [], [[x, x], [x, -x]], "src/gates/hadamard.rs:186-191")
+    mat_case("X", [], [[z, o], [o, z]], "src/gates/x.rs:164-170")
+    mat_case("Y", [], [[z, -i], [i, z]], "src/gates/y.rs:161-167")
+    mat_case("Z", [], [[o, z], [z, -o]], "src/gates/z.rs:152-158")
+    mat_case("I", [], [[o, z], [z, o]], "src/gates/identity.rs:142-148")
+    mat_case("S", [], [[o, z], [z, i]], "src/gates/s.rs:297-308")
+    mat_case("Sdg", [], [[o, z], [z, -i]], "src/gates/s.rs:297-308")
+    mat_case("T", [], [[o, z], [z, t4]], "src/gates/t.rs:246-257")
+    mat_case("Tdg", [], [[o, z], [z, t4.conjugate()]], "src/gates/t.rs:246-257")
+    mat_case("U1", [math.pi / 2], [[o, z], [z, i]], "src/gates/u1.rs:154-161")
+    mat_case("RY", [math.pi / 2], [[x, -x], [x, x]], "src/gates/ry.rs:184-195")
+    mat_case("RY", [math.pi], [[z, -o], [o, z]], "src/gates/ry.rs:184-195")
+    mat_case("Swap", [], [[o, z, z, z], [z, z, o, z], [z, o, z, z], [z, z, z, o]], "src/gates/swap.rs:189-200")
+    mat_case("CY", [], [[o, z, z, z], [z, o, z, z], [z, z, z, -i], [z, z, i, z]], "src/gates/cy.rs:146-159")
+    mat_case("CZ", [], [[o, z, z, z], [z, o, z, z], [z, z, o, z], [z, z, z, -o]], "src/gates/cz.rs:144-156")
 
     # gate_test KATs: the gate applied to every column of a k-qubit state
     ak = []
@@ -194,6 +210,38 @@ def main():
                [[o, z, h, z], [z, z, -h, z], [z, o, h, x], [z, z, -h, -x]],
                [[o, z, h, z], [z, z, -h, z], [z, x, z, z], [z, x, x, o]],
                "src/gates/controlled.rs:611-645")
+    # the one-qubit gates on the 2-row state [[1, 0, x, x], [0, 1, x, -x]]
+    one = [[o, z, x, x], [z, o, x, -x]]
+    apply_case("H", [], MATS["H"], one, [[x, x, o, z], [x, -x, z, o]], "src/gates/hadamard.rs:194-202")
+    apply_case("X", [], MATS["X"], one, [[z, o, x, -x], [o, z, x, x]], "src/gates/x.rs:173-181")
+    apply_case("Y", [], MATS["Y"], one, [[z, -i, -i * x, i * x], [i, z, i * x, i * x]], "src/gates/y.rs:170-179")
+    apply_case("Z", [], [[o, z], [z, -o]], one, [[o, z, x, x], [z, -o, -x, x]], "src/gates/z.rs:161-169")
+    apply_case("S", [], [[o, z], [z, i]], one, [[o, z, x, x], [z, i, x * i, -x * i]], "src/gates/s.rs:311-337")
+    apply_case("Sdg", [], [[o, z], [z, -i]], one, [[o, z, x, x], [z, -i, -x * i, x * i]], "src/gates/s.rs:311-337")
+    apply_case("U1", [math.pi / 4], [[o, z], [z, polar(1.0, math.pi / 4)]], one,
+               [[o, z, x, x], [z, x * (o + i), 0.5 * (o + i), -0.5 * (o + i)]], "src/gates/u1.rs:164-174")
+    apply_case("RY", [math.pi / 2], [[x, -x], [x, x]], one, [[x, -x, z, o], [x, x, o, z]],
+               "src/gates/ry.rs:198-213")
+    # T and Tdg on the top qubit of a 4-row state
+    tq = polar(1.0, math.pi / 4)
+    four = [[o, z, x, h], [z, o, z, -h], [z, z, x, h], [z, z, z, -h]]
+    four = [row + [e] for row, e in zip(four, [z, z, z, o])]
+    apply_case("T", [], [[o, z], [z, tq]], four,
+               [[o, z, x, h, z], [z, o, z, -h, z], [z, z, tq * x, tq * h, z], [z, z, z, -tq * h, tq]],
+               "src/gates/t.rs:260-296")
+    td = tq.conjugate()
+    apply_case("Tdg", [], [[o, z], [z, td]], four,
+               [[o, z, x, h, z], [z, o, z, -h, z], [z, z, td * x, td * h, z], [z, z, z, -td * h, td]],
+               "src/gates/t.rs:260-296")
+    apply_case("Swap", [], [[o, z, z, z], [z, z, o, z], [z, o, z, z], [z, z, z, o]],
+               [[o, z, x, x, x, h, z], [z, o, x, -x, z, -h, z], [z, z, z, z, x, h, o], [z, z, z, z, z, -h, z]],
+               [[o, z, x, x, x, h, z], [z, z, z, z, x, h, o], [z, o, x, -x, z, -h, z], [z, z, z, z, z, -h, z]],
+               "src/gates/swap.rs:203-222")
+    two = [[o, z, h, z], [z, z, -h, z], [z, o, h, x], [z, z, -h, -x]]
+    apply_case("CY", [], [[o, z, z, z], [z, o, z, z], [z, z, z, -i], [z, z, i, z]], two,
+               [[o, z, h, z], [z, z, -h, z], [z, z, h * i, x * i], [z, i, h * i, x * i]], "src/gates/cy.rs:162-183")
+    apply_case("CZ", [], [[o, z, z, z], [z, o, z, z], [z, z, o, z], [z, z, z, -o]], two,
+               [[o, z, h, z], [z, z, -h, z], [z, o, h, x], [z, z, h, x]], "src/gates/cz.rs:159-179")
     apply_case("CCX", [], MATS["CCX"],
                [[o, z, z], [z, z, z], [z, z, z], [z, x, z], [z, z, z], [z, z, z], [z, z, -x], [z, -x, x]],
                [[o, z, z], [z, z, z], [z, z, z], [z, x, z], [z, z, z], [z, z, z], [z, -x, x], [z, z, -x]],
