@@ -182,6 +182,41 @@ def main():
     mat_case("CY", [], [[o, z, z, z], [z, o, z, z], [z, z, z, -i], [z, z, i, z]], "src/gates/cy.rs:146-159")
     mat_case("CZ", [], [[o, z, z, z], [z, o, z, z], [z, z, o, z], [z, z, z, -o]], "src/gates/cz.rs:144-156")
 
+    # compound gates (test_matrix of kron.rs, composite.rs, staticloop.rs):
+    # a spec is {"gate", "params"}, {"kron": [a, b]}, {"composite": name,
+    # "nbits", "ops": [[spec, bits], ...]} or {"loop": count, "body": spec}
+    ck = []
+
+    def g(name, params=()):
+        return {"gate": name, "params": list(params)}
+
+    def compound(spec, expect, source):
+        ck.append({"spec": spec, "expect": enc(expect), "source": source})
+
+    compound({"kron": [g("I"), g("H")]}, [[x, x, z, z], [x, -x, z, z], [z, z, x, x], [z, z, x, -x]],
+             "src/gates/kron.rs:202-235")
+    compound({"kron": [g("H"), g("H")]}, [[h, h, h, h], [h, -h, h, -h], [h, h, -h, -h], [h, -h, -h, h]],
+             "src/gates/kron.rs:202-235")
+    compound({"kron": [g("H"), {"kron": [g("I"), g("H")]}]},
+             [[h, h, z, z, h, h, z, z], [h, -h, z, z, h, -h, z, z], [z, z, h, h, z, z, h, h],
+              [z, z, h, -h, z, z, h, -h], [h, h, z, z, -h, -h, z, z], [h, -h, z, z, -h, h, z, z],
+              [z, z, h, h, z, z, -h, -h], [z, z, h, -h, z, z, -h, h]],
+             "src/gates/kron.rs:202-235")
+    compound({"composite": "CZ", "nbits": 2, "ops": [[g("H"), [1]], [g("CX"), [0, 1]], [g("H"), [1]]]},
+             [[o, z, z, z], [z, o, z, z], [z, z, o, z], [z, z, z, -o]], "src/gates/composite.rs:665-717")
+    compound({"composite": "Inc", "nbits": 2,
+              "ops": [[g("H"), [0]], [g("H"), [1]], [g("CX"), [0, 1]], [g("H"), [1]], [g("H"), [0]],
+                      [g("X"), [1]]]},
+             [[z, z, z, o], [o, z, z, z], [z, o, z, z], [z, z, o, z]], "src/gates/composite.rs:665-717")
+    inc3 = np.roll(np.eye(8, dtype=complex), 1, axis=0)
+    compound({"composite": "Inc", "nbits": 3,
+              "ops": [[g("H"), [0]], [g("H"), [2]], [g("CCX"), [0, 1, 2]], [g("H"), [2]], [g("H"), [1]],
+                      [g("H"), [2]], [g("CX"), [1, 2]], [g("H"), [2]], [g("H"), [0]], [g("H"), [1]],
+                      [g("X"), [2]]]},
+             inc3.tolist(), "src/gates/composite.rs:665-717")
+    compound({"loop": 3, "body": {"composite": "body", "nbits": 1, "ops": [[g("RX", [1.0471975511965976]), [0]]]}},
+             [[z, -i], [-i, z]], "src/gates/staticloop.rs:265-272")
+
     # gate_test KATs: the gate applied to every column of a k-qubit state
     ak = []
 
@@ -260,11 +295,11 @@ def main():
                         [1234, 0.75, 1e-10, 828, 1023], [1_000_000, 0.43, 1e-4, 428158, 431842]],
              "source": "src/stats.rs:38-45"}
 
-    out = {"vectorstate": vs, "matrix": mk, "apply": ak, "bits": bits, "stats": stats}
+    out = {"vectorstate": vs, "matrix": mk, "compound": ck, "apply": ak, "bits": bits, "stats": stats}
     path = os.path.join(HERE, "vectorstate_kats.json")
     with open(path, "w") as f:
         json.dump(out, f, indent=1)
-    print(path, len(vs), len(mk), len(ak))
+    print(path, len(vs), len(mk), len(ck), len(ak))
 
 
 if __name__ == "__main__":

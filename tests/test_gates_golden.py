@@ -14,6 +14,23 @@ def test_matrix_kat(case):
     np.testing.assert_allclose(g.matrix(), dec(case["expect"]), rtol=0, atol=KAT_TOL)
 
 
+def _build(spec):
+    if "gate" in spec:
+        return G.by_name(spec["gate"], spec["params"])
+    if "kron" in spec:
+        return G.Kron(_build(spec["kron"][0]), _build(spec["kron"][1]))
+    if "loop" in spec:
+        return G.Loop("loop", spec["loop"], _build(spec["body"]))
+    return G.Composite(spec["composite"], spec["nbits"], [(_build(op), bits) for op, bits in spec["ops"]])
+
+
+@pytest.mark.parametrize("case", K["compound"], ids=lambda c: c["source"])
+def test_compound_matrix_kat(case):
+    """Kron, Composite and Loop gates built from parts, against the reference's
+    test_matrix known answers."""
+    np.testing.assert_allclose(_build(case["spec"]).matrix(), dec(case["expect"]), rtol=0, atol=KAT_TOL)
+
+
 @pytest.mark.parametrize("case", K["apply"], ids=lambda c: c["gate"] + "@" + c["source"])
 def test_apply_matrix_is_reference_gate(case):
     """The matrices the apply KATs use are the ones gates.py builds."""
